@@ -1,0 +1,396 @@
+"""Benchmark of the deferred-lighting path on GB300.
+
+Workload (the configuration the headline metric is quoted on): one 1920x1080 frame,
+FP16 G-buffer (18 B/px: RGBA16F albedo+roughness, RG16F octahedral normal, R16F
+metallic, R32F depth), 1024 GpuLights (768 point, 256 spot), froxel grid 16x9x24.
+A step is one frame: froxel binning (hl_bin_froxels) + shading (hl_shade) into an
+RGBA32F radiance target. Inputs are seeded synthetic data (helio_gb300.synthetic).
+
+  value   Mpix/s with inputs resident in HBM, L2 flushed (256 MiB write) before every
+          step; each step timed with CUDA events on the launching stream.
+  e2e     the same metric through the C ABI with pinned host buffers: every step
+          copies the G-buffer, lights, camera and globals host->device and the
+          radiance device->host inside the timed region.
+  roofline  the shading kernel (the dominant kernel) against the measured HBM copy
+          bandwidth (MEASURED_PEAKS.json) and the measured FP32 FMA rate
+          (hl_probe_fp32_peak), with algorithmic bytes and FLOPs (include/hl_flops.h).
+  cpu_baseline  the f32 CPU restatement of the same path (OpenMP over rows), full
+          frames on the host's cores.
+
+``--impl reference`` times the CPU restatement of the reference algorithm alone (the
+reference itself is WGSL run by wgpu on a graphics driver, which this machine lacks).
+Multi-GPU: the path does not exchange data between views, so N ranks run N
+independent replicas ("replicas only"); value = pixels of all ranks / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mpix/s lit, 1080p×1024 lights: plain fwd vs batched fwd+adjoint; % roofline"
+WORKLOAD = "w1: 1920x1080 FP16 G-buffer (18 B/px), 1024 GpuLights (768 point + 256 spot), froxels 16x9x24"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def flops_constants():
+    text = (ROOT / "include" / "hl_flops.h").read_text()
+    get = lambda k: int(re.search(rf"#define {k} (\d+)", text).group(1))
+    return get("HL_FLOPS_CULL"), get("HL_FLOPS_FULL"), get("HL_FLOPS_PIXEL")
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (copy bandwidth, measured)"
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+def profile_traffic():
+    """DRAM bytes per shading launch from the committed ncu summary, if present."""
+    p = ROOT / "profiles" / "shade_w1_ncu.md"
+    if not p.exists():
+        return None
+    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", p.read_text())
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [s.strip() for s in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if os.environ.get("HL_BENCH_BACKEND", "nccl") == "nccl" else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(world, v: float) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------------
+# CPU arm (the f32 restatement of the reference algorithm)
+# ----------------------------------------------------------------------------------
+
+
+def cpu_frame_time(w, p, reps):
+    import oracle
+
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        off, idx = oracle.bin_froxels(w.camera.record, w.lights, p, capacity=1 << 22)
+        oracle.shade(w.camera.record, w.globals_, w.gbuffer, w.lights, ("froxels", idx, off, p), precision="f32")
+        times.append(time.perf_counter() - t0)
+    return times
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    import oracle
+    from helio_gb300 import layouts as L
+    from helio_gb300 import synthetic as S
+
+    w = S.workload(1)
+    W, H = w.gbuffer.width, w.gbuffer.height
+    p = L.froxel_params(*w.froxel_grid, W, H, w.camera.far)
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    cpu_frame_time(w, p, max(1, min(args.warmup, 3)))
+    times = cpu_frame_time(w, p, args.steps)
+    t = sum(times) / len(times)
+    v = W * H / t / 1e6
+    line = {
+        "metric": METRIC, "value": round(v, 3), "unit": "Mpix/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": {"workload": WORKLOAD},
+        "cpu_baseline": {"value": round(v, 3), "unit": "Mpix/s", "cores": cores, "kind": "port",
+                         "sample": "full 1920x1080 frames: froxel binning + f32 shading (CPU restatement of "
+                                   "light_cull/deferred_lighting WGSL; the reference's own WGSL needs a graphics "
+                                   "stack, unavailable on this box)"},
+        "e2e": {"value": round(v, 3), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------------
+
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    from helio_gb300 import frame as FR
+    from helio_gb300 import layouts as L
+    from helio_gb300 import native as N
+    from helio_gb300 import synthetic as S
+
+    torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
+    w = S.workload(1)
+    W, H = w.gbuffer.width, w.gbuffer.height
+    p_np = L.froxel_params(*w.froxel_grid, W, H, w.camera.far)
+    fp = N.froxel_params_from_numpy(p_np)
+    F = fp.grid_x * fp.grid_y * fp.grid_z
+    ctx = N.Context(local)
+    df = FR.upload_workload(w, dev)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    offsets = torch.zeros(F + 1, dtype=torch.int32, device=dev)
+    cap = F * 64
+    indices = torch.zeros(cap, dtype=torch.int32, device=dev)
+    target = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
+    grid = N.froxel_grid_struct(indices, offsets, fp, cap)
+    tgt = N.target_struct(target)
+    gbs = df.gbuffer
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def frame():
+        ctx.bin_froxels(df.camera, df.lights, df.n_lights, fp, offsets, indices, cap, sh)
+        ctx.shade(df.camera, df.globals_, gbs, df.lights, df.n_lights, grid, tgt, sh)
+
+    for _ in range(max(3, args.warmup)):
+        frame()
+    ctx.sync_status(sh)
+    total_listed = int(offsets[-1].item())
+
+    # ---------------- device-resident timed loop ----------------
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            ev[k][0].record(stream)
+            ctx.bin_froxels(df.camera, df.lights, df.n_lights, fp, offsets, indices, cap, sh)
+            ev[k][1].record(stream)
+            ctx.shade(df.camera, df.globals_, gbs, df.lights, df.n_lights, grid, tgt, sh)
+            ev[k][2].record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ctx.sync_status(sh)
+    step_ms = [ev[k][0].elapsed_time(ev[k][2]) for k in range(args.steps)]
+    bin_ms = [ev[k][0].elapsed_time(ev[k][1]) for k in range(args.steps)]
+    shade_ms = [ev[k][1].elapsed_time(ev[k][2]) for k in range(args.steps)]
+    t_total = max_over_ranks(world, sum(step_ms) / 1e3)
+    value = W * H * args.steps * world / t_total / 1e6
+    ms_per_step = t_total * 1e3 / args.steps
+    clk = clocks.summary()
+
+    # ---------------- end-to-end through the C ABI with host buffers ----------------
+    host_planes = [FR.plane_tensor(pl, "cpu", pinned=True) for pl in w.gbuffer.planes]
+    host_lights = FR.bytes_tensor(w.lights, "cpu", pinned=True)
+    host_cam = FR.bytes_tensor(w.camera.record, "cpu", pinned=True)
+    host_glb = FR.bytes_tensor(w.globals_, "cpu", pinned=True)
+    host_out = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
+    h2d = sum(t.numel() * t.element_size() for t in host_planes) + host_lights.numel() + host_cam.numel() + host_glb.numel()
+    d2h = host_out.numel() * host_out.element_size()
+
+    def e2e_step():
+        for d, h in zip(df.planes, host_planes):
+            d.copy_(h, non_blocking=True)
+        df.lights.copy_(host_lights, non_blocking=True)
+        df.camera.copy_(host_cam, non_blocking=True)
+        df.globals_.copy_(host_glb, non_blocking=True)
+        frame()
+        host_out.copy_(target, non_blocking=True)
+
+    for _ in range(max(3, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    e_ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        e_ev[k][0].record(stream)
+        e2e_step()
+        e_ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    e2e_t = max_over_ranks(world, sum(e_ev[k][0].elapsed_time(e_ev[k][1]) for k in range(args.steps)) / 1e3)
+    e2e_value = W * H * args.steps * world / e2e_t / 1e6
+    ctx.sync_status(sh)
+
+    # ---------------- roofline of the shading kernel ----------------
+    counts = torch.zeros((H, W, 3), dtype=torch.int32, device=dev)
+    ctx.shade_stats(df.camera, df.globals_, gbs, df.lights, df.n_lights, grid, counts, sh)
+    ctx.sync_status(sh)
+    c = counts.view(-1, 3).to(torch.int64).sum(0).tolist()
+    depth = df.planes[-1]
+    lit = int((depth < 1.0).sum().item())
+    c_cull, c_full, c_px = flops_constants()
+    flops = c[0] * c_cull + c[2] * c_full + lit * c_px
+    bytes_alg = w.gbuffer.bytes_per_pixel * W * H + 16 * lit
+    t_shade = statistics.median(shade_ms) / 1e3
+    hbm_peak, hbm_src = measured_peaks()
+    fp32_peak = ctx.probe_fp32_peak()
+    gbs_ach = bytes_alg / t_shade / 1e9
+    tf_ach = flops / t_shade / 1e12
+    frac_hbm = gbs_ach / hbm_peak
+    frac_fp32 = tf_ach / fp32_peak
+    traffic = profile_traffic()
+    if frac_hbm >= frac_fp32:
+        roof = {"bound": "hbm", "achieved": round(gbs_ach, 1), "peak": hbm_peak, "unit": "GB/s",
+                "frac": round(frac_hbm, 4), "traffic": traffic, "peak_source": hbm_src + ", of measured"}
+    else:
+        roof = {"bound": "fp32", "achieved": round(tf_ach, 3), "peak": round(fp32_peak, 2), "unit": "TFLOP/s",
+                "frac": round(frac_fp32, 4), "traffic": traffic,
+                "peak_source": "hl_probe_fp32_peak FFMA loop, of measured"}
+    roof.update({
+        "kernel": "shade_kernel<F16, froxels>",
+        "kernel_ms": round(t_shade * 1e3, 4),
+        "algorithmic_bytes": int(bytes_alg),
+        "algorithmic_flops": int(flops),
+        "hbm_frac": round(frac_hbm, 4),
+        "fp32_frac": round(frac_fp32, 4),
+        "fp32_peak_tflops": round(fp32_peak, 2),
+        "pairs": {"listed": int(c[0]), "in_range": int(c[1]), "full": int(c[2]), "lit_pixels": lit},
+    })
+
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP16 G-buffer)", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "l2": "flushed before every step (256 MiB write)",
+                   "parallelism": f"replicas x{world}", "froxel_listed": total_listed},
+        "breakdown_ms": {"bin_froxels": round(statistics.median(bin_ms), 4),
+                         "shade": round(statistics.median(shade_ms), 4)},
+        "e2e": {"value": round(e2e_value, 1), "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": 5 * args.steps,
+        "roofline": roof,
+        "clocks": clk,
+    }
+
+    if rank == 0 and not args.no_cpu:
+        import oracle
+        from helio_gb300 import metrics
+
+        cores = os.cpu_count() or 1
+        oracle.set_threads(cores)
+        cpu_frame_time(w, p_np, 1)
+        times = cpu_frame_time(w, p_np, 5)
+        t_cpu = statistics.median(times)
+        line["cpu_baseline"] = {"value": round(W * H / t_cpu / 1e6, 3), "unit": "Mpix/s", "cores": cores,
+                                "kind": "port",
+                                "sample": "5 full 1920x1080 frames, froxel binning + f32 shading, OpenMP over rows"}
+        off_o, idx_o = oracle.bin_froxels(w.camera.record, w.lights, p_np, capacity=1 << 22)
+        ref = oracle.shade(w.camera.record, w.globals_, w.gbuffer, w.lights, ("froxels", idx_o, off_o, p_np))
+        img = target.cpu().numpy()
+        e = metrics.radiance_error(img, ref)
+        off_g = offsets.cpu().numpy().view(np.uint32)
+        line["error_vs_fp64_oracle"] = {k: (round(v, 9) if isinstance(v, float) else v) for k, v in e.items()}
+        line["error_vs_fp64_oracle"]["lists_bit_exact"] = bool(np.array_equal(off_g, off_o))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        # CPU arm: rank 0 alone runs; other ranks exit without work.
+        run_reference(args, int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")))
+        return
+    world, rank, local = dist_setup(args.gpus)
+    run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

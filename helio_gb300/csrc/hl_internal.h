@@ -1,0 +1,52 @@
+// hl_internal.h — launchers shared between the kernel translation units and the
+// C-ABI layer (hl_api.cu). Not part of the public interface.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "../../include/helio_gb300.h"
+
+namespace hl {
+
+struct BinLight;
+struct SliceTable;
+
+// Device view of a G-buffer (validated by the API layer).
+struct GBufView {
+    const unsigned char* plane[HL_GBUF_MAX_PLANES];
+    uint64_t pitch[HL_GBUF_MAX_PLANES];
+    uint32_t width, height;
+};
+
+struct TargetView {
+    unsigned char* data;
+    uint64_t pitch;
+};
+
+struct GridView {
+    const uint32_t* lists;
+    const uint32_t* counts;
+    uint32_t lists_capacity;  // entries in lists
+    uint32_t tiles;           // number of tiles (tile grid)
+    hl_froxel_params fp;      // froxel grid
+};
+
+cudaError_t launch_prep_bin_lights(const void* camera, const void* lights, uint32_t n, bool froxel_margin,
+                                   BinLight* out, cudaStream_t stream);
+cudaError_t launch_bin_tiles_ref(const void* camera, const BinLight* bl, uint32_t n, uint32_t W, uint32_t H,
+                                 uint32_t* lists, uint32_t* counts, cudaStream_t stream);
+cudaError_t launch_bin_froxels(const void* camera, const BinLight* bl, uint32_t n, const hl_froxel_params& p,
+                               const SliceTable& tab, uint32_t* counts_scratch, uint32_t* offsets,
+                               uint32_t* indices, uint32_t capacity, int* status, cudaStream_t stream);
+
+// Shading. layout: HL_GBUF_*, grid_kind: HL_GRID_*, target_format: HL_TARGET_*.
+// stats != nullptr selects the pair-statistics variant (no radiance written).
+cudaError_t launch_shade(uint32_t layout, uint32_t grid_kind, uint32_t target_format, const void* camera,
+                         const void* globals, const GBufView& gb, const void* lights, uint32_t n_lights,
+                         const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats,
+                         int* status, cudaStream_t stream);
+
+cudaError_t run_fp32_probe(int device, double* tflops);
+
+}  // namespace hl

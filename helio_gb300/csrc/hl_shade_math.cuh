@@ -1,0 +1,399 @@
+// hl_shade_math.cuh — f32 per-pixel and per-(pixel, light) shading math of
+// fs_main / pbr_direct_light (deferred_lighting.wgsl:699-820, 991-1259) and
+// pbr_eval.wgsl:6-66, written for accuracy against a float64 evaluation of the same
+// formulas. Compiles as CUDA device code and as plain C++ (host emulation).
+//
+// Accuracy measures (each keeps the result within ~1e-6 relative of the float64
+// evaluation where the reference's own f32 formulation loses digits):
+//  * world position: inv_view_proj * (ndc, depth, 1) as a compensated dot product
+//    (Ogita-Rump-Oishi Dot2) with the pixel-centre NDC carried as a double-float, then
+//    P = h.xyz / h.w kept as hi + lo. At depth ~100 the plain f32 product loses ~1e-4
+//    relative to cancellation in h.w.
+//  * to_light = (light.pos - P.hi) - P.lo, and the range falloff
+//    1 - (d/r)^4 = (r^2 - d^2)(r^2 + d^2)/r^4 with r^2 - d^2 from double-float
+//    squares, so lights near the edge of their range keep their relative accuracy.
+//  * GGX denominator NdH^2 (a^2 - 1) + 1 = |N x H|^2 + a^2 NdH^2 for unit N, H (no
+//    cancellation at the highlight of smooth surfaces).
+// The PRECISE=false variant (FP16 G-buffers, 2e-3 tolerance) skips the first two.
+#pragma once
+
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define HL_HD __host__ __device__ __forceinline__
+#else
+#define HL_HD inline
+#include <cmath>
+#endif
+
+namespace hl {
+namespace sm {
+
+constexpr float kPi = 3.14159265359f;      // pbr_eval.wgsl:6
+constexpr float kInvPi = 1.0f / 3.14159265359f;
+constexpr float kRadianceCut = 0.002f;     // deferred_lighting.wgsl:781
+
+HL_HD float fma_(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, c);
+#else
+    return std::fmaf(a, b, c);
+#endif
+}
+HL_HD float mul_(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+HL_HD float add_(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+HL_HD float div_(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fdiv_rn(a, b);
+#else
+    return a / b;
+#endif
+}
+// Reciprocal and reciprocal square root: correctly rounded reciprocal, hardware rsqrt.
+HL_HD float rcp_(float x) {
+#if defined(__CUDA_ARCH__)
+    return __frcp_rn(x);
+#else
+    return 1.0f / x;
+#endif
+}
+HL_HD float rsqrt_(float x) {
+#if defined(__CUDA_ARCH__)
+    return rsqrtf(x);
+#else
+    return 1.0f / std::sqrt(x);
+#endif
+}
+HL_HD float fmax_(float a, float b) { return a < b ? b : a; }
+HL_HD float fmin_(float a, float b) { return b < a ? b : a; }
+HL_HD float clamp01(float x) { return fmin_(fmax_(x, 0.0f), 1.0f); }
+
+// ---- error-free transformations -------------------------------------------------
+struct DF {
+    float hi, lo;
+};
+HL_HD DF two_sum(float a, float b) {
+    float s = add_(a, b);
+    float bb = add_(s, -a);
+    float e = add_(add_(a, -add_(s, -bb)), add_(b, -bb));
+    return DF{s, e};
+}
+HL_HD DF two_prod(float a, float b) {
+    float p = mul_(a, b);
+    return DF{p, fma_(a, b, -p)};
+}
+
+// ---- per-pixel surface ------------------------------------------------------------
+struct Pixel {
+    float Px, Py, Pz;      // world position (hi)
+    float Plx, Ply, Plz;   // world position (lo)
+    float Nx, Ny, Nz;      // unit normal
+    float Vx, Vy, Vz;      // unit view vector
+    float f0r, f0g, f0b;   // clamped F0
+    float dr, dg, db;      // albedo / pi
+    float rough, metal;
+    float NdV;             // max(dot(N,V), 0)
+    float nrx, nry, nrz;   // normal as stored (before normalisation)
+    float inv_n;           // 1 / |stored normal|
+};
+
+// Derived per-pixel BRDF constants hoisted out of the light loop.
+struct PixelBrdf {
+    float a2;          // roughness^4
+    float k, omk;      // (r+1)^2/8, 1-k
+    float gv;          // Schlick-GGX for the view
+    float one_m_metal;
+    float nv4;         // 4*NdV
+};
+
+HL_HD PixelBrdf pixel_brdf(const Pixel& p) {
+    PixelBrdf b;
+    const float a = p.rough * p.rough;
+    b.a2 = a * a;
+    const float r1 = p.rough + 1.0f;
+    b.k = (r1 * r1) * 0.125f;
+    b.omk = 1.0f - b.k;
+    b.gv = div_(p.NdV, fma_(p.NdV, b.omk, b.k + 0.0001f));
+    b.one_m_metal = 1.0f - p.metal;
+    b.nv4 = 4.0f * p.NdV;
+    return b;
+}
+
+// World position of a pixel centre: inv_view_proj (column major, 16 floats) times
+// (ndc_x, ndc_y, depth, 1), ndc of pixel centre (x+0.5, y+0.5) of a W x H target.
+template <bool PRECISE>
+HL_HD void reconstruct(const float* m, uint32_t x, uint32_t y, float W, float H, float depth, float& Px, float& Py,
+                       float& Pz, float& Plx, float& Ply, float& Plz) {
+    if (!PRECISE) {
+        // uv*2-1 and 1-uv*2 (deferred_lighting.wgsl:1043-1047) with FMA rows.
+        const float ux = div_(float(x) + 0.5f, W), uy = div_(float(y) + 0.5f, H);
+        const float nx = fma_(ux, 2.0f, -1.0f), ny = fma_(uy, -2.0f, 1.0f);
+        float h[4];
+        for (int r = 0; r < 4; ++r) h[r] = fma_(m[8 + r], depth, fma_(m[4 + r], ny, fma_(m[r], nx, m[12 + r])));
+        const float iw = rcp_(h[3]);
+        Px = h[0] * iw;
+        Py = h[1] * iw;
+        Pz = h[2] * iw;
+        Plx = Ply = Plz = 0.0f;
+        return;
+    }
+    // ndc_x = (2x+1)/W - 1 and ndc_y = 1 - (2y+1)/H as double-floats.
+    const float numx = float(2u * x + 1u), numy = float(2u * y + 1u);
+    const float qx = div_(numx, W), qy = div_(numy, H);
+    const float qxl = fma_(-qx, W, numx) * rcp_(W);
+    const float qyl = fma_(-qy, H, numy) * rcp_(H);
+    DF ndx = two_sum(qx, -1.0f);
+    ndx.lo += qxl;
+    DF ndy = two_sum(1.0f, -qy);
+    ndy.lo -= qyl;
+    float hh[4], hl[4];
+    for (int r = 0; r < 4; ++r) {
+        // Dot2 over (m0*ndx.hi, m1*ndy.hi, m2*depth) starting from m3; lo terms added.
+        float p = m[12 + r], s = 0.0f;
+        DF t = two_prod(m[r], ndx.hi);
+        DF u = two_sum(p, t.hi);
+        p = u.hi;
+        s = s + (u.lo + t.lo);
+        t = two_prod(m[4 + r], ndy.hi);
+        u = two_sum(p, t.hi);
+        p = u.hi;
+        s = s + (u.lo + t.lo);
+        t = two_prod(m[8 + r], depth);
+        u = two_sum(p, t.hi);
+        p = u.hi;
+        s = s + (u.lo + t.lo);
+        s = fma_(m[r], ndx.lo, s);
+        s = fma_(m[4 + r], ndy.lo, s);
+        hh[r] = p;
+        hl[r] = s;
+    }
+    const float w = hh[3], wl = hl[3];
+    float* outs[3] = {&Px, &Py, &Pz};
+    float* outl[3] = {&Plx, &Ply, &Plz};
+    const float iw = rcp_(w);
+    for (int r = 0; r < 3; ++r) {
+        const float q = div_(hh[r], w);
+        // residual of (hh + hl) / (w + wl) around q
+        const float res = fma_(-q, w, hh[r]) + fma_(-q, wl, hl[r]);
+        // renormalise so that |lo| <= ulp(hi)/2
+        const DF n = two_sum(q, res * iw);
+        *outs[r] = n.hi;
+        *outl[r] = n.lo;
+    }
+}
+
+// Finishes a Pixel from decoded G-buffer values (albedo, roughness, metallic, raw
+// normal, F0) and the camera position.
+HL_HD void finish_pixel(Pixel& p, float nx, float ny, float nz, float ar, float ag, float ab, float rough, float metal,
+                        float f0r, float f0g, float f0b, float cx, float cy, float cz) {
+    const float in = rsqrt_(fma_(nz, nz, fma_(ny, ny, nx * nx)));
+    p.nrx = nx;
+    p.nry = ny;
+    p.nrz = nz;
+    p.inv_n = in;
+    p.Nx = nx * in;
+    p.Ny = ny * in;
+    p.Nz = nz * in;
+    // V = cam - P as normalised double-floats
+    const DF ux = two_sum(cx, -p.Px), uy = two_sum(cy, -p.Py), uz = two_sum(cz, -p.Pz);
+    const DF vx = two_sum(ux.hi, ux.lo - p.Plx), vy = two_sum(uy.hi, uy.lo - p.Ply), vz = two_sum(uz.hi, uz.lo - p.Plz);
+    const float iv = rsqrt_(fma_(vz.hi, vz.hi, fma_(vy.hi, vy.hi, vx.hi * vx.hi)));
+    p.Vx = vx.hi * iv;
+    p.Vy = vy.hi * iv;
+    p.Vz = vz.hi * iv;
+    // NdV = (n_raw . v) / (|n_raw| |v|) with a compensated dot product: at grazing
+    // view angles the specular term is proportional to NdV.
+    DF d = two_prod(nx, vx.hi);
+    const DF t1 = two_prod(ny, vy.hi), t2 = two_prod(nz, vz.hi);
+    const DF s1 = two_sum(d.hi, t1.hi);
+    const DF s2 = two_sum(s1.hi, t2.hi);
+    float lo = d.lo + t1.lo + t2.lo + s1.lo + s2.lo;
+    lo = fma_(nx, vx.lo, fma_(ny, vy.lo, fma_(nz, vz.lo, lo)));
+    p.NdV = fmax_((s2.hi + lo) * in * iv, 0.0f);
+    p.f0r = fmin_(fmax_(f0r, 0.0f), 0.999f);
+    p.f0g = fmin_(fmax_(f0g, 0.0f), 0.999f);
+    p.f0b = fmin_(fmax_(f0b, 0.0f), 0.999f);
+    p.dr = ar * kInvPi;
+    p.dg = ag * kInvPi;
+    p.db = ab * kInvPi;
+    p.rough = rough;
+    p.metal = metal;
+}
+
+// F0 of the metallic workflow (gbuffer.wgsl:323-328): clamp(mix(0.04, albedo, m), 0, 0.999)
+HL_HD float metallic_f0(float albedo, float metal) { return fma_(albedo, metal, 0.04f * (1.0f - metal)); }
+
+// Octahedral unit-vector decode (Cigolle et al. 2014), z up; not normalised.
+HL_HD void oct_decode(float u, float v, float& x, float& y, float& z) {
+    z = 1.0f - fabsf(u) - fabsf(v);
+    if (z < 0.0f) {
+        const float ox = (1.0f - fabsf(v)) * (u >= 0.0f ? 1.0f : -1.0f);
+        const float oy = (1.0f - fabsf(u)) * (v >= 0.0f ? 1.0f : -1.0f);
+        u = ox;
+        v = oy;
+    }
+    x = u;
+    y = v;
+}
+
+// Light fields used by shading (from a GpuLight, deferred_lighting.wgsl:70-98).
+struct ShadeLight {
+    float px, py, pz, range;
+    float dx, dy, dz, cos_outer;
+    float cr, cg, cb, intensity;
+    uint32_t type;
+    float cos_inner;
+};
+
+// Cheap candidate test of phase 1: inside the range and in front of the surface.
+// Returns true when the pair may contribute; the exact cuts are re-applied by eval.
+HL_HD bool candidate(const Pixel& p, const ShadeLight& l) {
+    if (l.type == 0u) return true;
+    const float tx = (l.px - p.Px) - p.Plx, ty = (l.py - p.Py) - p.Ply, tz = (l.pz - p.Pz) - p.Plz;
+    const float d2 = fma_(tz, tz, fma_(ty, ty, tx * tx));
+    const float ndl = fma_(p.Nz, tz, fma_(p.Ny, ty, p.Nx * tx));
+    return (d2 <= l.range * l.range * 1.00001f) && (ndl > 0.0f);
+}
+
+// Range test of the reference's light loop (deferred_lighting.wgsl:1128-1131).
+HL_HD bool in_range(const Pixel& p, const ShadeLight& l) {
+    if (l.type == 0u) return true;
+    const float tx = (l.px - p.Px) - p.Plx, ty = (l.py - p.Py) - p.Ply, tz = (l.pz - p.Pz) - p.Plz;
+    const float d2 = fma_(tz, tz, fma_(ty, ty, tx * tx));
+    return d2 <= l.range * l.range;
+}
+
+// pbr_direct_light (deferred_lighting.wgsl:699-820) for a non-anisotropic, non-SSS
+// surface, sf = 1. Returns false (and leaves out untouched) when a cut applies.
+template <bool PRECISE>
+HL_HD bool eval(const Pixel& p, const PixelBrdf& b, const ShadeLight& l, float& outr, float& outg, float& outb) {
+    float Lx, Ly, Lz, rr, rg, rb;
+    float NdL;
+    if (l.type == 0u) {
+        const float il = rsqrt_(fma_(l.dz, l.dz, fma_(l.dy, l.dy, l.dx * l.dx)));
+        Lx = -l.dx * il;
+        Ly = -l.dy * il;
+        Lz = -l.dz * il;
+        rr = l.cr * l.intensity;
+        rg = l.cg * l.intensity;
+        rb = l.cb * l.intensity;
+        NdL = fma_(p.Nz, Lz, fma_(p.Ny, Ly, p.Nx * Lx));
+    } else {
+        float tx, ty, tz, d2, fall, ntl = 0.0f;
+        const float r2 = l.range * l.range;
+        if (PRECISE) {
+            // to_light = (light - P.hi) - P.lo as normalised double-floats
+            const DF ux = two_sum(l.px, -p.Px), uy = two_sum(l.py, -p.Py), uz = two_sum(l.pz, -p.Pz);
+            const DF sx = two_sum(ux.hi, ux.lo - p.Plx), sy = two_sum(uy.hi, uy.lo - p.Ply),
+                     sz = two_sum(uz.hi, uz.lo - p.Plz);
+            const float ex = sx.lo, ey = sy.lo, ez = sz.lo;
+            tx = sx.hi;
+            ty = sy.hi;
+            tz = sz.hi;
+            // d^2 = sum (s + e)^2 as a double-float
+            const DF qx = two_prod(sx.hi, sx.hi), qy = two_prod(sy.hi, sy.hi), qz = two_prod(sz.hi, sz.hi);
+            DF acc = two_sum(qx.hi, qy.hi);
+            DF acc2 = two_sum(acc.hi, qz.hi);
+            float lo = acc.lo + acc2.lo + qx.lo + qy.lo + qz.lo;
+            lo = fma_(2.0f * sx.hi, ex, lo);
+            lo = fma_(2.0f * sy.hi, ey, lo);
+            lo = fma_(2.0f * sz.hi, ez, lo);
+            d2 = acc2.hi + lo;
+            // r^2 - d^2 as a double-float difference
+            const DF rr2 = two_prod(l.range, l.range);
+            const DF diff = two_sum(rr2.hi, -acc2.hi);
+            const float gap = diff.hi + (diff.lo + (rr2.lo - lo));
+            if (gap < 0.0f) return false;  // dist > range
+            fall = div_(gap * (r2 + d2), r2 * r2);
+            // n_raw . to_light, compensated: at grazing light angles the diffuse and
+            // specular terms are proportional to NdL.
+            const DF q1 = two_prod(p.nrx, tx), q2 = two_prod(p.nry, ty), q3 = two_prod(p.nrz, tz);
+            const DF c1 = two_sum(q1.hi, q2.hi);
+            const DF c2 = two_sum(c1.hi, q3.hi);
+            float cl = q1.lo + q2.lo + q3.lo + c1.lo + c2.lo;
+            cl = fma_(p.nrx, ex, fma_(p.nry, ey, fma_(p.nrz, ez, cl)));
+            ntl = c2.hi + cl;
+        } else {
+            tx = l.px - p.Px;
+            ty = l.py - p.Py;
+            tz = l.pz - p.Pz;
+            d2 = fma_(tz, tz, fma_(ty, ty, tx * tx));
+            if (d2 > r2) return false;
+            const float nd2 = d2 * rcp_(r2);
+            fall = fmax_(0.0f, fma_(-nd2, nd2, 1.0f));
+        }
+        const float inv_d = rsqrt_(d2);
+        Lx = tx * inv_d;
+        Ly = ty * inv_d;
+        Lz = tz * inv_d;
+        NdL = PRECISE ? ntl * p.inv_n * inv_d : fma_(p.Nz, Lz, fma_(p.Ny, Ly, p.Nx * Lx));
+        float atten = rcp_(d2 + 0.0001f) * fall;
+        if (l.type == 2u) {
+            const float cos_a = -fma_(Lz, l.dz, fma_(Ly, l.dy, Lx * l.dx));
+            const float t = clamp01(div_(cos_a - l.cos_outer, l.cos_inner - l.cos_outer));
+            atten *= t * t * fma_(-2.0f, t, 3.0f);
+        }
+        const float ia = l.intensity * atten;
+        rr = l.cr * ia;
+        rg = l.cg * ia;
+        rb = l.cb * ia;
+    }
+    if (!(NdL > 0.0f)) return false;
+    if (rr < kRadianceCut && rg < kRadianceCut && rb < kRadianceCut) return false;
+    // H = normalize(V + L)
+    const float hx = p.Vx + Lx, hy = p.Vy + Ly, hz = p.Vz + Lz;
+    const float ih = rsqrt_(fma_(hz, hz, fma_(hy, hy, hx * hx)));
+    const float Hx = hx * ih, Hy = hy * ih, Hz = hz * ih;
+    // Fresnel-Schlick
+    const float HdV = fmax_(fma_(Hz, p.Vz, fma_(Hy, p.Vy, Hx * p.Vx)), 0.0f);
+    const float x = clamp01(1.0f - HdV);
+    const float x2 = x * x;
+    const float p5 = x2 * x2 * x;
+    const float Fr = fma_(1.0f - p.f0r, p5, p.f0r);
+    const float Fg = fma_(1.0f - p.f0g, p5, p.f0g);
+    const float Fb = fma_(1.0f - p.f0b, p5, p.f0b);
+    // GGX: NdH^2 (a2 - 1) + 1 = |N x H|^2 + a2 NdH^2
+    const float ndh_raw = fma_(p.Nz, Hz, fma_(p.Ny, Hy, p.Nx * Hx));
+    float den;
+    if (ndh_raw > 0.0f) {
+        const float cx = fma_(p.Ny, Hz, -p.Nz * Hy), cy = fma_(p.Nz, Hx, -p.Nx * Hz), cz = fma_(p.Nx, Hy, -p.Ny * Hx);
+        const float s2 = fma_(cz, cz, fma_(cy, cy, cx * cx));
+        den = fma_(b.a2 * ndh_raw, ndh_raw, s2);
+    } else {
+        den = 1.0f;
+    }
+    const float D = div_(b.a2, fma_(kPi * den, den, 0.0001f));
+    // Smith-Schlick G
+    const float gl = div_(NdL, fma_(NdL, b.omk, b.k + 0.0001f));
+    const float G = b.gv * gl;
+    const float spec = div_(D * G, fma_(b.nv4, NdL, 0.0001f));
+    // (kD * albedo / pi + spec * F) * radiance * NdL
+    const float wr = rr * NdL, wg = rg * NdL, wb = rb * NdL;
+    outr = fma_((1.0f - Fr) * b.one_m_metal, p.dr, spec * Fr) * wr;
+    outg = fma_((1.0f - Fg) * b.one_m_metal, p.dg, spec * Fg) * wg;
+    outb = fma_((1.0f - Fb) * b.one_m_metal, p.db, spec * Fb) * wb;
+    return true;
+}
+
+// Kahan (compensated) accumulation of one channel.
+HL_HD void kahan_add(float& sum, float& comp, float v) {
+    const float y = add_(v, -comp);
+    const float t = add_(sum, y);
+    comp = add_(add_(t, -sum), -y);
+    sum = t;
+}
+
+}  // namespace sm
+}  // namespace hl

@@ -1,0 +1,207 @@
+"""Byte layouts of the reference's GPU structs, as numpy structured dtypes.
+
+These are the contracts at the C-ABI boundary. Each dtype has exactly the size and
+field offsets of the reference's `#[repr(C)]` Rust struct:
+
+- ``GPU_LIGHT``           libhelio/src/light.rs:60-115 (128 B; const-assert at :111)
+- ``GPU_CAMERA``          libhelio/src/camera.rs:12-29 (368 B; column-major matrices
+                          from glam ``to_cols_array``, camera.rs:47-54)
+- ``DEFERRED_GLOBALS``    helio-pass-deferred-light/src/lib.rs:17-52 (112 B; the
+                          96 B in the reference's tests/layout_tests.rs:71 is stale)
+- ``LIGHT_CULL_PARAMS``   helio-pass-light-cull/src/lib.rs:26-35 (32 B)
+- ``GPU_MATERIAL``        libhelio/src/material.rs:231-254 (96 B)
+"""
+from __future__ import annotations
+
+import numpy as np
+
+# LightType discriminants (libhelio/src/light.rs:8-13)
+LIGHT_DIRECTIONAL = 0
+LIGHT_POINT = 1
+LIGHT_SPOT = 2
+LIGHT_AREA = 3
+
+NO_SHADOW = 0xFFFFFFFF  # shadow_index that disables shadow_factor (deferred_lighting.wgsl:459)
+
+TILE_SIZE = 16  # light_cull.wgsl:17
+MAX_LIGHTS_PER_TILE = 64  # light_cull.wgsl:18
+FROXEL_NEAR = 0.5  # prelude.wgsl:195
+
+GPU_LIGHT = np.dtype(
+    [
+        ("position_range", "<f4", (4,)),
+        ("direction_outer", "<f4", (4,)),
+        ("color_intensity", "<f4", (4,)),
+        ("shadow_index", "<u4"),
+        ("light_type", "<u4"),
+        ("inner_angle", "<f4"),
+        ("_pad", "<u4"),
+        ("god_rays_enabled", "<u4"),
+        ("god_rays_density", "<f4"),
+        ("god_rays_weight", "<f4"),
+        ("god_rays_decay", "<f4"),
+        ("god_rays_exposure", "<f4"),
+        ("flare_enabled", "<u4"),
+        ("flare_type", "<u4"),
+        ("flare_intensity", "<f4"),
+        ("flare_scale", "<f4"),
+        ("flare_tint", "<f4", (3,)),
+        ("ies_profile_index", "<i4"),
+        ("light_function_index", "<i4"),
+        ("ies_angle_scale", "<f4"),
+        ("ies_angle_offset", "<f4"),
+    ]
+)
+
+GPU_CAMERA = np.dtype(
+    [
+        ("view", "<f4", (16,)),
+        ("proj", "<f4", (16,)),
+        ("view_proj", "<f4", (16,)),
+        ("inv_view_proj", "<f4", (16,)),
+        ("position_near", "<f4", (4,)),
+        ("forward_far", "<f4", (4,)),
+        ("jitter_frame", "<f4", (4,)),
+        ("prev_view_proj", "<f4", (16,)),
+    ]
+)
+
+DEFERRED_GLOBALS = np.dtype(
+    [
+        ("frame", "<u4"),
+        ("delta_time", "<f4"),
+        ("light_count", "<u4"),
+        ("ambient_intensity", "<f4"),
+        ("ambient_color", "<f4", (4,)),
+        ("rc_world_min", "<f4", (4,)),
+        ("rc_world_max", "<f4", (4,)),
+        ("csm_splits", "<f4", (4,)),
+        ("debug_mode", "<u4"),
+        ("has_rc_gi", "<u4"),
+        ("num_tiles_x", "<u4"),
+        ("reflection_capture_count", "<u4"),
+        ("enable_reflections", "<u4"),
+        ("enable_env_reflections", "<u4"),
+        ("_pad", "<u4", (2,)),
+    ]
+)
+
+LIGHT_CULL_PARAMS = np.dtype(
+    [
+        ("num_tiles_x", "<u4"),
+        ("num_tiles_y", "<u4"),
+        ("num_lights", "<u4"),
+        ("screen_width", "<u4"),
+        ("screen_height", "<u4"),
+        ("_pad", "<u4", (3,)),
+    ]
+)
+
+GPU_MATERIAL = np.dtype(
+    [
+        ("base_color", "<f4", (4,)),
+        ("emissive", "<f4", (4,)),
+        ("roughness_metallic", "<f4", (4,)),
+        ("tex_base_color", "<u4"),
+        ("tex_normal", "<u4"),
+        ("tex_roughness", "<u4"),
+        ("tex_emissive", "<u4"),
+        ("tex_occlusion", "<u4"),
+        ("workflow", "<u4"),
+        ("flags", "<u4"),
+        ("material_class", "<u4"),
+        ("class_params", "<f4", (4,)),
+    ]
+)
+
+FROXEL_PARAMS = np.dtype(
+    [
+        ("grid_x", "<u4"),
+        ("grid_y", "<u4"),
+        ("grid_z", "<u4"),
+        ("width", "<u4"),
+        ("height", "<u4"),
+        ("slice_near", "<f4"),
+        ("slice_far", "<f4"),
+        ("reserved", "<u4"),
+    ]
+)
+
+# CSM split distances written into DeferredGlobals (libhelio/src/shadow.rs:13)
+CSM_SPLITS = (16.0, 80.0, 300.0, 1400.0)
+
+EXPECTED_SIZES = {
+    "GPU_LIGHT": 128,
+    "GPU_CAMERA": 368,
+    "DEFERRED_GLOBALS": 112,
+    "LIGHT_CULL_PARAMS": 32,
+    "GPU_MATERIAL": 96,
+    "FROXEL_PARAMS": 32,
+}
+
+for _name, _size in EXPECTED_SIZES.items():
+    assert globals()[_name].itemsize == _size, (_name, globals()[_name].itemsize)
+
+
+def default_light() -> np.ndarray:
+    """One ``GpuLight`` with the reference's ``Default`` values (light.rs:117-148):
+    a white point light with shadows off and no IES profile or light function."""
+    lt = np.zeros(1, GPU_LIGHT)
+    lt["direction_outer"] = (0.0, -1.0, 0.0, 0.0)
+    lt["color_intensity"] = (1.0, 1.0, 1.0, 1.0)
+    lt["shadow_index"] = NO_SHADOW
+    lt["light_type"] = LIGHT_POINT
+    lt["god_rays_density"] = 1.0
+    lt["god_rays_weight"] = 0.6
+    lt["god_rays_decay"] = 1.0
+    lt["god_rays_exposure"] = 0.7
+    lt["flare_intensity"] = 1.0
+    lt["flare_scale"] = 1.0
+    lt["flare_tint"] = (1.0, 1.0, 1.0)
+    lt["ies_profile_index"] = -1
+    lt["light_function_index"] = -1
+    lt["ies_angle_scale"] = 1.0
+    return lt
+
+
+def make_lights(n: int) -> np.ndarray:
+    """``n`` default lights, to be filled by the caller."""
+    base = default_light()
+    return np.repeat(base, n)
+
+
+def make_globals(
+    num_tiles_x: int,
+    light_count: int,
+    ambient_color=(0.0, 0.0, 0.0),
+    ambient_intensity: float = 0.0,
+    debug_mode: int = 0,
+) -> np.ndarray:
+    """A ``DeferredGlobals`` as DeferredLightPass::prepare fills it
+    (deferred-light/src/lib.rs:836-878) under fallback bindings: no RC GI, no
+    reflections captures. Ambient defaults to black (the bench's metric case); the
+    pass's own fallback is (0.5, 0.5, 0.6) x 1.0."""
+    g = np.zeros(1, DEFERRED_GLOBALS)
+    g["light_count"] = light_count
+    g["ambient_intensity"] = ambient_intensity
+    g["ambient_color"] = (*ambient_color, 1.0)
+    g["csm_splits"] = CSM_SPLITS
+    g["debug_mode"] = debug_mode
+    g["has_rc_gi"] = 0
+    g["num_tiles_x"] = num_tiles_x
+    g["enable_reflections"] = 1
+    g["enable_env_reflections"] = 0
+    return g
+
+
+def froxel_params(grid_x, grid_y, grid_z, width, height, slice_far, slice_near=FROXEL_NEAR) -> np.ndarray:
+    p = np.zeros(1, FROXEL_PARAMS)
+    p["grid_x"], p["grid_y"], p["grid_z"] = grid_x, grid_y, grid_z
+    p["width"], p["height"] = width, height
+    p["slice_near"], p["slice_far"] = slice_near, slice_far
+    return p
+
+
+def tile_grid(width: int, height: int):
+    """(tiles_x, tiles_y) of the reference's 16-pixel tiling (light-cull/src/lib.rs:65-66)."""
+    return (width + TILE_SIZE - 1) // TILE_SIZE, (height + TILE_SIZE - 1) // TILE_SIZE

@@ -1,0 +1,293 @@
+"""ctypes binding of the C ABI (include/helio_gb300.h).
+
+The library ``helio_gb300/_lib/libhelio_gb300.so`` is built by
+``helio_gb300.build``. There is no fallback: if the library is missing or no CUDA
+device is usable, every call raises. Device memory is passed as raw pointers; the
+helpers accept torch CUDA tensors for convenience (``tensor.data_ptr()``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+from . import build as _build
+
+HL_OK = 0
+HL_ERR_INVALID_ARGUMENT = -1
+HL_ERR_LAYOUT = -2
+HL_ERR_SIZE = -3
+HL_ERR_CUDA = -4
+HL_ERR_TIMEOUT = -5
+HL_ERR_CAPACITY = -6
+HL_ERR_DEVICE_BOUNDS = -7
+HL_ERR_NOT_SUPPORTED = -8
+
+GBUF_REFERENCE, GBUF_F32, GBUF_F16 = 0, 1, 2
+GRID_TILES, GRID_FROXELS = 0, 1
+TARGET_RGBA32F, TARGET_RGBA16F = 0, 1
+MAX_PLANES = 6
+
+
+class HelioError(RuntimeError):
+    """A non-OK status returned by the C ABI."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+
+
+class FroxelParams(C.Structure):
+    _fields_ = [
+        ("grid_x", C.c_uint32), ("grid_y", C.c_uint32), ("grid_z", C.c_uint32),
+        ("width", C.c_uint32), ("height", C.c_uint32),
+        ("slice_near", C.c_float), ("slice_far", C.c_float), ("reserved", C.c_uint32),
+    ]
+
+
+class FroxelLists(C.Structure):
+    _fields_ = [("offsets", C.c_void_p), ("indices", C.c_void_p), ("capacity", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class GBuffer(C.Structure):
+    _fields_ = [
+        ("layout", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32), ("reserved", C.c_uint32),
+        ("planes", C.c_void_p * MAX_PLANES), ("pitch", C.c_uint64 * MAX_PLANES),
+    ]
+
+
+class LightGrid(C.Structure):
+    _fields_ = [
+        ("kind", C.c_uint32), ("lists_capacity", C.c_uint32),
+        ("lists", C.c_void_p), ("counts", C.c_void_p), ("froxel", FroxelParams),
+    ]
+
+
+class Target(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("pitch", C.c_uint64), ("format", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class View(C.Structure):
+    _fields_ = [("camera", C.c_void_p), ("gbuffer", GBuffer), ("radiance", Target)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [
+        ("autotune", C.c_uint32), ("grid_x", C.c_uint32), ("grid_y", C.c_uint32), ("grid_z", C.c_uint32),
+        ("cache_path", C.c_char_p),
+    ]
+
+
+EXPORTS = [
+    "hl_abi_version", "hl_status_string", "hl_create", "hl_destroy", "hl_last_error_message", "hl_sync_status",
+    "hl_tile_count", "hl_bin_tiles_ref", "hl_froxel_slice_table", "hl_bin_froxels", "hl_shade", "hl_shade_stats",
+    "hl_shade_adjoint", "hl_batch_plan_create", "hl_batch_execute", "hl_batch_plan_view_grid",
+    "hl_batch_plan_destroy", "hl_probe_fp32_peak",
+]
+
+_lock = threading.Lock()
+_lib = None
+
+
+def lib_path() -> Path:
+    return _build.lib_path()
+
+
+def load(path: Path | None = None):
+    """Load (once) and bind the shared library. Raises if it has not been built."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = Path(path) if path else lib_path()
+        if not p.exists():
+            raise RuntimeError(f"helio_gb300 CUDA library not built: {p} missing (run helio_gb300.build.build())")
+        l = C.CDLL(str(p))
+        _bind(l)
+        if path is None:
+            _lib = l
+        return l
+
+
+def _bind(l):
+    vp, u32, i32 = C.c_void_p, C.c_uint32, C.c_int32
+    P = C.POINTER
+    l.hl_abi_version.restype = u32
+    l.hl_status_string.restype = C.c_char_p
+    l.hl_status_string.argtypes = [i32]
+    l.hl_create.argtypes = [P(vp), C.c_int]
+    l.hl_create.restype = i32
+    l.hl_destroy.argtypes = [vp]
+    l.hl_destroy.restype = i32
+    l.hl_last_error_message.argtypes = [vp]
+    l.hl_last_error_message.restype = C.c_char_p
+    l.hl_sync_status.argtypes = [vp, vp]
+    l.hl_sync_status.restype = i32
+    l.hl_tile_count.argtypes = [u32, u32]
+    l.hl_tile_count.restype = u32
+    l.hl_bin_tiles_ref.argtypes = [vp, vp, vp, u32, u32, u32, vp, vp, vp]
+    l.hl_bin_tiles_ref.restype = i32
+    l.hl_froxel_slice_table.argtypes = [P(FroxelParams), P(C.c_float)]
+    l.hl_froxel_slice_table.restype = i32
+    l.hl_bin_froxels.argtypes = [vp, vp, vp, u32, P(FroxelParams), P(FroxelLists), vp]
+    l.hl_bin_froxels.restype = i32
+    l.hl_shade.argtypes = [vp, vp, vp, P(GBuffer), vp, u32, P(LightGrid), P(Target), vp]
+    l.hl_shade.restype = i32
+    l.hl_shade_stats.argtypes = [vp, vp, vp, P(GBuffer), vp, u32, P(LightGrid), vp, vp]
+    l.hl_shade_stats.restype = i32
+    l.hl_shade_adjoint.argtypes = [vp, vp, vp, P(GBuffer), vp, u32, P(LightGrid), vp, C.c_uint64, vp, vp, vp]
+    l.hl_shade_adjoint.restype = i32
+    l.hl_batch_plan_create.argtypes = [vp, P(View), u32, vp, u32, vp, P(BatchConfig), P(vp), vp]
+    l.hl_batch_plan_create.restype = i32
+    l.hl_batch_execute.argtypes = [vp, vp, vp]
+    l.hl_batch_execute.restype = i32
+    l.hl_batch_plan_view_grid.argtypes = [vp, u32, P(u32)]
+    l.hl_batch_plan_view_grid.restype = i32
+    l.hl_batch_plan_destroy.argtypes = [vp]
+    l.hl_batch_plan_destroy.restype = i32
+    l.hl_probe_fp32_peak.argtypes = [vp, P(C.c_double)]
+    l.hl_probe_fp32_peak.restype = i32
+
+
+def status_string(status: int) -> str:
+    return load().hl_status_string(status).decode()
+
+
+def froxel_params(grid_x, grid_y, grid_z, width, height, slice_far, slice_near=0.5) -> FroxelParams:
+    return FroxelParams(grid_x, grid_y, grid_z, width, height, slice_near, slice_far, 0)
+
+
+def froxel_params_from_numpy(p) -> FroxelParams:
+    r = p[0] if getattr(p, "shape", ()) else p
+    return FroxelParams(int(r["grid_x"]), int(r["grid_y"]), int(r["grid_z"]), int(r["width"]), int(r["height"]),
+                        float(r["slice_near"]), float(r["slice_far"]), 0)
+
+
+def slice_table(params: FroxelParams):
+    out = (C.c_float * (params.grid_z + 1))()
+    st = load().hl_froxel_slice_table(C.byref(params), out)
+    if st != HL_OK:
+        raise HelioError(st, status_string(st))
+    return list(out)
+
+
+def _ptr(x) -> int:
+    if x is None:
+        return 0
+    if isinstance(x, int):
+        return x
+    return int(x.data_ptr())
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        return 0
+    if isinstance(stream, int):
+        return stream
+    return int(stream.cuda_stream)
+
+
+def gbuffer_struct(layout: int, width: int, height: int, planes, pitches=None) -> GBuffer:
+    """``planes``: device tensors (or pointers) in the layout's plane order;
+    ``pitches`` default to the tensors' row strides in bytes."""
+    g = GBuffer()
+    g.layout, g.width, g.height, g.reserved = layout, width, height, 0
+    for i, pl in enumerate(planes):
+        g.planes[i] = _ptr(pl)
+        if pitches is not None:
+            g.pitch[i] = int(pitches[i])
+        else:
+            g.pitch[i] = int(pl.stride(0) * pl.element_size())
+    return g
+
+
+class Context:
+    """Owns an ``hl_ctx``. Methods mirror the C ABI and raise ``HelioError``."""
+
+    def __init__(self, device: int = 0):
+        self._l = load()
+        h = C.c_void_p()
+        st = self._l.hl_create(C.byref(h), device)
+        if st != HL_OK:
+            raise HelioError(st, f"hl_create(device={device}) failed: {status_string(st)}")
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._l.hl_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st: int, what: str):
+        if st != HL_OK:
+            msg = self._l.hl_last_error_message(self._h).decode()
+            raise HelioError(st, f"{what}: {status_string(st)}: {msg}")
+
+    def probe_fp32_peak(self) -> float:
+        """Measured FP32 FMA throughput in TFLOP/s."""
+        v = C.c_double()
+        self._check(self._l.hl_probe_fp32_peak(self._h, C.byref(v)), "hl_probe_fp32_peak")
+        return float(v.value)
+
+    def sync_status(self, stream=None):
+        self._check(self._l.hl_sync_status(self._h, _stream(stream)), "hl_sync_status")
+
+    def bin_tiles_ref(self, camera, lights, n_lights, width, height, tile_lists, tile_counts, stream=None):
+        self._check(self._l.hl_bin_tiles_ref(self._h, _ptr(camera), _ptr(lights), n_lights, width, height,
+                                             _ptr(tile_lists), _ptr(tile_counts), _stream(stream)), "hl_bin_tiles_ref")
+
+    def bin_froxels(self, camera, lights, n_lights, params: FroxelParams, offsets, indices, capacity, stream=None):
+        out = FroxelLists(_ptr(offsets), _ptr(indices), capacity, 0)
+        self._check(self._l.hl_bin_froxels(self._h, _ptr(camera), _ptr(lights), n_lights, C.byref(params),
+                                           C.byref(out), _stream(stream)), "hl_bin_froxels")
+
+    def shade(self, camera, globals_, gbuffer: GBuffer, lights, n_lights, grid: LightGrid, target: Target, stream=None):
+        self._check(self._l.hl_shade(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer), _ptr(lights), n_lights,
+                                     C.byref(grid), C.byref(target), _stream(stream)), "hl_shade")
+
+    def shade_stats(self, camera, globals_, gbuffer: GBuffer, lights, n_lights, grid: LightGrid, counts, stream=None):
+        self._check(self._l.hl_shade_stats(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer), _ptr(lights),
+                                           n_lights, C.byref(grid), _ptr(counts), _stream(stream)), "hl_shade_stats")
+
+    def shade_adjoint(self, camera, globals_, gbuffer: GBuffer, lights, n_lights, grid: LightGrid, d_radiance,
+                      d_radiance_pitch, d_lights, d_pixels, stream=None):
+        self._check(self._l.hl_shade_adjoint(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer), _ptr(lights),
+                                             n_lights, C.byref(grid), _ptr(d_radiance), int(d_radiance_pitch),
+                                             _ptr(d_lights), _ptr(d_pixels), _stream(stream)), "hl_shade_adjoint")
+
+
+def tile_grid_struct(lists, counts) -> LightGrid:
+    g = LightGrid()
+    g.kind, g.lists_capacity, g.lists, g.counts = GRID_TILES, 0, _ptr(lists), _ptr(counts)
+    return g
+
+
+def froxel_grid_struct(indices, offsets, params: FroxelParams, capacity: int = 0) -> LightGrid:
+    g = LightGrid()
+    g.kind, g.lists_capacity, g.lists, g.counts = GRID_FROXELS, capacity, _ptr(indices), _ptr(offsets)
+    g.froxel = params
+    return g
+
+
+def target_struct(data, fmt: int = TARGET_RGBA32F, pitch: int | None = None) -> Target:
+    t = Target()
+    t.data = _ptr(data)
+    t.pitch = int(pitch if pitch is not None else data.stride(0) * data.element_size())
+    t.format = fmt
+    return t

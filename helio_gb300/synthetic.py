@@ -1,0 +1,408 @@
+"""Seeded synthetic scenes for the deferred-lighting path.
+
+The reference benchmarks no public dataset for this path; its inputs are a G-buffer,
+a camera and a light buffer. These generators build those inputs with the shapes and
+value distributions of the five workloads this project measures:
+
+  w0  1280x720  F32 G-buffer,   64 point lights,                      froxels 16x9x24
+  w1  1920x1080 F16 G-buffer, 1024 lights (768 point / 256 spot),     froxels 16x9x24
+  w2  3840x2160 F32 G-buffer, 4096 point lights in 8 Gaussian clumps, froxels 32x18x48
+  w3  98 views (96 cube faces 128^2/256^2/512^2 + 1080p + 720p), F16, 2048 lights
+  w4  1920x1080 F32 G-buffer,  256 point lights, adjoint against perturbed lights
+
+Camera: glam's right-handed look-at and DirectX-convention perspective (NDC z in
+[0,1], near -> 0), as Helio builds it (helio/src/scene/camera.rs:124-125); all
+matrices are formed in float64 and stored as float32, column major.
+
+G-buffer: linear view depth d ~ U[0.5, 100] stored as NDC depth; normal uniform on
+the hemisphere facing the camera; albedo ~ U[0,1]^3; roughness ~ U[0.05, 1];
+metallic in {0, 1} with P(1) = 0.3.
+
+Random numbers come from a counter-based SplitMix64 hash of (seed, stream, index), so
+every array is reproducible element by element on any machine.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import layouts as L
+
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _splitmix64(x: np.ndarray) -> np.ndarray:
+    x = (x + np.uint64(0x9E3779B97F4A7C15)) & _M64
+    z = x
+    z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & _M64
+    z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)) & _M64
+    return z ^ (z >> np.uint64(31))
+
+
+def uniform(seed: int, stream: int, n: int, lo: float = 0.0, hi: float = 1.0) -> np.ndarray:
+    """``n`` float64 values in [lo, hi) from the hash of (seed, stream, index)."""
+    with np.errstate(over="ignore"):
+        base = _splitmix64(np.array([(seed * 0x100000001B3 + stream * 0x9E3779B1) & 0xFFFFFFFFFFFFFFFF], np.uint64))[0]
+        idx = np.arange(n, dtype=np.uint64)
+        h = _splitmix64(idx ^ base)
+    u = (h >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    return lo + (hi - lo) * u
+
+
+# ----------------------------------------------------------------------------------
+# Camera
+# ----------------------------------------------------------------------------------
+
+
+def look_at_rh(eye, target, up) -> np.ndarray:
+    """glam ``look_at_rh`` as a 4x4 float64 matrix (row = math row)."""
+    eye, target, up = (np.asarray(v, np.float64) for v in (eye, target, up))
+    f = target - eye
+    f = f / np.linalg.norm(f)
+    s = np.cross(f, up)
+    s = s / np.linalg.norm(s)
+    u = np.cross(s, f)
+    m = np.eye(4)
+    m[0, :3], m[1, :3], m[2, :3] = s, u, -f
+    m[0, 3], m[1, 3], m[2, 3] = -s @ eye, -u @ eye, f @ eye
+    return m
+
+
+def perspective_rh_dx(fov_y: float, aspect: float, near: float, far: float) -> np.ndarray:
+    """glam ``perspective_rh`` (DirectX depth range) as a 4x4 float64 matrix."""
+    h = math.cos(0.5 * fov_y) / math.sin(0.5 * fov_y)
+    w = h / aspect
+    r = far / (near - far)
+    m = np.zeros((4, 4))
+    m[0, 0], m[1, 1], m[2, 2], m[2, 3], m[3, 2] = w, h, r, r * near, -1.0
+    return m
+
+
+@dataclass
+class Camera:
+    eye: np.ndarray
+    view: np.ndarray  # float64 4x4
+    proj: np.ndarray
+    near: float
+    far: float
+    width: int
+    height: int
+    fov_y: float
+    record: np.ndarray = field(repr=False)  # GPU_CAMERA, shape (1,)
+
+    @property
+    def inv_view_proj(self) -> np.ndarray:
+        return np.linalg.inv(self.proj @ self.view)
+
+    def bytes(self) -> bytes:
+        return self.record.tobytes()
+
+
+def _cols(m: np.ndarray) -> np.ndarray:
+    return m.T.reshape(16).astype(np.float32)
+
+
+def make_camera(eye, target, up, fov_y_deg, width, height, near=0.1, far=100.0) -> Camera:
+    view = look_at_rh(eye, target, up)
+    proj = perspective_rh_dx(math.radians(fov_y_deg), width / height, near, far)
+    vp = proj @ view
+    rec = np.zeros(1, L.GPU_CAMERA)
+    rec["view"] = _cols(view)
+    rec["proj"] = _cols(proj)
+    rec["view_proj"] = _cols(vp)
+    rec["inv_view_proj"] = _cols(np.linalg.inv(vp))
+    eye = np.asarray(eye, np.float64)
+    fwd = np.asarray(target, np.float64) - eye
+    fwd = fwd / np.linalg.norm(fwd)
+    rec["position_near"] = (*eye, near)
+    rec["forward_far"] = (*fwd, far)
+    rec["jitter_frame"] = (0.0, 0.0, 0.0, 0.0)
+    rec["prev_view_proj"] = _cols(vp)
+    return Camera(eye, view, proj, near, far, width, height, math.radians(fov_y_deg), rec)
+
+
+def default_camera(width: int, height: int, fov_y_deg: float = 60.0) -> Camera:
+    """Eye at the origin looking down -Z, up +Y, near 0.1, far 100."""
+    return make_camera((0, 0, 0), (0, 0, -1), (0, 1, 0), fov_y_deg, width, height)
+
+
+CUBE_FACES = (  # (forward, up) per face, +X -X +Y -Y +Z -Z
+    ((1, 0, 0), (0, -1, 0)),
+    ((-1, 0, 0), (0, -1, 0)),
+    ((0, 1, 0), (0, 0, 1)),
+    ((0, -1, 0), (0, 0, -1)),
+    ((0, 0, 1), (0, -1, 0)),
+    ((0, 0, -1), (0, -1, 0)),
+)
+
+
+def cube_face_camera(center, face: int, size: int) -> Camera:
+    f, up = CUBE_FACES[face]
+    c = np.asarray(center, np.float64)
+    return make_camera(c, c + np.asarray(f, np.float64), up, 90.0, size, size)
+
+
+# ----------------------------------------------------------------------------------
+# Half floats, octahedral normals
+# ----------------------------------------------------------------------------------
+
+
+def oct_encode(n: np.ndarray) -> np.ndarray:
+    """Octahedral encoding of unit vectors (Cigolle et al. 2014), z up; (..., 2)."""
+    a = np.abs(n).sum(-1, keepdims=True)
+    p = n[..., :2] / a
+    neg = n[..., 2] < 0
+    sgn = np.where(p >= 0, 1.0, -1.0)
+    q = (1.0 - np.abs(p[..., ::-1])) * sgn
+    return np.where(neg[..., None], q, p)
+
+
+def oct_decode(e: np.ndarray) -> np.ndarray:
+    x, y = e[..., 0].astype(np.float64), e[..., 1].astype(np.float64)
+    z = 1.0 - np.abs(x) - np.abs(y)
+    neg = z < 0
+    ox = (1.0 - np.abs(y)) * np.where(x >= 0, 1.0, -1.0)
+    oy = (1.0 - np.abs(x)) * np.where(y >= 0, 1.0, -1.0)
+    x = np.where(neg, ox, x)
+    y = np.where(neg, oy, y)
+    n = np.stack([x, y, z], -1)
+    return n / np.linalg.norm(n, axis=-1, keepdims=True)
+
+
+# ----------------------------------------------------------------------------------
+# G-buffers
+# ----------------------------------------------------------------------------------
+
+
+@dataclass
+class GBuffer:
+    layout: int  # 0 reference, 1 F32, 2 F16
+    width: int
+    height: int
+    planes: list  # numpy arrays, each (H, W, C) or (H, W)
+    # float64 ground truth of the generated surface (before storage rounding)
+    truth: dict = field(default_factory=dict, repr=False)
+
+    @property
+    def bytes_per_pixel(self) -> int:
+        return sum(p.dtype.itemsize * (p.shape[2] if p.ndim == 3 else 1) for p in self.planes)
+
+
+LAYOUT_REFERENCE, LAYOUT_F32, LAYOUT_F16 = 0, 1, 2
+
+
+def _surface(cam: Camera, seed: int):
+    W, H = cam.width, cam.height
+    n = W * H
+    d = uniform(seed, 1, n, 0.5, 100.0)
+    near, far = cam.near, cam.far
+    z = (far / (far - near)) * (1.0 - near / d)
+    depth = z.astype(np.float32)
+    # view direction of each pixel centre (float64) to orient the hemisphere
+    xs = (np.arange(W) + 0.5) / W * 2.0 - 1.0
+    ys = 1.0 - (np.arange(H) + 0.5) / H * 2.0
+    X, Y = np.meshgrid(xs, ys)
+    inv = cam.inv_view_proj
+    h = np.stack([X.ravel(), Y.ravel(), depth.astype(np.float64), np.ones(n)], 0)
+    wp = inv @ h
+    P = (wp[:3] / wp[3]).T
+    V = cam.eye[None, :] - P
+    V /= np.linalg.norm(V, axis=1, keepdims=True)
+    u1 = uniform(seed, 2, n)
+    u2 = uniform(seed, 3, n)
+    zc = 1.0 - 2.0 * u1
+    r = np.sqrt(np.maximum(0.0, 1.0 - zc * zc))
+    phi = 2.0 * math.pi * u2
+    N = np.stack([r * np.cos(phi), r * np.sin(phi), zc], 1)
+    flip = (N * V).sum(1) < 0
+    N[flip] *= -1.0
+    albedo = np.stack([uniform(seed, 4, n), uniform(seed, 5, n), uniform(seed, 6, n)], 1)
+    rough = uniform(seed, 7, n, 0.05, 1.0)
+    metal = (uniform(seed, 8, n) < 0.3).astype(np.float64)
+    return depth.reshape(H, W), N.reshape(H, W, 3), albedo.reshape(H, W, 3), rough.reshape(H, W), metal.reshape(H, W)
+
+
+def make_gbuffer(cam: Camera, layout: int, seed: int) -> GBuffer:
+    depth, N, albedo, rough, metal = _surface(cam, seed)
+    W, H = cam.width, cam.height
+    truth = dict(depth=depth, normal=N, albedo=albedo, roughness=rough, metallic=metal)
+    if layout == LAYOUT_F32:
+        p0 = np.concatenate([albedo, rough[..., None]], -1).astype(np.float32)
+        p1 = np.concatenate([N, metal[..., None]], -1).astype(np.float32)
+        planes = [np.ascontiguousarray(p0), np.ascontiguousarray(p1), np.ascontiguousarray(depth)]
+    elif layout == LAYOUT_F16:
+        p0 = np.concatenate([albedo, rough[..., None]], -1).astype(np.float16)
+        p1 = oct_encode(N).astype(np.float16)
+        p2 = metal.astype(np.float16)
+        planes = [np.ascontiguousarray(p0), np.ascontiguousarray(p1), np.ascontiguousarray(p2), np.ascontiguousarray(depth)]
+    elif layout == LAYOUT_REFERENCE:
+        f0 = np.clip(0.04 * (1.0 - metal[..., None]) + albedo * metal[..., None], 0.0, 0.999)
+        u8 = lambda v: np.clip(np.rint(v * 255.0), 0, 255).astype(np.uint8)
+        a = np.concatenate([u8(albedo), np.full((H, W, 1), 255, np.uint8)], -1)
+        nrm = np.concatenate([N, f0[..., :1]], -1).astype(np.float16)
+        orm = np.stack([np.full((H, W), 255, np.uint8), u8(rough), u8(metal), u8(f0[..., 1])], -1)
+        emi = np.concatenate([np.zeros((H, W, 3)), f0[..., 2:3]], -1).astype(np.float16)
+        planes = [a, nrm, orm, emi, np.ascontiguousarray(depth)]
+    else:
+        raise ValueError(f"unknown layout {layout}")
+    return GBuffer(layout, W, H, planes, truth)
+
+
+# ----------------------------------------------------------------------------------
+# Lights
+# ----------------------------------------------------------------------------------
+
+
+def _frustum_points(cam: Camera, seed: int, stream: int, n: int) -> np.ndarray:
+    """``n`` world points uniform in the camera frustum volume (rejection sampling in
+    the view-space bounding box)."""
+    ty = math.tan(0.5 * cam.fov_y)
+    tx = ty * cam.width / cam.height
+    far, near = cam.far, cam.near
+    out = []
+    got, batch, k = 0, max(4 * n, 64), 0
+    while got < n:
+        u = uniform(seed, stream * 1000 + 3 * k, batch, -1.0, 1.0)
+        v = uniform(seed, stream * 1000 + 3 * k + 1, batch, -1.0, 1.0)
+        w = uniform(seed, stream * 1000 + 3 * k + 2, batch, near, far)
+        x, y, zd = u * far * tx, v * far * ty, w
+        ok = (np.abs(x) <= zd * tx) & (np.abs(y) <= zd * ty)
+        pts = np.stack([x[ok], y[ok], -zd[ok], np.ones(ok.sum())], 1)
+        out.append(pts)
+        got += len(pts)
+        k += 1
+    vs = np.concatenate(out)[:n]
+    inv_view = np.linalg.inv(cam.view)
+    return (inv_view @ vs.T).T[:, :3]
+
+
+def _unit_vectors(seed: int, stream: int, n: int) -> np.ndarray:
+    zc = uniform(seed, stream, n, -1.0, 1.0)
+    phi = uniform(seed, stream + 1, n, 0.0, 2.0 * math.pi)
+    r = np.sqrt(np.maximum(0.0, 1.0 - zc * zc))
+    return np.stack([r * np.cos(phi), r * np.sin(phi), zc], 1)
+
+
+def make_lights(
+    cam: Camera,
+    seed: int,
+    n_point: int,
+    n_spot: int = 0,
+    radius=(1.0, 10.0),
+    intensity=(0.5, 5.0),
+    clumps: int = 0,
+    clump_sigma: float = 5.0,
+) -> np.ndarray:
+    """A ``GpuLight`` array: point and spot lights (spots spread through the index
+    order by a seeded permutation), shadows off, no IES, no light function."""
+    n = n_point + n_spot
+    lt = L.make_lights(n)
+    if clumps:
+        centres = _frustum_points(cam, seed, 10, clumps)
+        which = np.minimum((uniform(seed, 11, n) * clumps).astype(np.int64), clumps - 1)
+        g = np.stack([uniform(seed, 12 + a, n) for a in range(6)], 1)
+        # Box-Muller: three normals from six uniforms
+        u1 = np.maximum(g[:, 0:3], 1e-300)
+        u2 = g[:, 3:6]
+        gauss = np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * math.pi * u2)
+        pos = centres[which] + clump_sigma * gauss
+    else:
+        pos = _frustum_points(cam, seed, 20, n)
+    rng = uniform(seed, 30, n, *radius)
+    inten = uniform(seed, 31, n, *intensity)
+    col = np.stack([uniform(seed, 32, n), uniform(seed, 33, n), uniform(seed, 34, n)], 1)
+    types = np.full(n, L.LIGHT_POINT, np.uint32)
+    if n_spot:
+        order = np.argsort(uniform(seed, 35, n), kind="stable")
+        types[order[:n_spot]] = L.LIGHT_SPOT
+    dirs = _unit_vectors(seed, 36, n)
+    outer = np.radians(uniform(seed, 38, n, 10.0, 45.0))
+    inner = 0.75 * outer
+    lt["position_range"][:, :3] = pos
+    lt["position_range"][:, 3] = rng
+    lt["color_intensity"][:, :3] = col
+    lt["color_intensity"][:, 3] = inten
+    lt["light_type"] = types
+    spot = types == L.LIGHT_SPOT
+    lt["direction_outer"][spot, :3] = dirs[spot]
+    lt["direction_outer"][spot, 3] = np.cos(outer[spot])
+    lt["inner_angle"][spot] = np.cos(inner[spot])
+    return lt
+
+
+# ----------------------------------------------------------------------------------
+# Workloads
+# ----------------------------------------------------------------------------------
+
+
+@dataclass
+class Workload:
+    name: str
+    camera: Camera
+    gbuffer: GBuffer
+    lights: np.ndarray
+    globals_: np.ndarray
+    froxel_grid: tuple
+
+
+def workload(index: int, scale: float = 1.0) -> Workload:
+    """The single-view workloads w0, w1, w2, w4 (w3 is ``batched_views``). ``scale``
+    shrinks the resolution for quick tests while keeping every distribution."""
+    specs = {
+        0: dict(W=1280, H=720, layout=LAYOUT_F32, n_point=64, n_spot=0, grid=(16, 9, 24), radius=(1.0, 10.0), clumps=0),
+        1: dict(W=1920, H=1080, layout=LAYOUT_F16, n_point=768, n_spot=256, grid=(16, 9, 24), radius=(1.0, 10.0), clumps=0),
+        2: dict(W=3840, H=2160, layout=LAYOUT_F32, n_point=4096, n_spot=0, grid=(32, 18, 48), radius=(0.5, 20.0), clumps=8),
+        4: dict(W=1920, H=1080, layout=LAYOUT_F32, n_point=256, n_spot=0, grid=(16, 9, 24), radius=(1.0, 10.0), clumps=0),
+    }
+    s = specs[index]
+    W, H = max(16, int(round(s["W"] * scale))), max(16, int(round(s["H"] * scale)))
+    cam = default_camera(W, H)
+    gb = make_gbuffer(cam, s["layout"], seed=index * 1000)
+    lights = make_lights(cam, index * 1000 + 500, s["n_point"], s["n_spot"], radius=s["radius"], clumps=s["clumps"])
+    tx, _ = L.tile_grid(W, H)
+    glb = L.make_globals(tx, len(lights))
+    return Workload(f"w{index}", cam, gb, lights, glb, s["grid"])
+
+
+def perturbed_lights(lights: np.ndarray, seed: int, sigma: float = 0.5, lo: float = 0.8, hi: float = 1.2) -> np.ndarray:
+    """Target lights of the adjoint workload: position + N(0, sigma^2) per axis and
+    intensity x U[lo, hi]."""
+    n = len(lights)
+    out = lights.copy()
+    g = np.stack([uniform(seed, 60 + a, n) for a in range(6)], 1)
+    gauss = np.sqrt(-2.0 * np.log(np.maximum(g[:, :3], 1e-300))) * np.cos(2.0 * math.pi * g[:, 3:])
+    out["position_range"][:, :3] += (sigma * gauss).astype(np.float32)
+    out["color_intensity"][:, 3] *= uniform(seed, 70, n, lo, hi).astype(np.float32)
+    return out
+
+
+@dataclass
+class View:
+    camera: Camera
+    gbuffer: GBuffer
+
+
+def batched_views(scale: float = 1.0, layout: int = LAYOUT_F16):
+    """Workload w3: 16 probes x 6 cube faces (probes 0-5 at 128^2, 6-10 at 256^2,
+    11-15 at 512^2) plus a 1920x1080 and a 1280x720 viewport, sharing 2048 lights
+    (3 point : 1 spot) placed in the 1080p viewport's frustum. Probe centres are
+    uniform in that frustum as well."""
+    main = default_camera(max(16, int(1920 * scale)), max(16, int(1080 * scale)))
+    lights = make_lights(main, 3500, 1536, 512)
+    centres = _frustum_points(main, 3000, 40, 16)
+    views = []
+    vi = 0
+    for p in range(16):
+        size = 128 if p < 6 else (256 if p < 11 else 512)
+        size = max(16, int(size * scale))
+        for f in range(6):
+            cam = cube_face_camera(centres[p], f, size)
+            views.append(View(cam, make_gbuffer(cam, layout, seed=3000 + vi)))
+            vi += 1
+    for (w, h) in ((1920, 1080), (1280, 720)):
+        cam = default_camera(max(16, int(w * scale)), max(16, int(h * scale)))
+        views.append(View(cam, make_gbuffer(cam, layout, seed=3000 + vi)))
+        vi += 1
+    return views, lights

@@ -1,0 +1,292 @@
+/*
+ * helio_gb300.h — C ABI of the GB300 (sm_103a) deferred-lighting engine.
+ *
+ * This library replaces the two passes on Helio's deferred-lighting path:
+ *
+ *   LightCullPass     crates/passes/3d/helio-pass-light-cull/src/lib.rs:41-362
+ *                     + shaders/light_cull.wgsl:123-180
+ *   DeferredLightPass crates/passes/3d/helio-pass-deferred-light/src/lib.rs:110-1199
+ *                     + shaders/deferred_lighting.wgsl:699-820,991-1259
+ *
+ * Conventions
+ *   - Every pointer named as "device" is a CUDA device pointer owned by the caller.
+ *     Byte layouts are Helio's: GpuLight (128 B, libhelio/src/light.rs:60-115),
+ *     GpuCameraUniforms (368 B, libhelio/src/camera.rs:12-29), DeferredGlobals
+ *     (112 B, helio-pass-deferred-light/src/lib.rs:17-52).
+ *   - `stream` is a cudaStream_t passed as void* (0 = legacy default stream).
+ *     All work is enqueued asynchronously on it.
+ *   - Argument errors are returned synchronously. Device-side conditions (an
+ *     out-of-range light index, froxel index capacity exceeded, a bounded wait that
+ *     gave up) raise a flag in the context that hl_sync_status() reports.
+ *   - One hl_ctx is not reentrant: calls on one context must come from one host
+ *     thread at a time (the reference's frame is single threaded,
+ *     helio-core/src/context.rs:13-15). Different contexts are independent.
+ *   - No function falls back to the CPU. Without a usable GPU, hl_create fails.
+ */
+#ifndef HELIO_GB300_H
+#define HELIO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HL_ABI_VERSION 1u
+
+/* Reference constants (light_cull.wgsl:17-18, deferred_lighting.wgsl:199-200). */
+#define HL_TILE_SIZE 16u
+#define HL_MAX_LIGHTS_PER_TILE 64u
+/* Froxel slice-mapping near plane (helio-core/src/shader/prelude.wgsl:195). */
+#define HL_FROXEL_NEAR 0.5f
+
+/* Byte sizes of the reference's POD structs. */
+#define HL_SIZEOF_GPU_LIGHT 128u
+#define HL_SIZEOF_GPU_CAMERA 368u
+#define HL_SIZEOF_DEFERRED_GLOBALS 112u
+#define HL_SIZEOF_LIGHT_CULL_PARAMS 32u
+#define HL_SIZEOF_GPU_MATERIAL 96u
+
+typedef int32_t hl_status;
+#define HL_OK 0
+#define HL_ERR_INVALID_ARGUMENT (-1) /* null pointer, zero-sized grid, bad enum     */
+#define HL_ERR_LAYOUT (-2)           /* misaligned pointer or pitch for the layout  */
+#define HL_ERR_SIZE (-3)             /* a size beyond the limits the kernels support */
+#define HL_ERR_CUDA (-4)             /* a CUDA runtime call failed                  */
+#define HL_ERR_TIMEOUT (-5)          /* a bounded device-side wait gave up          */
+#define HL_ERR_CAPACITY (-6)         /* froxel index buffer too small               */
+#define HL_ERR_DEVICE_BOUNDS (-7)    /* a device-side bounds check rejected an index */
+#define HL_ERR_NOT_SUPPORTED (-8)    /* valid request this build does not implement */
+
+typedef struct hl_ctx hl_ctx;
+
+/* ---------------------------------------------------------------------------------
+ * Context
+ * -------------------------------------------------------------------------------*/
+
+/* Library ABI version (HL_ABI_VERSION of the build). */
+uint32_t hl_abi_version(void);
+
+/* Human-readable text for a status code. Never NULL. */
+const char* hl_status_string(hl_status status);
+
+/* Creates a context bound to `cuda_device`. Holds scratch memory, the device-side
+ * status word and cached batch plans. Replaces the per-pass GPU state the reference
+ * keeps in LightCullPass / DeferredLightPass (light-cull/src/lib.rs:41-61,
+ * deferred-light/src/lib.rs:54-108). */
+hl_status hl_create(hl_ctx** out_ctx, int cuda_device);
+
+/* Frees everything the context owns. NULL is accepted. */
+hl_status hl_destroy(hl_ctx* ctx);
+
+/* Message of the last error recorded on this context ("" if none). */
+const char* hl_last_error_message(const hl_ctx* ctx);
+
+/* Synchronises `stream`, reads and clears the context's device-side status word and
+ * returns it (HL_OK, HL_ERR_CAPACITY, HL_ERR_DEVICE_BOUNDS or HL_ERR_TIMEOUT). */
+hl_status hl_sync_status(hl_ctx* ctx, void* stream);
+
+/* ---------------------------------------------------------------------------------
+ * Tile light culling — the reference's LightCullPass
+ * -------------------------------------------------------------------------------*/
+
+/* Number of 16-pixel tiles of a width x height target, ceil(w/16)*ceil(h/16)
+ * (light-cull/src/lib.rs:65-69). Returns 0 on overflow. */
+uint32_t hl_tile_count(uint32_t width, uint32_t height);
+
+/* Bins lights into 16x16-pixel screen tiles exactly like light_cull.wgsl:123-180:
+ * four lateral planes per tile, sphere test in view space, directional lights always
+ * listed, at most 64 lights per tile in ascending light index (the 65th and later are
+ * dropped). Output buffers have the reference's shapes: tile_lists[tiles*64] (slot
+ * tile*64+i) and tile_counts[tiles]. With n_lights == 0 both buffers are cleared, as
+ * LightCullPass::execute does (light-cull/src/lib.rs:285-292).
+ *   camera : device, GpuCameraUniforms (only view and proj are read)
+ *   lights : device, GpuLight[n_lights]
+ * Replaces: LightCullPass::prepare + execute (light-cull/src/lib.rs:264-362). */
+hl_status hl_bin_tiles_ref(hl_ctx* ctx, const void* camera, const void* lights, uint32_t n_lights,
+                           uint32_t width, uint32_t height, uint32_t* tile_lists,
+                           uint32_t* tile_counts, void* stream);
+
+/* ---------------------------------------------------------------------------------
+ * Froxel light clustering (no reference kernel; slice convention of
+ * helio-core/src/shader/prelude.wgsl:185-211)
+ * -------------------------------------------------------------------------------*/
+
+typedef struct hl_froxel_params {
+    uint32_t grid_x, grid_y, grid_z; /* froxel grid                              */
+    uint32_t width, height;          /* viewport in pixels                       */
+    float slice_near;                /* first exponential slice boundary (0.5)   */
+    float slice_far;                 /* last slice boundary, usually camera far  */
+    uint32_t reserved;               /* must be 0                                */
+} hl_froxel_params;
+
+typedef struct hl_froxel_lists {
+    uint32_t* offsets; /* device, F+1 entries, F = grid_x*grid_y*grid_z; offsets[F] = total */
+    uint32_t* indices; /* device, `capacity` entries                                        */
+    uint32_t capacity;
+    uint32_t reserved;
+} hl_froxel_lists;
+
+/* Host helper: the f32 view-depth boundaries of the grid's slices, grid_z+1 values.
+ * With F = max(slice_far, 2*slice_near): out[0] = 0 (slice 0 also holds everything
+ * nearer than slice_near), out[k] = slice_near*(F/slice_near)^(k/grid_z) for
+ * 0<k<grid_z (prelude.wgsl:202-211), out[grid_z] = F. Pixels beyond F fall in the last
+ * slice, whose box reaches to max(F, camera far). Computed in double and rounded to
+ * f32; binning and shading both use exactly these values. */
+hl_status hl_froxel_slice_table(const hl_froxel_params* params, float* out_host);
+
+/* Clusters lights into froxels. A froxel (fx,fy,s) is the view-space box spanned by
+ * the pixel columns with (px*grid_x)/width == fx, the rows with (py*grid_y)/height == fy
+ * and the slice's depth range, widened by a 2^-10 relative margin. A light is listed
+ * when its range sphere meets the box (Arvo), and for a spot with 0 < cos_outer <
+ * cos_inner also when its outer cone meets the box's bounding sphere; directional
+ * lights are always listed. Lists are in ascending light index with no cap, froxel
+ * index f = (fy*grid_x + fx)*grid_z + s, offsets[] is the exclusive prefix sum. The
+ * result is deterministic and bit-identical to the documented f32 operation order.
+ * If the total exceeds `capacity`, only indices below capacity are written, offsets
+ * are still complete, and hl_sync_status reports HL_ERR_CAPACITY. */
+hl_status hl_bin_froxels(hl_ctx* ctx, const void* camera, const void* lights, uint32_t n_lights,
+                         const hl_froxel_params* params, const hl_froxel_lists* out,
+                         void* stream);
+
+/* ---------------------------------------------------------------------------------
+ * Deferred lighting — the reference's DeferredLightPass (fs_main)
+ * -------------------------------------------------------------------------------*/
+
+/* G-buffer layouts.
+ *  HL_GBUF_REFERENCE (28 B/px, helio-pass-gbuffer/src/lib.rs:236-282):
+ *     plane0 albedo RGBA8 unorm (rgb, alpha)      plane1 normal RGBA16F (N.xyz, F0.r)
+ *     plane2 orm RGBA8 unorm (ao, rough, metal, F0.g)
+ *     plane3 emissive RGBA16F (rgb, F0.b)         plane4 depth R32F (NDC z in [0,1])
+ *  HL_GBUF_F32 (36 B/px):
+ *     plane0 RGBA32F (albedo.rgb, roughness)      plane1 RGBA32F (N.xyz, metallic)
+ *     plane2 depth R32F
+ *  HL_GBUF_F16 (18 B/px):
+ *     plane0 RGBA16F (albedo.rgb, roughness)      plane1 RG16F octahedral normal
+ *     plane2 R16F metallic                        plane3 depth R32F
+ *  For F32/F16, F0 = clamp(mix(0.04, albedo, metallic), 0, 0.999) as gbuffer.wgsl:323-328
+ *  writes it, ao = 1, emissive = 0, alpha = 1. */
+#define HL_GBUF_REFERENCE 0u
+#define HL_GBUF_F32 1u
+#define HL_GBUF_F16 2u
+#define HL_GBUF_MAX_PLANES 6
+
+typedef struct hl_gbuffer {
+    uint32_t layout;
+    uint32_t width, height;
+    uint32_t reserved;
+    const void* planes[HL_GBUF_MAX_PLANES]; /* device */
+    uint64_t pitch[HL_GBUF_MAX_PLANES];     /* row pitch in bytes */
+} hl_gbuffer;
+
+#define HL_GRID_TILES 0u   /* reference tile lists: lists = tile_light_lists, counts = tile_light_counts */
+#define HL_GRID_FROXELS 1u /* froxel lists: lists = indices, counts = offsets[F+1]                        */
+
+typedef struct hl_light_grid {
+    uint32_t kind;
+    uint32_t lists_capacity; /* entries in `lists`; 0 = tiles*64 (tiles) or offsets[F] (froxels) */
+    const uint32_t* lists;   /* device */
+    const uint32_t* counts;  /* device */
+    hl_froxel_params froxel; /* used when kind == HL_GRID_FROXELS */
+} hl_light_grid;
+
+#define HL_TARGET_RGBA32F 0u
+#define HL_TARGET_RGBA16F 1u
+
+typedef struct hl_target {
+    void* data;     /* device */
+    uint64_t pitch; /* row pitch in bytes */
+    uint32_t format;
+    uint32_t reserved;
+} hl_target;
+
+/* Direct + ambient + emissive lighting of every G-buffer pixel, fs_main under the
+ * pass's fallback bindings (no shadows, RC GI, lightmap, reflections, SSS, IES):
+ *   color = sum over the pixel's list of pbr_direct_light + hemisphere ambient * ao
+ *           + emissive, alpha from the G-buffer (deferred_lighting.wgsl:991-1259).
+ * Pixels with depth >= 1 are left untouched (the shader discards them, :996-997).
+ * Lights are summed in list order in f32 with compensated (Kahan) accumulation.
+ *   camera  : device GpuCameraUniforms     globals : device DeferredGlobals (112 B)
+ *   lights  : device GpuLight[n_lights]    grid    : tile or froxel lists
+ * Replaces: DeferredLightPass::prepare + execute (deferred-light/src/lib.rs:836-1199). */
+hl_status hl_shade(hl_ctx* ctx, const void* camera, const void* globals, const hl_gbuffer* gbuffer,
+                   const void* lights, uint32_t n_lights, const hl_light_grid* grid,
+                   const hl_target* radiance, void* stream);
+
+/* Per-pixel pair statistics of the same shading pass, for FLOP accounting: for every
+ * pixel (x,y), counts[(y*W+x)*3 + {0,1,2}] = lights listed for the pixel, lights in
+ * range (the reference's light-loop test, deferred_lighting.wgsl:1128-1131), and full
+ * BRDF evaluations (past the NdL == 0 and radiance < 0.002 cuts, :778-781). Sky pixels
+ * get zeros. No reference counterpart. */
+hl_status hl_shade_stats(hl_ctx* ctx, const void* camera, const void* globals, const hl_gbuffer* gbuffer,
+                         const void* lights, uint32_t n_lights, const hl_light_grid* grid,
+                         uint32_t* counts, void* stream);
+
+/* ---------------------------------------------------------------------------------
+ * Adjoint of the direct-lighting term (no reference counterpart)
+ * -------------------------------------------------------------------------------*/
+
+/* Given dL/d(radiance) for every pixel (RGBA32F, alpha ignored), returns
+ *   d_lights[n_lights*7] (f64): d/d position.xyz, d/d intensity, d/d color.rgb
+ *   d_pixels[W*H*5]      (f32): d/d albedo.rgb, d/d roughness, d/d metallic
+ * for the radiance hl_shade computes on an HL_GBUF_F32 G-buffer with a froxel grid.
+ * BRDF terms are recomputed, not stored. Light gradients are reduced per block in
+ * f32 and across blocks in f64 in a fixed order, so results are deterministic.
+ * The branch decisions (range, NdL == 0, radiance < 0.002) are held fixed. d_lights
+ * and d_pixels are overwritten. */
+hl_status hl_shade_adjoint(hl_ctx* ctx, const void* camera, const void* globals,
+                           const hl_gbuffer* gbuffer, const void* lights, uint32_t n_lights,
+                           const hl_light_grid* grid, const float* d_radiance,
+                           uint64_t d_radiance_pitch, double* d_lights, float* d_pixels,
+                           void* stream);
+
+/* ---------------------------------------------------------------------------------
+ * Batched views (no reference counterpart)
+ * -------------------------------------------------------------------------------*/
+
+typedef struct hl_view {
+    const void* camera; /* device GpuCameraUniforms */
+    hl_gbuffer gbuffer;
+    hl_target radiance;
+} hl_view;
+
+typedef struct hl_batch_config {
+    uint32_t autotune;        /* 1: time candidate froxel/tile shapes and keep the fastest */
+    uint32_t grid_x, grid_y;  /* used when autotune == 0: froxel grid for every view        */
+    uint32_t grid_z;
+    const char* cache_path;   /* optional autotuner cache file (read and written), or NULL  */
+} hl_batch_config;
+
+typedef struct hl_batch_plan hl_batch_plan;
+
+/* Builds a plan that lights all views with one shared light list: one batched froxel
+ * binning launch over every view and one persistent shading launch over a
+ * (view, tile) work list, captured together in a CUDA graph. View buffers and the
+ * light buffer are baked into the plan; change them by building a new plan. */
+hl_status hl_batch_plan_create(hl_ctx* ctx, const hl_view* views, uint32_t n_views,
+                               const void* lights, uint32_t n_lights, const void* globals,
+                               const hl_batch_config* config, hl_batch_plan** out_plan,
+                               void* stream);
+
+/* Replays the plan's graph on `stream`. */
+hl_status hl_batch_execute(hl_ctx* ctx, hl_batch_plan* plan, void* stream);
+
+/* Chosen froxel grid of the plan for one view (after autotuning). */
+hl_status hl_batch_plan_view_grid(const hl_batch_plan* plan, uint32_t view, uint32_t* grid_xyz);
+
+hl_status hl_batch_plan_destroy(hl_batch_plan* plan);
+
+/* ---------------------------------------------------------------------------------
+ * Diagnostics (no reference counterpart)
+ * -------------------------------------------------------------------------------*/
+
+/* Measures the device's FP32 FMA throughput with a register-resident FFMA loop
+ * (best of 5 timed launches); the denominator of the FP32 roofline. Synchronous. */
+hl_status hl_probe_fp32_peak(hl_ctx* ctx, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HELIO_GB300_H */

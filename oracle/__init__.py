@@ -1,0 +1,182 @@
+"""ctypes wrapper of the CPU oracle (oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: the checker for the CUDA library. Only tests/,
+__graft_entry__.smoke() and bench.py's cpu_baseline / reference legs import this
+package. Parity against the reference's own execution is UNPINNED (see the header of
+oracle.cpp); the restatement is pinned by layout constants, known-answer cases and the
+golden vectors under tests/golden/.
+
+Build recipe: ``python -m oracle.build`` or ``oracle.build()``; compiles oracle.cpp with
+g++ (-O3 -ffp-contract=off -fopenmp) into oracle/_build/liboracle.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD_DIR = HERE / "_build"
+LIB_PATH = BUILD_DIR / "liboracle.so"
+SOURCES = [HERE / "oracle.cpp"]
+
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    """Compile the oracle if it is missing or older than its source."""
+    BUILD_DIR.mkdir(exist_ok=True)
+    newest = max(p.stat().st_mtime for p in SOURCES)
+    if not force and LIB_PATH.exists() and LIB_PATH.stat().st_mtime >= newest:
+        return LIB_PATH
+    tmp = LIB_PATH.with_suffix(f".{os.getpid()}.tmp")
+    cmd = [
+        "g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
+        "-ffp-contract=off", "-fno-fast-math", "-fno-strict-aliasing",
+        *map(str, SOURCES), "-o", str(tmp),
+    ]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            _lib = _bind(C.CDLL(str(LIB_PATH)))
+    return _lib
+
+
+def _bind(l):
+    vp, u32, u64p, u32p, f32p, f64p = C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p
+    l.oracle_bin_tiles_ref_f32.argtypes = [vp, vp, u32, u32, u32, u32p, u32p]
+    l.oracle_bin_tiles_ref_f64.argtypes = [vp, vp, u32, u32, u32, u32p, u32p]
+    l.oracle_froxel_slice_table.argtypes = [vp, f32p]
+    l.oracle_bin_froxels_f32.argtypes = [vp, vp, u32, vp, u32p, u32p, u32]
+    shade_args = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, f64p, u32p, u32, u32]
+    l.oracle_shade_f64.argtypes = shade_args
+    l.oracle_shade_f32.argtypes = shade_args
+    l.oracle_shade_adjoint_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, f64p, f64p, f64p]
+    l.oracle_set_threads.argtypes = [C.c_int]
+    l.oracle_num_threads.restype = C.c_int
+    return l
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def set_threads(n: int) -> None:
+    lib().oracle_set_threads(int(n))
+
+
+def num_threads() -> int:
+    return int(lib().oracle_num_threads())
+
+
+# ----------------------------------------------------------------------------------
+# Binning
+# ----------------------------------------------------------------------------------
+
+
+def bin_tiles_ref(camera_rec, lights, width, height, precision="f32"):
+    """Reference tile lists (light_cull.wgsl:123-180): (lists[tiles,64], counts[tiles])."""
+    tx, ty = (width + 15) // 16, (height + 15) // 16
+    lists = np.zeros((tx * ty, 64), np.uint32)
+    counts = np.zeros(tx * ty, np.uint32)
+    cam = np.ascontiguousarray(camera_rec)
+    lts = np.ascontiguousarray(lights)
+    fn = lib().oracle_bin_tiles_ref_f32 if precision == "f32" else lib().oracle_bin_tiles_ref_f64
+    fn(_ptr(cam), _ptr(lts) if len(lts) else None, len(lts), width, height, _ptr(lists), _ptr(counts))
+    return lists, counts
+
+
+def froxel_slice_table(params) -> np.ndarray:
+    p = np.ascontiguousarray(params)
+    out = np.zeros(int(p["grid_z"][0]) + 1, np.float32)
+    lib().oracle_froxel_slice_table(_ptr(p), _ptr(out))
+    return out
+
+
+def bin_froxels(camera_rec, lights, params, capacity=None):
+    """Froxel lists in the documented f32 order: (offsets[F+1], indices[total])."""
+    p = np.ascontiguousarray(params)
+    F = int(p["grid_x"][0] * p["grid_y"][0] * p["grid_z"][0])
+    n = len(lights)
+    cap = capacity if capacity is not None else max(1, F * max(n, 1))
+    cap = min(cap, 1 << 28)
+    offsets = np.zeros(F + 1, np.uint32)
+    indices = np.zeros(cap, np.uint32)
+    lts = np.ascontiguousarray(lights)
+    lib().oracle_bin_froxels_f32(_ptr(np.ascontiguousarray(camera_rec)), _ptr(lts) if n else None, n, _ptr(p),
+                                 _ptr(offsets), _ptr(indices), cap)
+    total = int(offsets[F])
+    return offsets, indices[: min(total, cap)].copy()
+
+
+# ----------------------------------------------------------------------------------
+# Shading
+# ----------------------------------------------------------------------------------
+
+
+def _planes(gb):
+    arrs = [np.ascontiguousarray(p) for p in gb.planes]
+    ptrs = (C.c_void_p * 6)(*([a.ctypes.data for a in arrs] + [None] * (6 - len(arrs))))
+    pitch = (C.c_uint64 * 6)(*([a.strides[0] for a in arrs] + [0] * (6 - len(arrs))))
+    return arrs, ptrs, pitch
+
+
+def _grid_args(grid):
+    """grid: ('tiles', lists, counts) or ('froxels', indices, offsets, params)."""
+    kind = grid[0]
+    if kind == "tiles":
+        lists = np.ascontiguousarray(grid[1], np.uint32)
+        counts = np.ascontiguousarray(grid[2], np.uint32)
+        return 0, lists, counts, None
+    lists = np.ascontiguousarray(grid[1], np.uint32)
+    if lists.size == 0:
+        lists = np.zeros(1, np.uint32)
+    offsets = np.ascontiguousarray(grid[2], np.uint32)
+    params = np.ascontiguousarray(grid[3])
+    return 1, lists, offsets, params
+
+
+def shade(camera_rec, globals_rec, gb, lights, grid, precision="f64", rows=None, pair_counts=False):
+    """Radiance (H, W, 4) float64 of fs_main's direct + ambient + emissive terms.
+    Sky pixels (depth >= 1) are NaN. Optionally per-pixel (listed, in_range, full)."""
+    W, H = gb.width, gb.height
+    r0, r1 = (0, H) if rows is None else rows
+    out = np.full((H, W, 4), np.nan, np.float64)
+    pc = np.zeros((H, W, 3), np.uint32) if pair_counts else None
+    arrs, ptrs, pitch = _planes(gb)
+    kind, lists, counts, params = _grid_args(grid)
+    lts = np.ascontiguousarray(lights)
+    fn = lib().oracle_shade_f64 if precision == "f64" else lib().oracle_shade_f32
+    fn(_ptr(np.ascontiguousarray(camera_rec)), _ptr(np.ascontiguousarray(globals_rec)), gb.layout, W, H, ptrs, pitch,
+       _ptr(lts) if len(lts) else None, len(lts), kind, _ptr(lists), _ptr(counts),
+       _ptr(params) if params is not None else None, _ptr(out), _ptr(pc) if pc is not None else None, r0, r1)
+    return (out, pc) if pair_counts else out
+
+
+def shade_adjoint(camera_rec, globals_rec, gb, lights, grid, weights):
+    """FP64 gradient of sum(weights * radiance) (branch decisions fixed):
+    (d_lights[n,7], d_pixels[H,W,5])."""
+    W, H = gb.width, gb.height
+    arrs, ptrs, pitch = _planes(gb)
+    kind, lists, counts, params = _grid_args(grid)
+    lts = np.ascontiguousarray(lights)
+    w = np.ascontiguousarray(weights, np.float64).reshape(H, W, 4)
+    dl = np.zeros((len(lts), 7), np.float64)
+    dp = np.zeros((H, W, 5), np.float64)
+    lib().oracle_shade_adjoint_f64(_ptr(np.ascontiguousarray(camera_rec)), _ptr(np.ascontiguousarray(globals_rec)),
+                                   gb.layout, W, H, ptrs, pitch, _ptr(lts) if len(lts) else None, len(lts), kind,
+                                   _ptr(lists), _ptr(counts), _ptr(params) if params is not None else None, _ptr(w),
+                                   _ptr(dl), _ptr(dp))
+    return dl, dp

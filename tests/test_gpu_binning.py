@@ -1,0 +1,113 @@
+"""GPU parity of the binning kernels: bit-exact against the f32 oracle.
+
+Reference behaviour covered (light_cull.wgsl:123-180, light-cull/src/lib.rs:264-362):
+ordered lists, the 64-light cap, directional lights always listed, clamped NDC at
+the right/bottom edge tiles, zero lights clearing both buffers. Froxel lists: every
+workload grid, capacity overflow, zero lights."""
+import numpy as np
+import pytest
+
+import oracle
+from helio_gb300 import layouts as L
+from helio_gb300 import native as N
+from helio_gb300 import synthetic as S
+
+from gpu_util import assert_tile_lists_equal, gpu_bin_froxels, gpu_bin_tiles
+from scenes import mixed_lights, overlapping_lights
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("wi", [0, 1, 2, 4])
+def test_tile_lists_workloads(ctx, wi):
+    w = S.workload(wi)
+    W, H = w.gbuffer.width, w.gbuffer.height
+    got = gpu_bin_tiles(ctx, w.camera.record, w.lights, W, H)
+    want = oracle.bin_tiles_ref(w.camera.record, w.lights, W, H)
+    assert_tile_lists_equal(got, want)
+
+
+@pytest.mark.parametrize("size", [(1000, 500), (17, 17), (1, 1), (1283, 719), (16, 4096)])
+def test_tile_lists_ragged_viewports(ctx, size):
+    W, H = size
+    cam = S.default_camera(W, H)
+    lt = mixed_lights(cam, 7, 120, 40)
+    assert_tile_lists_equal(gpu_bin_tiles(ctx, cam.record, lt, W, H), oracle.bin_tiles_ref(cam.record, lt, W, H))
+
+
+def test_tile_cap_drops_65th_light(ctx):
+    W, H = 320, 180
+    cam = S.default_camera(W, H)
+    lt = overlapping_lights(70)
+    lists, counts = gpu_bin_tiles(ctx, cam.record, lt, W, H)
+    assert (counts == 64).all()
+    assert (lists == np.arange(64, dtype=np.uint32)[None, :]).all()
+    assert_tile_lists_equal((lists, counts), oracle.bin_tiles_ref(cam.record, lt, W, H))
+
+
+def test_tile_directional_always_listed(ctx):
+    W, H = 256, 128
+    cam = S.default_camera(W, H)
+    lt = mixed_lights(cam, 3, 10, 0, n_dir=3)
+    lists, counts = gpu_bin_tiles(ctx, cam.record, lt, W, H)
+    dirs = np.nonzero(lt["light_type"] == L.LIGHT_DIRECTIONAL)[0]
+    for t in range(len(counts)):
+        assert set(dirs.tolist()) <= set(lists[t, : counts[t]].tolist())
+
+
+def test_tile_zero_lights_clears(ctx):
+    W, H = 200, 100
+    cam = S.default_camera(W, H)
+    lists, counts = gpu_bin_tiles(ctx, cam.record, np.zeros(0, L.GPU_LIGHT), W, H)
+    assert (counts == 0).all() and (lists == 0).all()
+
+
+@pytest.mark.parametrize("wi", [0, 1, 2, 4])
+def test_froxel_lists_workloads(ctx, wi):
+    w = S.workload(wi)
+    p = L.froxel_params(*w.froxel_grid, w.gbuffer.width, w.gbuffer.height, w.camera.far)
+    off_w, idx_w = oracle.bin_froxels(w.camera.record, w.lights, p, capacity=1 << 26)
+    off, idx, _ = gpu_bin_froxels(ctx, w.camera.record, w.lights, p, capacity=int(off_w[-1]) + 16)
+    np.testing.assert_array_equal(off, off_w)
+    np.testing.assert_array_equal(idx, idx_w)
+
+
+@pytest.mark.parametrize("grid", [(1, 1, 1), (7, 5, 3), (16, 9, 24), (40, 23, 128)])
+def test_froxel_lists_mixed_lights(ctx, grid):
+    W, H = 640, 368
+    cam = S.default_camera(W, H)
+    lt = mixed_lights(cam, 11, 200, 80, n_dir=2)
+    p = L.froxel_params(*grid, W, H, cam.far)
+    off_w, idx_w = oracle.bin_froxels(cam.record, lt, p, capacity=1 << 26)
+    off, idx, _ = gpu_bin_froxels(ctx, cam.record, lt, p, capacity=int(off_w[-1]) + 1)
+    np.testing.assert_array_equal(off, off_w)
+    np.testing.assert_array_equal(idx, idx_w)
+
+
+def test_froxel_capacity_overflow(ctx):
+    w = S.workload(0)
+    p = L.froxel_params(*w.froxel_grid, w.gbuffer.width, w.gbuffer.height, w.camera.far)
+    off_w, idx_w = oracle.bin_froxels(w.camera.record, w.lights, p, capacity=1 << 24)
+    cap = int(off_w[-1]) // 2
+    off, idx, _ = gpu_bin_froxels(ctx, w.camera.record, w.lights, p, capacity=cap, expect_status=N.HL_ERR_CAPACITY)
+    np.testing.assert_array_equal(off, off_w)
+    np.testing.assert_array_equal(idx[:cap], idx_w[:cap])
+
+
+def test_froxel_zero_lights(ctx):
+    cam = S.default_camera(320, 180)
+    p = L.froxel_params(8, 4, 6, 320, 180, cam.far)
+    off, idx, _ = gpu_bin_froxels(ctx, cam.record, np.zeros(0, L.GPU_LIGHT), p, capacity=16)
+    assert (off == 0).all() and idx.size == 0
+
+
+def test_froxel_lists_large_light_count(ctx):
+    """More lights than one shared-memory round of the column list holds."""
+    W, H = 256, 144
+    cam = S.default_camera(W, H)
+    lt = S.make_lights(cam, 21, 9000, 1000, radius=(5.0, 30.0))
+    p = L.froxel_params(4, 2, 8, W, H, cam.far)
+    off_w, idx_w = oracle.bin_froxels(cam.record, lt, p, capacity=1 << 26)
+    off, idx, _ = gpu_bin_froxels(ctx, cam.record, lt, p, capacity=int(off_w[-1]))
+    np.testing.assert_array_equal(off, off_w)
+    np.testing.assert_array_equal(idx, idx_w)

@@ -1,0 +1,172 @@
+"""GPU parity of hl_shade against the float64 oracle of fs_main / pbr_direct_light.
+
+Tolerances (relative, per pixel, floor 1e-6 of the image maximum; see
+helio_gb300/metrics.py):
+  FP32 / reference G-buffers: p99.99 <= 1e-5, max <= 1e-3
+  FP16 G-buffer:              max <= 2e-3
+Pixels where the kernel and the oracle take different sides of a cut ("flips",
+detected from the per-pixel full-evaluation counts) are counted separately and must
+be rare (< 1e-4 of the pixels)."""
+import numpy as np
+import pytest
+
+import oracle
+from helio_gb300 import frame as FR
+from helio_gb300 import layouts as L
+from helio_gb300 import metrics
+from helio_gb300 import native as N
+from helio_gb300 import synthetic as S
+
+from gpu_util import gpu_bin_froxels, gpu_bin_tiles, gpu_shade
+from scenes import mixed_lights
+
+pytestmark = pytest.mark.gpu
+
+TOL = {S.LAYOUT_F32: (1e-5, 1e-3), S.LAYOUT_REFERENCE: (1e-5, 1e-3), S.LAYOUT_F16: (2e-3, 2e-3)}
+
+
+def _grids(ctx, w_cam_rec, lights, gb, grid_shape, kind):
+    import torch
+
+    W, H = gb.width, gb.height
+    if kind == "tiles":
+        lists, counts = oracle.bin_tiles_ref(w_cam_rec, lights, W, H)
+        dl = torch.from_numpy(lists.reshape(-1).view(np.int32).copy()).cuda()
+        dc = torch.from_numpy(counts.view(np.int32).copy()).cuda()
+        return ("tiles", lists, counts), N.tile_grid_struct(dl, dc), (dl, dc)
+    p = L.froxel_params(*grid_shape, W, H, 100.0)
+    off, idx = oracle.bin_froxels(w_cam_rec, lights, p, capacity=1 << 26)
+    doff = torch.from_numpy(off.view(np.int32).copy()).cuda()
+    didx = torch.from_numpy((idx if idx.size else np.zeros(1, np.uint32)).view(np.int32).copy()).cuda()
+    return ("froxels", idx, off, p), N.froxel_grid_struct(didx, doff, N.froxel_params_from_numpy(p), didx.numel()), (didx, doff)
+
+
+def _check(ctx, cam_rec, glb, lights, gb, grid_shape, kind, tol):
+    df = FR.upload(cam_rec, glb, lights, gb)
+    ogrid, dgrid, keep = _grids(ctx, cam_rec, lights, gb, grid_shape, kind)
+    img = gpu_shade(ctx, df, dgrid)
+    ref, pc = oracle.shade(cam_rec, glb, gb, lights, ogrid, pair_counts=True)
+    st = gpu_shade(ctx, df, dgrid, stats=True)
+    e = metrics.radiance_error(img, ref, st[..., 2], pc[..., 2])
+    sky = np.isnan(ref[..., 0])
+    assert np.all(img[sky] == 7.0), "sky pixels must be left untouched"
+    assert e["flips"] <= max(2, 1e-4 * e["n"]), e
+    p_tol, max_tol = tol
+    assert e["p9999"] <= p_tol and e["max"] <= max_tol, e
+    # alpha channel
+    assert np.allclose(img[~sky][:, 3], ref[~sky][:, 3])
+    return e, st, pc
+
+
+@pytest.mark.parametrize("wi", [0, 1, 4])
+@pytest.mark.parametrize("kind", ["froxels", "tiles"])
+def test_shade_workloads(ctx, wi, kind):
+    w = S.workload(wi)
+    _check(ctx, w.camera.record, w.globals_, w.lights, w.gbuffer, w.froxel_grid, kind, TOL[w.gbuffer.layout])
+
+
+def test_shade_4k_clumped(ctx):
+    w = S.workload(2)
+    _check(ctx, w.camera.record, w.globals_, w.lights, w.gbuffer, w.froxel_grid, "froxels", TOL[S.LAYOUT_F32])
+
+
+@pytest.mark.parametrize("layout", [S.LAYOUT_REFERENCE, S.LAYOUT_F32, S.LAYOUT_F16])
+def test_shade_mixed_lights_with_ambient(ctx, layout):
+    W, H = 480, 272
+    cam = S.default_camera(W, H)
+    gb = S.make_gbuffer(cam, layout, seed=77)
+    lt = mixed_lights(cam, 5, 150, 60, n_dir=2)
+    tx, _ = L.tile_grid(W, H)
+    glb = L.make_globals(tx, len(lt), ambient_color=(0.5, 0.5, 0.6), ambient_intensity=1.0)
+    for kind in ("tiles", "froxels"):
+        _check(ctx, cam.record, glb, lt, gb, (12, 8, 16), kind, TOL[layout])
+
+
+def test_shade_pair_counts_match_oracle(ctx):
+    w = S.workload(1)
+    _, st, pc = _check(ctx, w.camera.record, w.globals_, w.lights, w.gbuffer, w.froxel_grid, "froxels",
+                       TOL[w.gbuffer.layout])
+    mism = (st != pc).any(-1).mean()
+    assert mism < 1e-4, mism
+
+
+def test_shade_debug_modes(ctx):
+    W, H = 128, 96
+    cam = S.default_camera(W, H)
+    gb = S.make_gbuffer(cam, S.LAYOUT_F32, seed=3)
+    lt = mixed_lights(cam, 9, 20, 5)
+    tx, _ = L.tile_grid(W, H)
+    for mode in (1, 5):
+        glb = L.make_globals(tx, len(lt), debug_mode=mode)
+        df = FR.upload(cam.record, glb, lt, gb)
+        ogrid, dgrid, keep = _grids(ctx, cam.record, lt, gb, None, "tiles")
+        img = gpu_shade(ctx, df, dgrid)
+        ref = oracle.shade(cam.record, glb, gb, lt, ogrid)
+        m = ~np.isnan(ref[..., 0])
+        np.testing.assert_allclose(img[m], ref[m], rtol=1e-6, atol=1e-6)
+
+
+def test_shade_rgba16f_target(ctx):
+    w = S.workload(0, scale=0.5)
+    df = FR.upload_workload(w)
+    ogrid, dgrid, keep = _grids(ctx, w.camera.record, w.lights, w.gbuffer, w.froxel_grid, "froxels")
+    img = gpu_shade(ctx, df, dgrid, target_format=N.TARGET_RGBA16F)
+    ref = oracle.shade(w.camera.record, w.globals_, w.gbuffer, w.lights, ogrid)
+    m = ~np.isnan(ref[..., 0])
+    np.testing.assert_allclose(img[m][:, :3], ref[m][:, :3], rtol=2e-3, atol=1e-6)
+
+
+def test_shade_uses_gpu_lists(ctx):
+    """The whole path: lists from the GPU binning feed the GPU shading."""
+    w = S.workload(1)
+    p = L.froxel_params(*w.froxel_grid, w.gbuffer.width, w.gbuffer.height, w.camera.far)
+    off, idx, keep = gpu_bin_froxels(ctx, w.camera.record, w.lights, p, capacity=1 << 20)
+    cam_t, lt_t, d_off, d_idx, fp, cap = keep
+    df = FR.upload_workload(w)
+    img = gpu_shade(ctx, df, N.froxel_grid_struct(d_idx, d_off, fp, cap))
+    ref = oracle.shade(w.camera.record, w.globals_, w.gbuffer, w.lights, ("froxels", idx, off, p))
+    e = metrics.radiance_error(img, ref)
+    assert e["max"] <= 2e-3, e
+
+
+def test_shade_rejects_bad_arguments(ctx):
+    w = S.workload(0, scale=0.25)
+    df = FR.upload_workload(w)
+    ogrid, dgrid, keep = _grids(ctx, w.camera.record, w.lights, w.gbuffer, w.froxel_grid, "froxels")
+    import torch
+
+    out = torch.zeros((df.height, df.width, 4), dtype=torch.float32, device="cuda")
+    bad = df.gbuffer
+    bad.layout = 9
+    with pytest.raises(N.HelioError) as e:
+        ctx.shade(df.camera, df.globals_, bad, df.lights, df.n_lights, dgrid, N.target_struct(out))
+    assert e.value.status == N.HL_ERR_INVALID_ARGUMENT
+    gbm = df.gbuffer
+    gbm.planes[0] = gbm.planes[0] + 4  # misaligned float4 plane
+    with pytest.raises(N.HelioError) as e:
+        ctx.shade(df.camera, df.globals_, gbm, df.lights, df.n_lights, dgrid, N.target_struct(out))
+    assert e.value.status == N.HL_ERR_LAYOUT
+    with pytest.raises(N.HelioError) as e:
+        ctx.shade(df.camera, df.globals_, df.gbuffer, 0, df.n_lights, dgrid, N.target_struct(out))
+    assert e.value.status == N.HL_ERR_INVALID_ARGUMENT
+
+
+def test_shade_out_of_range_light_index_is_reported(ctx):
+    """A list entry beyond n_lights is skipped and reported, never read."""
+    import torch
+
+    w = S.workload(0, scale=0.25)
+    df = FR.upload_workload(w)
+    lists, counts = oracle.bin_tiles_ref(w.camera.record, w.lights, df.width, df.height)
+    lists = lists.copy()
+    counts = counts.copy()
+    lists[0, 0] = 10_000_000
+    counts[0] = max(int(counts[0]), 1)
+    dl = torch.from_numpy(lists.reshape(-1).view(np.int32).copy()).cuda()
+    dc = torch.from_numpy(counts.view(np.int32).copy()).cuda()
+    out = torch.zeros((df.height, df.width, 4), dtype=torch.float32, device="cuda")
+    ctx.shade(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, N.tile_grid_struct(dl, dc), N.target_struct(out))
+    with pytest.raises(N.HelioError) as e:
+        ctx.sync_status()
+    assert e.value.status == N.HL_ERR_DEVICE_BOUNDS
+    ctx.sync_status()  # cleared
