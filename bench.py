@@ -323,7 +323,7 @@ def run_ours(args, world, rank, local):
                 "frac": round(frac_fp32, 4), "traffic": traffic,
                 "peak_source": "hl_probe_fp32_peak FFMA loop, of measured"}
     roof.update({
-        "kernel": "shade_kernel<F16, froxels>",
+        "kernel": "shade_kernel<F16 G-buffer, froxel grid, 32x16 tile>",
         "kernel_ms": round(t_shade * 1e3, 4),
         "algorithmic_bytes": int(bytes_alg),
         "algorithmic_flops": int(flops),
@@ -375,8 +375,8 @@ def run_ours(args, world, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()

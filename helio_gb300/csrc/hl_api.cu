@@ -147,7 +147,7 @@ hl_status check_common(hl_ctx* ctx, const void* camera, const void* lights, uint
     if (!aligned(camera, 16)) return fail(ctx, HL_ERR_LAYOUT, "camera pointer not 16-byte aligned");
     if (n_lights > 0 && !lights) return fail(ctx, HL_ERR_INVALID_ARGUMENT, "lights is NULL with n_lights=%u", n_lights);
     if (lights && !aligned(lights, 16)) return fail(ctx, HL_ERR_LAYOUT, "lights pointer not 16-byte aligned");
-    if (n_lights > (1u << 24)) return fail(ctx, HL_ERR_SIZE, "n_lights %u exceeds 2^24", n_lights);
+    if (n_lights > (1u << 23)) return fail(ctx, HL_ERR_SIZE, "n_lights %u exceeds 2^23", n_lights);
     return HL_OK;
 }
 

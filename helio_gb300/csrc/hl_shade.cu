@@ -1,9 +1,20 @@
 // hl_shade.cu — deferred lighting (fs_main under fallback bindings) for sm_103a.
 //
-// One thread per pixel, 16x16-pixel CTAs (one reference light-cull tile per CTA).
-// Each thread decodes its G-buffer texel, reconstructs the world position, walks its
-// tile or froxel light list in list order and accumulates pbr_direct_light in f32
-// with Kahan compensation, then adds hemisphere ambient and emissive.
+// One CTA of 256 threads lights a 32x16-pixel tile (froxel grid) or one 16x16 reference
+// light-cull tile (tile grid):
+//  1. threads decode the tile's G-buffer texels (coalesced along x) and set each pixel
+//     up (world position, N, V, NdV, albedo, F0, Schlick-GGX of the view) into shared
+//     memory, with its light list (its froxel's list, or the tile's reference list);
+//  2. pixels are counting-sorted by froxel (slice, column), so a group of 32 pixels
+//     mostly shares one list; each warp takes a light and a heavy group;
+//  3. each lane walks its own pixel's list in list order, four entries at a time with the
+//     loads of the next entries in flight, and tests each light for range and the NdL
+//     sign; passing (pixel, light) pairs go to a per-warp queue;
+//  4. queued pairs are evaluated 32 at a time, one per lane, so the full BRDF of
+//     pbr_direct_light runs with all lanes busy, and are added into per-pixel Kahan
+//     accumulators in queue order, which is list order for every pixel, as the
+//     reference's light loop adds them;
+//  5. threads compose hemisphere ambient and emissive and store their pixels.
 #include "hl_common.cuh"
 #include "hl_internal.h"
 #include "hl_shade_math.cuh"
@@ -13,8 +24,6 @@ namespace hl {
 namespace {
 
 using namespace sm;
-
-constexpr int kShadeTile = 16;
 
 __device__ __forceinline__ float h2f(uint16_t h) { return __half2float(__ushort_as_half(h)); }
 
@@ -88,148 +97,450 @@ __device__ __forceinline__ Texel<LAYOUT> load_texel(const GBufView& g, uint32_t 
     return t;
 }
 
-__device__ __forceinline__ ShadeLight load_light(const GpuLight* __restrict__ lights, uint32_t i) {
-    const float4* p = reinterpret_cast<const float4*>(lights + i);
-    const float4 a = __ldg(p + 0), b = __ldg(p + 1), c = __ldg(p + 2);
-    const uint4 d = __ldg(reinterpret_cast<const uint4*>(p + 3));
-    ShadeLight l;
-    l.px = a.x;
-    l.py = a.y;
-    l.pz = a.z;
-    l.range = a.w;
-    l.dx = b.x;
-    l.dy = b.y;
-    l.dz = b.z;
-    l.cos_outer = b.w;
-    l.cr = c.x;
-    l.cg = c.y;
-    l.cb = c.z;
-    l.intensity = c.w;
-    l.type = d.y;
-    l.cos_inner = __uint_as_float(d.z);
-    return l;
+
+namespace sk {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kQueue = 256;      // per-warp pair ring (up to 31 + kPipe * 32 pending)
+constexpr int kBins = 512;       // froxel keys of the pixel sort
+constexpr int kPipe = 4;         // list entries in flight per lane
+
+// Pixel record fields (structure of arrays).
+enum Field : int {
+    F_PX, F_PY, F_PZ, F_PLX, F_PLY, F_PLZ, F_NX, F_NY, F_NZ, F_VX, F_VY, F_VZ, F_NDV, F_AR, F_AG, F_AB, F_ROUGH,
+    F_METAL, F_F0R, F_F0G, F_F0B, F_GV, F_GUARD, F_DEPTH, F_NRX, F_NRY, F_NRZ, F_INVN, F_COUNT
+};
+
+template <int NPX>
+struct Smem {
+    float px[F_COUNT][NPX];
+    float acc[6][NPX];              // Kahan (sum, compensation) x RGB; statistics reuse it
+    uint32_t base[NPX], len[NPX];   // each pixel's light list
+    uint32_t hist[kBins];
+    uint16_t order[NPX];            // pixels sorted by froxel
+    uint32_t queue[kWarps][kQueue]; // ring of (pixel << 23) | light index
+    uint32_t warp_tot[kWarps];
+    float tab[kMaxSlices + 1];      // slice boundaries
+    uint32_t n_valid;
+};
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
 }
 
-template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS>
-__global__ void __launch_bounds__(kShadeTile* kShadeTile) shade_kernel(
+template <int NPX>
+__device__ __forceinline__ void store_pixel(Smem<NPX>& s, int i, const Pixel& p, const PixelBrdf& b, float guard,
+                                            float depth, float ar, float ag, float ab) {
+    s.px[F_PX][i] = p.Px; s.px[F_PY][i] = p.Py; s.px[F_PZ][i] = p.Pz;
+    s.px[F_PLX][i] = p.Plx; s.px[F_PLY][i] = p.Ply; s.px[F_PLZ][i] = p.Plz;
+    s.px[F_NX][i] = p.Nx; s.px[F_NY][i] = p.Ny; s.px[F_NZ][i] = p.Nz;
+    s.px[F_VX][i] = p.Vx; s.px[F_VY][i] = p.Vy; s.px[F_VZ][i] = p.Vz; s.px[F_NDV][i] = p.NdV;
+    s.px[F_AR][i] = ar; s.px[F_AG][i] = ag; s.px[F_AB][i] = ab;
+    s.px[F_ROUGH][i] = p.rough; s.px[F_METAL][i] = p.metal;
+    s.px[F_F0R][i] = p.f0r; s.px[F_F0G][i] = p.f0g; s.px[F_F0B][i] = p.f0b;
+    s.px[F_GV][i] = b.gv; s.px[F_GUARD][i] = guard; s.px[F_DEPTH][i] = depth;
+    s.px[F_NRX][i] = p.nrx; s.px[F_NRY][i] = p.nry; s.px[F_NRZ][i] = p.nrz; s.px[F_INVN][i] = p.inv_n;
+}
+
+template <int NPX>
+__device__ __forceinline__ void load_pixel(const Smem<NPX>& s, int i, Pixel& p, PixelBrdf& b) {
+    p.Px = s.px[F_PX][i]; p.Py = s.px[F_PY][i]; p.Pz = s.px[F_PZ][i];
+    p.Plx = s.px[F_PLX][i]; p.Ply = s.px[F_PLY][i]; p.Plz = s.px[F_PLZ][i];
+    p.Nx = s.px[F_NX][i]; p.Ny = s.px[F_NY][i]; p.Nz = s.px[F_NZ][i];
+    p.Vx = s.px[F_VX][i]; p.Vy = s.px[F_VY][i]; p.Vz = s.px[F_VZ][i]; p.NdV = s.px[F_NDV][i];
+    p.dr = s.px[F_AR][i] * kInvPi; p.dg = s.px[F_AG][i] * kInvPi; p.db = s.px[F_AB][i] * kInvPi;
+    p.rough = s.px[F_ROUGH][i]; p.metal = s.px[F_METAL][i];
+    p.f0r = s.px[F_F0R][i]; p.f0g = s.px[F_F0G][i]; p.f0b = s.px[F_F0B][i];
+    p.nrx = s.px[F_NRX][i]; p.nry = s.px[F_NRY][i]; p.nrz = s.px[F_NRZ][i]; p.inv_n = s.px[F_INVN][i];
+    const float a = p.rough * p.rough;  // pixel_brdf, with the view's Schlick-GGX stored
+    b.a2 = a * a;
+    const float r1 = p.rough + 1.0f;
+    b.k = (r1 * r1) * 0.125f;
+    b.omk = 1.0f - b.k;
+    b.gv = s.px[F_GV][i];
+    b.one_m_metal = 1.0f - p.metal;
+    b.nv4 = 4.0f * p.NdV;
+}
+
+}  // namespace sk
+
+// Precise re-evaluation of an ill-conditioned pair of the fast path: the pixel's
+// position as a camera-relative double-float (the light's rounding residual r folded
+// into its lo part), compensated NdV and NdL. Rare; kept out of line.
+__device__ __noinline__ int precise_pair(const GpuCamera* cam, uint32_t x, uint32_t y, float W, float H, float depth,
+                                         const Pixel& pin, float ar, float ag, float ab, const ShadeLight& l, float rx,
+                                         float ry, float rz, float& cr, float& cg, float& cb) {
+    Pixel p = pin;
+    const float camx = cam->position_near[0], camy = cam->position_near[1], camz = cam->position_near[2];
+    reconstruct<true>(cam->inv_view_proj, x, y, W, H, depth, p.Px, p.Py, p.Pz, p.Plx, p.Ply, p.Plz);
+    const DF ax = two_sum(p.Px, -camx), ay = two_sum(p.Py, -camy), az = two_sum(p.Pz, -camz);
+    const DF bx = two_sum(ax.hi, ax.lo + p.Plx), by = two_sum(ay.hi, ay.lo + p.Ply), bz = two_sum(az.hi, az.lo + p.Plz);
+    p.Px = bx.hi; p.Plx = bx.lo - rx;
+    p.Py = by.hi; p.Ply = by.lo - ry;
+    p.Pz = bz.hi; p.Plz = bz.lo - rz;
+    // V = -(true P): the camera sits at minus the residual
+    finish_pixel<true>(p, p.nrx, p.nry, p.nrz, ar, ag, ab, p.rough, p.metal, p.f0r, p.f0g, p.f0b, -rx, -ry, -rz);
+    const PixelBrdf pb = pixel_brdf(p);
+    return eval<true>(p, pb, l, cr, cg, cb);
+}
+
+// Evaluates nb queued pairs (ring positions head..head+nb-1), one per lane, and adds
+// them into the per-pixel Kahan accumulators in queue order. Out of line so that the
+// BRDF code exists once in the kernel.
+template <uint32_t LAYOUT, bool STATS, int TW, int NPX>
+__device__ __noinline__ void flush_batch(sk::Smem<NPX>& s, const uint32_t* queue, uint32_t head, uint32_t nb,
+                                         uint32_t lane, const GpuCamera* cam, const GpuLight* lights, uint32_t x0,
+                                         uint32_t y0, float W, float H) {
+    using namespace sk;
+    constexpr bool PRECISE = (LAYOUT != HL_GBUF_F16);
+    uint32_t (*cnt)[NPX] = reinterpret_cast<uint32_t (*)[NPX]>(s.acc);
+    const bool act = lane < nb;
+    const uint32_t e = act ? queue[(head + lane) & (kQueue - 1)] : 0u;
+    const uint32_t q = e >> 23, li = e & 0x7fffffu;
+    int st = kCut;
+    float cr = 0.0f, cg = 0.0f, cb = 0.0f;
+    bool rng = false;
+    if (act) {
+        Pixel p;
+        PixelBrdf pb;
+        load_pixel(s, q, p, pb);
+        const float4* gl = reinterpret_cast<const float4*>(lights + li);
+        const float4 a = __ldg(gl + 0), b = __ldg(gl + 1), c = __ldg(gl + 2);
+        const uint4 d = __ldg(reinterpret_cast<const uint4*>(gl + 3));
+        ShadeLight l;
+        l.range = a.w;
+        l.dx = b.x; l.dy = b.y; l.dz = b.z; l.cos_outer = b.w;
+        l.cr = c.x; l.cg = c.y; l.cb = c.z; l.intensity = c.w;
+        l.type = d.y;
+        l.cos_inner = __uint_as_float(d.z);
+        DF ux{a.x, 0.0f}, uy{a.y, 0.0f}, uz{a.z, 0.0f};
+        if (!PRECISE) {  // camera-relative light position and its exact rounding residual
+            ux = two_sum(a.x, -cam->position_near[0]);
+            uy = two_sum(a.y, -cam->position_near[1]);
+            uz = two_sum(a.z, -cam->position_near[2]);
+        }
+        l.px = ux.hi; l.py = uy.hi; l.pz = uz.hi;
+        if (STATS) rng = in_range(p, l);
+        st = eval<PRECISE>(p, pb, l, cr, cg, cb, PRECISE ? 0.0f : s.px[F_GUARD][q]);
+        if (!PRECISE && st == kNeedsPrecise)
+            st = precise_pair(cam, x0 + q % TW, y0 + q / TW, W, H, s.px[F_DEPTH][q], p, s.px[F_AR][q], s.px[F_AG][q],
+                              s.px[F_AB][q], l, ux.lo, uy.lo, uz.lo, cr, cg, cb);
+    }
+    const bool lit = act && st == kLit;
+    if (STATS) {
+        if (act && rng) atomicAdd(&cnt[1][q], 1u);
+        if (lit) atomicAdd(&cnt[2][q], 1u);
+    } else {
+        // rank of this pair among the batch's pairs of the same pixel (queue order)
+        const uint32_t k2 = lit ? q : (0x10000u | lane);
+        const uint32_t peers = __match_any_sync(0xffffffffu, k2);
+        const uint32_t rank = __popc(peers & lanemask_lt());
+        const uint32_t rounds = __reduce_max_sync(0xffffffffu, lit ? rank + 1 : 0u);
+        for (uint32_t r = 0; r < rounds; ++r) {
+            if (lit && rank == r) {
+                kahan_add(s.acc[0][q], s.acc[3][q], cr);
+                kahan_add(s.acc[1][q], s.acc[4][q], cg);
+                kahan_add(s.acc[2][q], s.acc[5][q], cb);
+            }
+            __syncwarp();
+        }
+    }
+    __syncwarp();
+}
+
+// TW x TH = 512 (froxel grid) or 256 (tile grid) pixels, 256 threads.
+template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, int TW, int TH>
+__global__ void __launch_bounds__(sk::kThreads, 2) shade_kernel(
     const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const GBufView gb,
     const GpuLight* __restrict__ lights, uint32_t n_lights, const GridView grid, const __grid_constant__ SliceTable tab,
     const TargetView out, uint32_t* __restrict__ stats, int* __restrict__ status) {
+    using namespace sk;
+    constexpr bool FROXELS = (GRID == HL_GRID_FROXELS);
+    constexpr int NPX = TW * TH;
+    constexpr int PPT = NPX / kThreads;  // pixels per thread in set-up and output
+    constexpr int NG = NPX / 32;         // groups of 32 sorted pixels
+    static_assert(NPX % kThreads == 0 && (NG == kWarps || NG == 2 * kWarps), "256 or 512 pixels per tile");
     constexpr bool PRECISE = (LAYOUT != HL_GBUF_F16);
-    __shared__ float s_tab[kMaxSlices + 1];
-    if (GRID == HL_GRID_FROXELS) {
-        for (uint32_t i = threadIdx.y * kShadeTile + threadIdx.x; i <= grid.fp.grid_z; i += kShadeTile * kShadeTile)
-            s_tab[i] = tab.z[i];
-        __syncthreads();
-    }
-    const uint32_t x = blockIdx.x * kShadeTile + threadIdx.x;
-    const uint32_t y = blockIdx.y * kShadeTile + threadIdx.y;
-    if (x >= gb.width || y >= gb.height) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem<NPX>& s = *reinterpret_cast<Smem<NPX>*>(smem_raw);
+    uint32_t (*cnt)[NPX] = reinterpret_cast<uint32_t (*)[NPX]>(s.acc);  // statistics view
+    const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
+    const float W = float(gb.width), H = float(gb.height);
+    const float camx = cam->position_near[0], camy = cam->position_near[1], camz = cam->position_near[2];
 
-    const Texel<LAYOUT> t = load_texel<LAYOUT>(gb, x, y);
-    if (!(t.depth < 1.0f)) {  // sky: the reference discards (deferred_lighting.wgsl:996-997)
-        if (STATS) {
-            uint32_t* s = stats + (size_t(y) * gb.width + x) * 3;
-            s[0] = s[1] = s[2] = 0;
-        }
-        return;
-    }
-    const uint32_t debug_mode = glb->debug_mode;
-    if (glb->has_rc_gi != 0u || debug_mode == 10u || debug_mode == 11u) raise_status(status, HL_ERR_NOT_SUPPORTED);
+    for (uint32_t b = t; b < uint32_t(kBins); b += kThreads) s.hist[b] = 0;
+    if (FROXELS)
+        for (uint32_t k = t; k <= grid.fp.grid_z; k += kThreads) s.tab[k] = tab.z[k];
+#pragma unroll
+    for (int k = 0; k < PPT; ++k)
+        for (int c = 0; c < 6; ++c) s.acc[c][t + k * kThreads] = 0.0f;
 
-    Pixel p;
-    reconstruct<PRECISE>(cam->inv_view_proj, x, y, float(gb.width), float(gb.height), t.depth, p.Px, p.Py, p.Pz, p.Plx,
-                         p.Ply, p.Plz);
-    finish_pixel(p, t.nx, t.ny, t.nz, t.ar, t.ag, t.ab, t.rough, t.metal, t.f0r, t.f0g, t.f0b, cam->position_near[0],
-                 cam->position_near[1], cam->position_near[2]);
-    const PixelBrdf brdf = pixel_brdf(p);
-
-    // Light list of the pixel.
-    const uint32_t* list = nullptr;
-    uint32_t count = 0;
-    if (GRID == HL_GRID_TILES) {
-        const uint32_t tile = (y / kTile) * glb->num_tiles_x + x / kTile;
-        if (tile < grid.tiles) {
-            count = grid.counts[tile];
-            if (count > kMaxPerTile) {
-                raise_status(status, HL_ERR_DEVICE_BOUNDS);
-                count = kMaxPerTile;
-            }
-            list = grid.lists + size_t(tile) * kMaxPerTile;
-        } else {
-            raise_status(status, HL_ERR_DEVICE_BOUNDS);
-        }
-    } else {
-        const float nr = cam->position_near[3], fr = cam->forward_far[3];
-        const float d = div_(nr * fr, fma_(-t.depth, fr - nr, fr));
+    // the tile's froxel columns, and the tile grid's list
+    uint32_t fx0 = 0, fy0 = 0, ncx = 1, ncols = 1, tile_base = 0, tile_len = 0;
+    bool key_by_column = false;
+    if (FROXELS) {
         const hl_froxel_params& fp = grid.fp;
-        uint32_t s = 0;
-        for (uint32_t step = 64; step > 0; step >>= 1)
-            if (s + step < fp.grid_z && s_tab[s + step] <= d) s += step;
-        const uint32_t fx = uint32_t((uint64_t(x) * fp.grid_x) / fp.width);
-        const uint32_t fy = uint32_t((uint64_t(y) * fp.grid_y) / fp.height);
-        const uint32_t f = (fy * fp.grid_x + fx) * fp.grid_z + s;
-        const uint32_t b = grid.counts[f], e = grid.counts[f + 1];
-        if (b <= e && e <= grid.lists_capacity) {
-            list = grid.lists + b;
-            count = e - b;
-        } else {
+        const uint32_t xe = min(x0 + TW, gb.width) - 1, ye = min(y0 + TH, gb.height) - 1;
+        fx0 = (x0 * fp.grid_x) / fp.width;
+        fy0 = (y0 * fp.grid_y) / fp.height;
+        ncx = (xe * fp.grid_x) / fp.width - fx0 + 1;
+        ncols = ncx * ((ye * fp.grid_y) / fp.height - fy0 + 1);
+        key_by_column = ncols * fp.grid_z <= uint32_t(kBins);
+    } else {
+        const uint32_t tile = blockIdx.y * glb->num_tiles_x + blockIdx.x;
+        if (tile < grid.tiles) {
+            tile_len = __ldg(grid.counts + tile);
+            if (tile_len > kMaxPerTile) {
+                if (t == 0) raise_status(status, HL_ERR_DEVICE_BOUNDS);
+                tile_len = kMaxPerTile;
+            }
+            tile_base = tile * kMaxPerTile;
+        } else if (t == 0) {
             raise_status(status, HL_ERR_DEVICE_BOUNDS);
         }
     }
+    __syncthreads();
 
-    float sr = 0.0f, sg = 0.0f, sb = 0.0f, cr = 0.0f, cg = 0.0f, cb = 0.0f;
-    uint32_t n_range = 0, n_full = 0;
-    for (uint32_t j = 0; j < count; ++j) {
-        const uint32_t idx = __ldg(list + j);
-        if (idx >= n_lights) {
-            raise_status(status, HL_ERR_DEVICE_BOUNDS);
+    // ---- 1. pixel set-up -------------------------------------------------------
+    float rel[12], wrow[4];
+    if (!PRECISE) camera_relative_rows(cam->inv_view_proj, camx, camy, camz, rel, wrow);
+    const float iW = rcp_(W), iH = rcp_(H);
+    bool valid[PPT];
+    uint32_t key[PPT], slot[PPT];
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+        const uint32_t i = t + k * kThreads;
+        const uint32_t x = x0 + i % TW, y = y0 + i / TW;
+        valid[k] = false;
+        key[k] = 0;
+        slot[k] = 0;
+        if (x < gb.width && y < gb.height) {
+            const Texel<LAYOUT> tx = load_texel<LAYOUT>(gb, x, y);
+            valid[k] = tx.depth < 1.0f;
+            if (valid[k]) {
+                Pixel p;
+                float guard = 0.0f;
+                if (PRECISE) {
+                    reconstruct<true>(cam->inv_view_proj, x, y, W, H, tx.depth, p.Px, p.Py, p.Pz, p.Plx, p.Ply, p.Plz);
+                    finish_pixel<true>(p, tx.nx, tx.ny, tx.nz, tx.ar, tx.ag, tx.ab, tx.rough, tx.metal, tx.f0r, tx.f0g,
+                                       tx.f0b, camx, camy, camz);
+                } else {
+                    const float ndx = fma_(float(2u * x + 1u), iW, -1.0f);
+                    const float ndy = fma_(float(2u * y + 1u), -iH, 1.0f);
+                    reconstruct_relative(rel, wrow, ndx, ndy, tx.depth, p.Px, p.Py, p.Pz);
+                    p.Plx = p.Ply = p.Plz = 0.0f;
+                    finish_pixel<false>(p, tx.nx, tx.ny, tx.nz, tx.ar, tx.ag, tx.ab, tx.rough, tx.metal, tx.f0r,
+                                        tx.f0g, tx.f0b, 0.0f, 0.0f, 0.0f);
+                    guard = fast_guard(p);
+                    if (p.NdV < kFastMinNdV) {
+                        // grazing view: precise set-up, camera-relative double-float position
+                        reconstruct<true>(cam->inv_view_proj, x, y, W, H, tx.depth, p.Px, p.Py, p.Pz, p.Plx, p.Ply,
+                                          p.Plz);
+                        const DF ax = two_sum(p.Px, -camx), ay = two_sum(p.Py, -camy), az = two_sum(p.Pz, -camz);
+                        const DF bx = two_sum(ax.hi, ax.lo + p.Plx), by = two_sum(ay.hi, ay.lo + p.Ply),
+                                 bz = two_sum(az.hi, az.lo + p.Plz);
+                        p.Px = bx.hi; p.Plx = bx.lo; p.Py = by.hi; p.Ply = by.lo; p.Pz = bz.hi; p.Plz = bz.lo;
+                        finish_pixel<true>(p, tx.nx, tx.ny, tx.nz, tx.ar, tx.ag, tx.ab, tx.rough, tx.metal, tx.f0r,
+                                           tx.f0g, tx.f0b, 0.0f, 0.0f, 0.0f);
+                        guard = 0.0f;
+                    }
+                }
+                store_pixel(s, i, p, pixel_brdf(p), guard, tx.depth, tx.ar, tx.ag, tx.ab);
+                uint32_t b = tile_base, n = tile_len;
+                if (FROXELS) {
+                    // own froxel: column of (x, y), slice of the linear view depth
+                    const float nr = cam->position_near[3], fr = cam->forward_far[3];
+                    const float dv = div_(nr * fr, fma_(-tx.depth, fr - nr, fr));
+                    const hl_froxel_params& fp = grid.fp;
+                    uint32_t sl = 0;
+                    for (uint32_t step = 64; step > 0; step >>= 1)
+                        if (sl + step < fp.grid_z && s.tab[sl + step] <= dv) sl += step;
+                    const uint32_t fx = (x * fp.grid_x) / fp.width;
+                    const uint32_t fy = (y * fp.grid_y) / fp.height;
+                    const uint32_t f = (fy * fp.grid_x + fx) * fp.grid_z + sl;
+                    b = __ldg(grid.counts + f);
+                    const uint32_t e = __ldg(grid.counts + f + 1);
+                    if (b <= e && e <= grid.lists_capacity) {
+                        n = e - b;
+                    } else {
+                        raise_status(status, HL_ERR_DEVICE_BOUNDS);
+                        n = 0;
+                    }
+                    key[k] = key_by_column ? sl * ncols + (fy - fy0) * ncx + (fx - fx0) : sl;
+                }
+                s.base[i] = b;
+                s.len[i] = n;
+                if (STATS) cnt[3][i] = n;
+                slot[k] = atomicAdd(&s.hist[key[k]], 1u);
+            }
+        }
+    }
+    __syncthreads();
+    {   // exclusive scan of the froxel-key histogram, two bins per thread
+        const uint32_t a = s.hist[2 * t], b = s.hist[2 * t + 1];
+        uint32_t v = a + b;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t n = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= uint32_t(o)) v += n;
+        }
+        if (lane == 31) s.warp_tot[warp] = v;
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t wt = s.warp_tot[w];
+            before += (uint32_t(w) < warp) ? wt : 0u;
+            total += wt;
+        }
+        const uint32_t excl = before + v - (a + b);
+        __syncthreads();
+        s.hist[2 * t] = excl;
+        s.hist[2 * t + 1] = excl + a;
+        if (t == 0) s.n_valid = total;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < PPT; ++k)
+        if (valid[k]) s.order[s.hist[key[k]] + slot[k]] = uint16_t(t + k * kThreads);
+    __syncthreads();
+
+    // ---- 2-4. groups of 32 sorted pixels walk their lists --------------------------
+    const uint32_t n_valid = s.n_valid;
+    uint32_t qlen = 0;
+    uint32_t* queue = s.queue[warp];
+
+    uint32_t head = 0;  // ring position of the oldest pending pair
+
+#pragma unroll 1
+    for (int gi = 0; gi < NG / kWarps; ++gi) {
+        // warp w takes group w and, with 16 groups, group 15 - w (a light and a heavy one)
+        const uint32_t g = gi == 0 ? warp : uint32_t(NG - 1) - warp;
+        const uint32_t gs = g * 32 + lane;
+        const bool own = gs < n_valid;
+        const uint32_t i = own ? s.order[gs] : 0u;
+        float px = 0, py = 0, pz = 0, plx = 0, ply = 0, plz = 0, nx = 0, ny = 0, nz = 0, slack = 0;
+        uint32_t lb = 0, ln = 0;
+        if (own) {
+            px = s.px[F_PX][i]; py = s.px[F_PY][i]; pz = s.px[F_PZ][i];
+            plx = s.px[F_PLX][i]; ply = s.px[F_PLY][i]; plz = s.px[F_PLZ][i];
+            nx = s.px[F_NX][i]; ny = s.px[F_NY][i]; nz = s.px[F_NZ][i];
+            // |N.t| within |P| 2^-20 of zero is left to the exact NdL cut
+            slack = fma_(pz, pz, fma_(py, py, px * px)) * (1.0f / 1099511627776.0f);
+            lb = s.base[i];
+            ln = s.len[i];
+        }
+        const uint32_t maxlen = __reduce_max_sync(0xffffffffu, ln);
+        for (uint32_t j0 = 0; j0 < maxlen; j0 += kPipe) {
+            uint32_t li[kPipe];
+            float4 a[kPipe];
+            uint32_t ty[kPipe];
+#pragma unroll
+            for (int u = 0; u < kPipe; ++u) li[u] = (j0 + u < ln) ? __ldg(grid.lists + lb + j0 + u) : 0xffffffffu;
+#pragma unroll
+            for (int u = 0; u < kPipe; ++u) {
+                const bool ok = li[u] < n_lights;
+                a[u] = ok ? __ldg(reinterpret_cast<const float4*>(lights + li[u])) : make_float4(0, 0, 0, 0);
+                ty[u] = ok ? __ldg(reinterpret_cast<const uint32_t*>(lights + li[u]) + 13) : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < kPipe; ++u) {
+                if (j0 + u >= maxlen) break;  // warp-uniform
+                bool pass = false;
+                if (j0 + u < ln) {
+                    if (li[u] >= n_lights) {
+                        raise_status(status, HL_ERR_DEVICE_BOUNDS);
+                    } else if (ty[u] == 0u) {
+                        pass = true;
+                    } else {
+                        const float lx = PRECISE ? a[u].x : a[u].x - camx, ly = PRECISE ? a[u].y : a[u].y - camy,
+                                    lz = PRECISE ? a[u].z : a[u].z - camz;
+                        pass = candidate(px, py, pz, plx, ply, plz, nx, ny, nz, lx, ly, lz,
+                                         a[u].w * a[u].w * (1.0f + 1.0f / 512.0f), slack, !STATS);
+                    }
+                }
+                const uint32_t pm = __ballot_sync(0xffffffffu, pass);
+                if (pass) queue[(head + qlen + __popc(pm & lanemask_lt())) & (kQueue - 1)] = (i << 23) | li[u];
+                qlen += __popc(pm);
+            }
+            __syncwarp();
+            while (qlen >= 32) {
+                flush_batch<LAYOUT, STATS, TW, NPX>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H);
+                head += 32;
+                qlen -= 32;
+            }
+        }
+    }
+    if (qlen > 0) flush_batch<LAYOUT, STATS, TW, NPX>(s, queue, head, qlen, lane, cam, lights, x0, y0, W, H);
+
+    // ---- 5. output -----------------------------------------------------------------
+    __syncthreads();
+    const uint32_t debug_mode = glb->debug_mode;
+    if (!STATS && t == 0 && (glb->has_rc_gi != 0u || debug_mode == 10u || debug_mode == 11u))
+        raise_status(status, HL_ERR_NOT_SUPPORTED);
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+        const uint32_t i = t + k * kThreads;
+        const uint32_t x = x0 + i % TW, y = y0 + i / TW;
+        if (x >= gb.width || y >= gb.height) continue;
+        if (STATS) {
+            uint32_t* o = stats + (size_t(y) * gb.width + x) * 3;
+            if (valid[k]) {
+                o[0] = cnt[3][i];
+                o[1] = cnt[1][i];
+                o[2] = cnt[2][i];
+            } else {
+                o[0] = o[1] = o[2] = 0;
+            }
             continue;
         }
-        const ShadeLight l = load_light(lights, idx);
-        if (STATS && in_range(p, l)) ++n_range;
-        float r, g, b;
-        if (eval<PRECISE>(p, brdf, l, r, g, b)) {
-            kahan_add(sr, cr, r);
-            kahan_add(sg, cg, g);
-            kahan_add(sb, cb, b);
-            ++n_full;
+        if (!valid[k]) continue;
+        // albedo from the record; ao, emissive and alpha exist only in the reference layout
+        Texel<LAYOUT> tx;
+        if (LAYOUT == HL_GBUF_REFERENCE) {
+            tx = load_texel<LAYOUT>(gb, x, y);
+        } else {
+            tx.ar = s.px[F_AR][i];
+            tx.ag = s.px[F_AG][i];
+            tx.ab = s.px[F_AB][i];
+            tx.ao = 1.0f;
+            tx.alpha = 1.0f;
+            tx.er = tx.eg = tx.eb = 0.0f;
         }
-    }
-    if (STATS) {
-        uint32_t* s = stats + (size_t(y) * gb.width + x) * 3;
-        s[0] = count;
-        s[1] = n_range;
-        s[2] = n_full;
-        return;
-    }
-
-    // Hemisphere ambient (deferred_lighting.wgsl:1196-1199) times ao (x white SSAO).
-    const float amb = glb->ambient_intensity;
-    const float skr = glb->ambient_color[0] * amb, skg = glb->ambient_color[1] * amb, skb = glb->ambient_color[2] * amb;
-    const float ht = fma_(p.Ny, 0.5f, 0.5f);
-    const float hr = fma_(skr, ht, skr * 0.15f * (1.0f - ht)) * t.ar;
-    const float hg = fma_(skg, ht, skg * 0.15f * (1.0f - ht)) * t.ag;
-    const float hb = fma_(skb, ht, skb * 0.15f * (1.0f - ht)) * t.ab;
-    float4 c;
-    c.x = (sr + fma_(hr, t.ao, 0.0f)) + t.er;
-    c.y = (sg + fma_(hg, t.ao, 0.0f)) + t.eg;
-    c.z = (sb + fma_(hb, t.ao, 0.0f)) + t.eb;
-    c.w = t.alpha;
-    if (debug_mode == 1u || debug_mode == 2u || debug_mode == 4u || debug_mode == 20u || debug_mode == 21u) {
-        c = make_float4(t.ar, t.ag, t.ab, t.alpha);
-    } else if (debug_mode == 5u) {
-        c = make_float4(fma_(p.Nx, 0.5f, 0.5f), fma_(p.Ny, 0.5f, 0.5f), fma_(p.Nz, 0.5f, 0.5f), 1.0f);
-    }
-    unsigned char* row = out.data + out.pitch * y;
-    if (TARGET == HL_TARGET_RGBA32F) {
-        reinterpret_cast<float4*>(row)[x] = c;
-    } else {
-        const __half2 lo = __floats2half2_rn(c.x, c.y), hi = __floats2half2_rn(c.z, c.w);
-        uint2 v;
-        v.x = *reinterpret_cast<const uint32_t*>(&lo);
-        v.y = *reinterpret_cast<const uint32_t*>(&hi);
-        reinterpret_cast<uint2*>(row)[x] = v;
+        const float ny = s.px[F_NY][i];
+        const float amb = glb->ambient_intensity;
+        const float skr = glb->ambient_color[0] * amb, skg = glb->ambient_color[1] * amb,
+                    skb = glb->ambient_color[2] * amb;
+        const float ht = fma_(ny, 0.5f, 0.5f);
+        // hemisphere ambient (deferred_lighting.wgsl:1196-1199) times ao (x white SSAO)
+        const float hr = fma_(skr, ht, skr * 0.15f * (1.0f - ht)) * tx.ar;
+        const float hg = fma_(skg, ht, skg * 0.15f * (1.0f - ht)) * tx.ag;
+        const float hb = fma_(skb, ht, skb * 0.15f * (1.0f - ht)) * tx.ab;
+        float4 c;
+        c.x = (s.acc[0][i] + fma_(hr, tx.ao, 0.0f)) + tx.er;
+        c.y = (s.acc[1][i] + fma_(hg, tx.ao, 0.0f)) + tx.eg;
+        c.z = (s.acc[2][i] + fma_(hb, tx.ao, 0.0f)) + tx.eb;
+        c.w = tx.alpha;
+        if (debug_mode == 1u || debug_mode == 2u || debug_mode == 4u || debug_mode == 20u || debug_mode == 21u) {
+            c = make_float4(tx.ar, tx.ag, tx.ab, tx.alpha);
+        } else if (debug_mode == 5u) {
+            c = make_float4(fma_(s.px[F_NX][i], 0.5f, 0.5f), fma_(ny, 0.5f, 0.5f), fma_(s.px[F_NZ][i], 0.5f, 0.5f),
+                            1.0f);
+        }
+        unsigned char* row = out.data + out.pitch * y;
+        if (TARGET == HL_TARGET_RGBA32F) {
+            reinterpret_cast<float4*>(row)[x] = c;
+        } else {
+            const __half2 lo = __floats2half2_rn(c.x, c.y), hi = __floats2half2_rn(c.z, c.w);
+            uint2 v;
+            v.x = *reinterpret_cast<const uint32_t*>(&lo);
+            v.y = *reinterpret_cast<const uint32_t*>(&hi);
+            reinterpret_cast<uint2*>(row)[x] = v;
+        }
     }
 }
 
@@ -237,11 +548,22 @@ template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS>
 cudaError_t launch_one(const void* camera, const void* globals, const GBufView& gb, const void* lights, uint32_t n,
                        const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats, int* status,
                        cudaStream_t stream) {
-    const dim3 block(kShadeTile, kShadeTile);
-    const dim3 g((gb.width + kShadeTile - 1) / kShadeTile, (gb.height + kShadeTile - 1) / kShadeTile);
-    shade_kernel<LAYOUT, GRID, TARGET, STATS><<<g, block, 0, stream>>>(
-        static_cast<const GpuCamera*>(camera), static_cast<const DeferredGlobals*>(globals), gb,
-        static_cast<const GpuLight*>(lights), n, grid, tab, out, stats, status);
+    constexpr bool FROXELS = (GRID == HL_GRID_FROXELS);
+    constexpr int TW = FROXELS ? 32 : 16, TH = 16;
+    auto kern = shade_kernel<LAYOUT, GRID, TARGET, STATS, TW, TH>;
+    const int smem = int(sizeof(sk::Smem<TW * TH>));
+    static unsigned long long attr_devices = 0;  // devices on which the smem limit is raised
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 64 && !(attr_devices & (1ull << dev))) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr_devices |= 1ull << dev;
+    }
+    const dim3 g((gb.width + TW - 1) / TW, (gb.height + TH - 1) / TH);
+    kern<<<g, sk::kThreads, smem, stream>>>(static_cast<const GpuCamera*>(camera),
+                                            static_cast<const DeferredGlobals*>(globals), gb,
+                                            static_cast<const GpuLight*>(lights), n, grid, tab, out, stats, status);
     return cudaGetLastError();
 }
 
@@ -249,10 +571,14 @@ template <uint32_t LAYOUT, uint32_t GRID>
 cudaError_t dispatch_target(uint32_t target, const void* camera, const void* globals, const GBufView& gb,
                             const void* lights, uint32_t n, const GridView& grid, const SliceTable& tab,
                             const TargetView& out, uint32_t* stats, int* status, cudaStream_t stream) {
-    if (stats) return launch_one<LAYOUT, GRID, HL_TARGET_RGBA32F, true>(camera, globals, gb, lights, n, grid, tab, out, stats, status, stream);
+    if (stats)
+        return launch_one<LAYOUT, GRID, HL_TARGET_RGBA32F, true>(camera, globals, gb, lights, n, grid, tab, out, stats,
+                                                                 status, stream);
     if (target == HL_TARGET_RGBA16F)
-        return launch_one<LAYOUT, GRID, HL_TARGET_RGBA16F, false>(camera, globals, gb, lights, n, grid, tab, out, stats, status, stream);
-    return launch_one<LAYOUT, GRID, HL_TARGET_RGBA32F, false>(camera, globals, gb, lights, n, grid, tab, out, stats, status, stream);
+        return launch_one<LAYOUT, GRID, HL_TARGET_RGBA16F, false>(camera, globals, gb, lights, n, grid, tab, out,
+                                                                  stats, status, stream);
+    return launch_one<LAYOUT, GRID, HL_TARGET_RGBA32F, false>(camera, globals, gb, lights, n, grid, tab, out, stats,
+                                                              status, stream);
 }
 
 template <uint32_t LAYOUT>
@@ -261,8 +587,10 @@ cudaError_t dispatch_grid(uint32_t grid_kind, uint32_t target, const void* camer
                           const SliceTable& tab, const TargetView& out, uint32_t* stats, int* status,
                           cudaStream_t stream) {
     if (grid_kind == HL_GRID_FROXELS)
-        return dispatch_target<LAYOUT, HL_GRID_FROXELS>(target, camera, globals, gb, lights, n, grid, tab, out, stats, status, stream);
-    return dispatch_target<LAYOUT, HL_GRID_TILES>(target, camera, globals, gb, lights, n, grid, tab, out, stats, status, stream);
+        return dispatch_target<LAYOUT, HL_GRID_FROXELS>(target, camera, globals, gb, lights, n, grid, tab, out, stats,
+                                                        status, stream);
+    return dispatch_target<LAYOUT, HL_GRID_TILES>(target, camera, globals, gb, lights, n, grid, tab, out, stats,
+                                                  status, stream);
 }
 
 }  // namespace
@@ -273,11 +601,14 @@ cudaError_t launch_shade(uint32_t layout, uint32_t grid_kind, uint32_t target_fo
                          int* status, cudaStream_t stream) {
     switch (layout) {
         case HL_GBUF_REFERENCE:
-            return dispatch_grid<HL_GBUF_REFERENCE>(grid_kind, target_format, camera, globals, gb, lights, n_lights, grid, tab, out, stats, status, stream);
+            return dispatch_grid<HL_GBUF_REFERENCE>(grid_kind, target_format, camera, globals, gb, lights, n_lights,
+                                                    grid, tab, out, stats, status, stream);
         case HL_GBUF_F32:
-            return dispatch_grid<HL_GBUF_F32>(grid_kind, target_format, camera, globals, gb, lights, n_lights, grid, tab, out, stats, status, stream);
+            return dispatch_grid<HL_GBUF_F32>(grid_kind, target_format, camera, globals, gb, lights, n_lights, grid,
+                                              tab, out, stats, status, stream);
         default:
-            return dispatch_grid<HL_GBUF_F16>(grid_kind, target_format, camera, globals, gb, lights, n_lights, grid, tab, out, stats, status, stream);
+            return dispatch_grid<HL_GBUF_F16>(grid_kind, target_format, camera, globals, gb, lights, n_lights, grid,
+                                              tab, out, stats, status, stream);
     }
 }
 

@@ -76,6 +76,19 @@ HL_HD float rsqrt_(float x) {
     return 1.0f / std::sqrt(x);
 #endif
 }
+// Reciprocal from the hardware approximation refined by one Newton-Raphson step
+// (r' = r + r(1 - x r)), within ~1 ulp; the division a/b as a * rcpn_(b) is within
+// ~2 ulp. Used on the shading path where the f64 comparison tolerates it.
+HL_HD float rcpn_(float x) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return __fmaf_rn(__fmaf_rn(-x, r, 1.0f), r, r);
+#else
+    return 1.0f / x;
+#endif
+}
+HL_HD float divn_(float a, float b) { return a * rcpn_(b); }
 HL_HD float fmax_(float a, float b) { return a < b ? b : a; }
 HL_HD float fmin_(float a, float b) { return b < a ? b : a; }
 HL_HD float clamp01(float x) { return fmin_(fmax_(x, 0.0f), 1.0f); }
@@ -125,10 +138,35 @@ HL_HD PixelBrdf pixel_brdf(const Pixel& p) {
     const float r1 = p.rough + 1.0f;
     b.k = (r1 * r1) * 0.125f;
     b.omk = 1.0f - b.k;
-    b.gv = div_(p.NdV, fma_(p.NdV, b.omk, b.k + 0.0001f));
+    b.gv = divn_(p.NdV, fma_(p.NdV, b.omk, b.k + 0.0001f));
     b.one_m_metal = 1.0f - p.metal;
     b.nv4 = 4.0f * p.NdV;
     return b;
+}
+
+// Camera-relative reconstruction rows: with M = inv_view_proj and c the camera
+// position, P - c = (M_r - c_r M_3) v / (M_3 v) for v = (ndc, depth, 1). The rows
+// M_r - c_r M_3 are each one fma (exact product, one rounding), so they carry no
+// cancellation for points far from the origin. rel[r*4 + k] = row r, w[k] = M_3.
+HL_HD void camera_relative_rows(const float* m, float cx, float cy, float cz, float* rel, float* w) {
+    const float c[3] = {cx, cy, cz};
+    for (int k = 0; k < 4; ++k) w[k] = m[4 * k + 3];
+    for (int r = 0; r < 3; ++r)
+        for (int k = 0; k < 4; ++k) rel[r * 4 + k] = fma_(-c[r], m[4 * k + 3], m[4 * k + r]);
+}
+
+// P - camera for a pixel centre, from the camera-relative rows (FMA rows; the
+// DirectX-style perspective makes the w row a single-rounding fma of depth).
+HL_HD void reconstruct_relative(const float* rel, const float* w, float ndc_x, float ndc_y, float depth, float& Px,
+                                float& Py, float& Pz) {
+    const float hw = fma_(w[2], depth, fma_(w[1], ndc_y, fma_(w[0], ndc_x, w[3])));
+    const float iw = rcpn_(hw);
+    float h[3];
+    for (int r = 0; r < 3; ++r)
+        h[r] = fma_(rel[r * 4 + 2], depth, fma_(rel[r * 4 + 1], ndc_y, fma_(rel[r * 4 + 0], ndc_x, rel[r * 4 + 3])));
+    Px = h[0] * iw;
+    Py = h[1] * iw;
+    Pz = h[2] * iw;
 }
 
 // World position of a pixel centre: inv_view_proj (column major, 16 floats) times
@@ -196,6 +234,7 @@ HL_HD void reconstruct(const float* m, uint32_t x, uint32_t y, float W, float H,
 
 // Finishes a Pixel from decoded G-buffer values (albedo, roughness, metallic, raw
 // normal, F0) and the camera position.
+template <bool PRECISE>
 HL_HD void finish_pixel(Pixel& p, float nx, float ny, float nz, float ar, float ag, float ab, float rough, float metal,
                         float f0r, float f0g, float f0b, float cx, float cy, float cz) {
     const float in = rsqrt_(fma_(nz, nz, fma_(ny, ny, nx * nx)));
@@ -206,22 +245,32 @@ HL_HD void finish_pixel(Pixel& p, float nx, float ny, float nz, float ar, float 
     p.Nx = nx * in;
     p.Ny = ny * in;
     p.Nz = nz * in;
-    // V = cam - P as normalised double-floats
-    const DF ux = two_sum(cx, -p.Px), uy = two_sum(cy, -p.Py), uz = two_sum(cz, -p.Pz);
-    const DF vx = two_sum(ux.hi, ux.lo - p.Plx), vy = two_sum(uy.hi, uy.lo - p.Ply), vz = two_sum(uz.hi, uz.lo - p.Plz);
-    const float iv = rsqrt_(fma_(vz.hi, vz.hi, fma_(vy.hi, vy.hi, vx.hi * vx.hi)));
-    p.Vx = vx.hi * iv;
-    p.Vy = vy.hi * iv;
-    p.Vz = vz.hi * iv;
-    // NdV = (n_raw . v) / (|n_raw| |v|) with a compensated dot product: at grazing
-    // view angles the specular term is proportional to NdV.
-    DF d = two_prod(nx, vx.hi);
-    const DF t1 = two_prod(ny, vy.hi), t2 = two_prod(nz, vz.hi);
-    const DF s1 = two_sum(d.hi, t1.hi);
-    const DF s2 = two_sum(s1.hi, t2.hi);
-    float lo = d.lo + t1.lo + t2.lo + s1.lo + s2.lo;
-    lo = fma_(nx, vx.lo, fma_(ny, vy.lo, fma_(nz, vz.lo, lo)));
-    p.NdV = fmax_((s2.hi + lo) * in * iv, 0.0f);
+    if (PRECISE) {
+        // V = cam - P as normalised double-floats
+        const DF ux = two_sum(cx, -p.Px), uy = two_sum(cy, -p.Py), uz = two_sum(cz, -p.Pz);
+        const DF vx = two_sum(ux.hi, ux.lo - p.Plx), vy = two_sum(uy.hi, uy.lo - p.Ply),
+                 vz = two_sum(uz.hi, uz.lo - p.Plz);
+        const float iv = rsqrt_(fma_(vz.hi, vz.hi, fma_(vy.hi, vy.hi, vx.hi * vx.hi)));
+        p.Vx = vx.hi * iv;
+        p.Vy = vy.hi * iv;
+        p.Vz = vz.hi * iv;
+        // NdV = (n_raw . v) / (|n_raw| |v|) with a compensated dot product: at grazing
+        // view angles the specular term is proportional to NdV.
+        DF d = two_prod(nx, vx.hi);
+        const DF t1 = two_prod(ny, vy.hi), t2 = two_prod(nz, vz.hi);
+        const DF s1 = two_sum(d.hi, t1.hi);
+        const DF s2 = two_sum(s1.hi, t2.hi);
+        float lo = d.lo + t1.lo + t2.lo + s1.lo + s2.lo;
+        lo = fma_(nx, vx.lo, fma_(ny, vy.lo, fma_(nz, vz.lo, lo)));
+        p.NdV = fmax_((s2.hi + lo) * in * iv, 0.0f);
+    } else {
+        const float vx = cx - p.Px, vy = cy - p.Py, vz = cz - p.Pz;
+        const float iv = rsqrt_(fma_(vz, vz, fma_(vy, vy, vx * vx)));
+        p.Vx = vx * iv;
+        p.Vy = vy * iv;
+        p.Vz = vz * iv;
+        p.NdV = fmax_(fma_(nz, vz, fma_(ny, vy, nx * vx)) * in * iv, 0.0f);
+    }
     p.f0r = fmin_(fmax_(f0r, 0.0f), 0.999f);
     p.f0g = fmin_(fmax_(f0g, 0.0f), 0.999f);
     p.f0b = fmin_(fmax_(f0b, 0.0f), 0.999f);
@@ -259,12 +308,14 @@ struct ShadeLight {
 
 // Cheap candidate test of phase 1: inside the range and in front of the surface.
 // Returns true when the pair may contribute; the exact cuts are re-applied by eval.
-HL_HD bool candidate(const Pixel& p, const ShadeLight& l) {
-    if (l.type == 0u) return true;
-    const float tx = (l.px - p.Px) - p.Plx, ty = (l.py - p.Py) - p.Ply, tz = (l.pz - p.Pz) - p.Plz;
+// r2m is the light's squared range widened by a relative margin; pairs whose N.to_light
+// is within sqrt(slack2) of zero are kept so the exact NdL cut decides them.
+HL_HD bool candidate(float px, float py, float pz, float plx, float ply, float plz, float nx, float ny, float nz,
+                     float lx, float ly, float lz, float r2m, float slack2, bool check_ndl) {
+    const float tx = (lx - px) - plx, ty = (ly - py) - ply, tz = (lz - pz) - plz;
     const float d2 = fma_(tz, tz, fma_(ty, ty, tx * tx));
-    const float ndl = fma_(p.Nz, tz, fma_(p.Ny, ty, p.Nx * tx));
-    return (d2 <= l.range * l.range * 1.00001f) && (ndl > 0.0f);
+    const float ndl = fma_(nz, tz, fma_(ny, ty, nx * tx));
+    return (d2 <= r2m) && (!check_ndl || ndl > 0.0f || ndl * ndl <= slack2);
 }
 
 // Range test of the reference's light loop (deferred_lighting.wgsl:1128-1131).
@@ -275,12 +326,30 @@ HL_HD bool in_range(const Pixel& p, const ShadeLight& l) {
     return d2 <= l.range * l.range;
 }
 
+// Results of eval().
+constexpr int kCut = 0;           // a cut applies: no contribution
+constexpr int kLit = 1;           // contribution written to out*
+constexpr int kNeedsPrecise = 2;  // fast path only: ill-conditioned pair, redo with PRECISE
+
+// Guard of the fast path, for a pixel whose camera-relative position P is a plain f32
+// value: its rounding (|P| 2^-24) turns the light direction by |P| 2^-24 / dist. The
+// guard G = |P|^2 2^-26 flags the pairs where that moves the result by more than
+// ~2^-11 relative: NdL dist < |P| 2^-13, dist < |P| 2^-12, or, near the end of the
+// range, falloff * dist < |P| 2^-11. Such pairs are re-evaluated on the precise path.
+HL_HD float fast_guard(const Pixel& p) {
+    return fma_(p.Pz, p.Pz, fma_(p.Py, p.Py, p.Px * p.Px)) * (1.0f / 67108864.0f);
+}
+// Pixels with NdV below this are set up on the precise path from the start.
+constexpr float kFastMinNdV = 1.0f / 8192.0f;
+
 // pbr_direct_light (deferred_lighting.wgsl:699-820) for a non-anisotropic, non-SSS
-// surface, sf = 1. Returns false (and leaves out untouched) when a cut applies.
+// surface, sf = 1. Returns kCut (out* untouched) when a cut applies, kLit with the
+// contribution in out*, or — on the fast path with guard > 0 — kNeedsPrecise.
 template <bool PRECISE>
-HL_HD bool eval(const Pixel& p, const PixelBrdf& b, const ShadeLight& l, float& outr, float& outg, float& outb) {
+HL_HD int eval(const Pixel& p, const PixelBrdf& b, const ShadeLight& l, float& outr, float& outg, float& outb,
+               float guard = 0.0f) {
     float Lx, Ly, Lz, rr, rg, rb;
-    float NdL;
+    float NdL, d2_near = 0.0f, fall_near = 1.0f;
     if (l.type == 0u) {
         const float il = rsqrt_(fma_(l.dz, l.dz, fma_(l.dy, l.dy, l.dx * l.dx)));
         Lx = -l.dx * il;
@@ -315,8 +384,8 @@ HL_HD bool eval(const Pixel& p, const PixelBrdf& b, const ShadeLight& l, float& 
             const DF rr2 = two_prod(l.range, l.range);
             const DF diff = two_sum(rr2.hi, -acc2.hi);
             const float gap = diff.hi + (diff.lo + (rr2.lo - lo));
-            if (gap < 0.0f) return false;  // dist > range
-            fall = div_(gap * (r2 + d2), r2 * r2);
+            if (gap < 0.0f) return kCut;  // dist > range
+            fall = divn_(gap * (r2 + d2), r2 * r2);
             // n_raw . to_light, compensated: at grazing light angles the diffuse and
             // specular terms are proportional to NdL.
             const DF q1 = two_prod(p.nrx, tx), q2 = two_prod(p.nry, ty), q3 = two_prod(p.nrz, tz);
@@ -326,20 +395,22 @@ HL_HD bool eval(const Pixel& p, const PixelBrdf& b, const ShadeLight& l, float& 
             cl = fma_(p.nrx, ex, fma_(p.nry, ey, fma_(p.nrz, ez, cl)));
             ntl = c2.hi + cl;
         } else {
-            tx = l.px - p.Px;
-            ty = l.py - p.Py;
-            tz = l.pz - p.Pz;
+            tx = (l.px - p.Px) - p.Plx;
+            ty = (l.py - p.Py) - p.Ply;
+            tz = (l.pz - p.Pz) - p.Plz;
             d2 = fma_(tz, tz, fma_(ty, ty, tx * tx));
-            if (d2 > r2) return false;
-            const float nd2 = d2 * rcp_(r2);
+            if (d2 > r2) return kCut;
+            const float nd2 = d2 * rcpn_(r2);
             fall = fmax_(0.0f, fma_(-nd2, nd2, 1.0f));
         }
+        d2_near = d2;
+        fall_near = fall;
         const float inv_d = rsqrt_(d2);
         Lx = tx * inv_d;
         Ly = ty * inv_d;
         Lz = tz * inv_d;
         NdL = PRECISE ? ntl * p.inv_n * inv_d : fma_(p.Nz, Lz, fma_(p.Ny, Ly, p.Nx * Lx));
-        float atten = rcp_(d2 + 0.0001f) * fall;
+        float atten = rcpn_(d2 + 0.0001f) * fall;
         if (l.type == 2u) {
             const float cos_a = -fma_(Lz, l.dz, fma_(Ly, l.dy, Lx * l.dx));
             const float t = clamp01(div_(cos_a - l.cos_outer, l.cos_inner - l.cos_outer));
@@ -350,8 +421,13 @@ HL_HD bool eval(const Pixel& p, const PixelBrdf& b, const ShadeLight& l, float& 
         rg = l.cg * ia;
         rb = l.cb * ia;
     }
-    if (!(NdL > 0.0f)) return false;
-    if (rr < kRadianceCut && rg < kRadianceCut && rb < kRadianceCut) return false;
+    if (!PRECISE && guard > 0.0f && l.type != 0u) {
+        const float ndl2d2 = NdL * NdL * d2_near;
+        if (ndl2d2 < guard || d2_near < 4.0f * guard || fall_near * fall_near * d2_near < 16.0f * guard)
+            return kNeedsPrecise;
+    }
+    if (!(NdL > 0.0f)) return kCut;
+    if (rr < kRadianceCut && rg < kRadianceCut && rb < kRadianceCut) return kCut;
     // H = normalize(V + L)
     const float hx = p.Vx + Lx, hy = p.Vy + Ly, hz = p.Vz + Lz;
     const float ih = rsqrt_(fma_(hz, hz, fma_(hy, hy, hx * hx)));
@@ -374,17 +450,17 @@ HL_HD bool eval(const Pixel& p, const PixelBrdf& b, const ShadeLight& l, float& 
     } else {
         den = 1.0f;
     }
-    const float D = div_(b.a2, fma_(kPi * den, den, 0.0001f));
+    const float D = divn_(b.a2, fma_(kPi * den, den, 0.0001f));
     // Smith-Schlick G
-    const float gl = div_(NdL, fma_(NdL, b.omk, b.k + 0.0001f));
+    const float gl = divn_(NdL, fma_(NdL, b.omk, b.k + 0.0001f));
     const float G = b.gv * gl;
-    const float spec = div_(D * G, fma_(b.nv4, NdL, 0.0001f));
+    const float spec = divn_(D * G, fma_(b.nv4, NdL, 0.0001f));
     // (kD * albedo / pi + spec * F) * radiance * NdL
     const float wr = rr * NdL, wg = rg * NdL, wb = rb * NdL;
     outr = fma_((1.0f - Fr) * b.one_m_metal, p.dr, spec * Fr) * wr;
     outg = fma_((1.0f - Fg) * b.one_m_metal, p.dg, spec * Fg) * wg;
     outb = fma_((1.0f - Fb) * b.one_m_metal, p.db, spec * Fb) * wb;
-    return true;
+    return kLit;
 }
 
 // Kahan (compensated) accumulation of one channel.

@@ -123,9 +123,13 @@ def test_shade_uses_gpu_lists(ctx):
     off, idx, keep = gpu_bin_froxels(ctx, w.camera.record, w.lights, p, capacity=1 << 20)
     cam_t, lt_t, d_off, d_idx, fp, cap = keep
     df = FR.upload_workload(w)
-    img = gpu_shade(ctx, df, N.froxel_grid_struct(d_idx, d_off, fp, cap))
-    ref = oracle.shade(w.camera.record, w.globals_, w.gbuffer, w.lights, ("froxels", idx, off, p))
-    e = metrics.radiance_error(img, ref)
+    grid = N.froxel_grid_struct(d_idx, d_off, fp, cap)
+    img = gpu_shade(ctx, df, grid)
+    st = gpu_shade(ctx, df, grid, stats=True)
+    ref, pc = oracle.shade(w.camera.record, w.globals_, w.gbuffer, w.lights, ("froxels", idx, off, p),
+                           pair_counts=True)
+    e = metrics.radiance_error(img, ref, st[..., 2], pc[..., 2])
+    assert e["flips"] <= max(2, 1e-4 * e["n"]), e
     assert e["max"] <= 2e-3, e
 
 
