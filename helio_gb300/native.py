@@ -82,7 +82,7 @@ EXPORTS = [
     "hl_abi_version", "hl_status_string", "hl_create", "hl_destroy", "hl_last_error_message", "hl_sync_status",
     "hl_tile_count", "hl_bin_tiles_ref", "hl_froxel_slice_table", "hl_bin_froxels", "hl_shade", "hl_shade_stats",
     "hl_shade_adjoint", "hl_batch_plan_create", "hl_batch_execute", "hl_batch_plan_view_grid",
-    "hl_batch_plan_destroy", "hl_probe_fp32_peak",
+    "hl_batch_plan_destroy", "hl_probe_fp32_peak", "hl_bin_froxels_noalloc",
 ]
 
 _lock = threading.Lock()
@@ -147,6 +147,8 @@ def _bind(l):
     l.hl_batch_plan_destroy.restype = i32
     l.hl_probe_fp32_peak.argtypes = [vp, P(C.c_double)]
     l.hl_probe_fp32_peak.restype = i32
+    l.hl_bin_froxels_noalloc.argtypes = [vp, vp, u32, P(FroxelParams), P(FroxelLists), vp]
+    l.hl_bin_froxels_noalloc.restype = i32
 
 
 def status_string(status: int) -> str:
@@ -291,3 +293,20 @@ def target_struct(data, fmt: int = TARGET_RGBA32F, pitch: int | None = None) -> 
     t.pitch = int(pitch if pitch is not None else data.stride(0) * data.element_size())
     t.format = fmt
     return t
+
+
+NOALLOC_MAX_LIGHTS = 4096
+NOALLOC_MAX_FROXELS = 32768
+
+
+def bin_froxels_noalloc(camera, lights, n_lights, params: FroxelParams, offsets, indices, capacity, stream=None):
+    """Froxel clustering without a context and without device allocation, for callers
+    that cannot allocate (their frame runs inside a stream capture, or a pool owns all
+    device memory). Scratch lives in one static device array of the library, so calls
+    that overlap on the GPU race; make the first call on a device before any capture.
+    Raises HelioError (HL_ERR_SIZE beyond NOALLOC_MAX_LIGHTS / NOALLOC_MAX_FROXELS)."""
+    out = FroxelLists(_ptr(offsets), _ptr(indices), capacity, 0)
+    st = load().hl_bin_froxels_noalloc(_ptr(camera), _ptr(lights), n_lights, C.byref(params), C.byref(out),
+                                       _stream(stream))
+    if st != HL_OK:
+        raise HelioError(st, f"hl_bin_froxels_noalloc: {status_string(st)}")

@@ -150,6 +150,27 @@ hl_status hl_bin_froxels(hl_ctx* ctx, const void* camera, const void* lights, ui
                          const hl_froxel_params* params, const hl_froxel_lists* out,
                          void* stream);
 
+/* Froxel clustering for callers that cannot allocate device memory. No counterpart in
+ * the reference. hl_bin_froxels takes its scratch space from the context, which grows
+ * it with cudaMalloc; a caller whose frame runs inside a CUDA stream capture (where
+ * allocation is not allowed), or whose device memory is all owned by its own pool
+ * under a fixed budget, cannot let the library allocate. This entry point needs no
+ * context and allocates nothing: it produces the same lists as hl_bin_froxels, with
+ * its scratch in one static device array of HL_NOALLOC_MAX_LIGHTS light records and
+ * HL_NOALLOC_MAX_FROXELS counts (320 KiB, held by every GPU that loads the library
+ * until the process exits). Larger requests return HL_ERR_SIZE.
+ *   - The first call on a device looks the array's address up (cudaGetSymbolAddress,
+ *     with that device current); make that first call before any stream capture.
+ *   - All calls share the array: calls that overlap on the GPU (different streams or
+ *     host threads) race and must be serialised by the caller.
+ *   - There is no device status word: a total above `capacity` shows as
+ *     offsets[F] > capacity (indices are written only below capacity). */
+#define HL_NOALLOC_MAX_LIGHTS 4096u
+#define HL_NOALLOC_MAX_FROXELS 32768u
+hl_status hl_bin_froxels_noalloc(const void* camera, const void* lights, uint32_t n_lights,
+                                 const hl_froxel_params* params, const hl_froxel_lists* out,
+                                 void* stream);
+
 /* ---------------------------------------------------------------------------------
  * Deferred lighting — the reference's DeferredLightPass (fs_main)
  * -------------------------------------------------------------------------------*/
