@@ -367,9 +367,129 @@ def run_ours(args, world, rank, local):
         off_g = offsets.cpu().numpy().view(np.uint32)
         line["error_vs_fp64_oracle"] = {k: (round(v, 9) if isinstance(v, float) else v) for k, v in e.items()}
         line["error_vs_fp64_oracle"]["lists_bit_exact"] = bool(np.array_equal(off_g, off_o))
+    if rank == 0 and not args.no_forms:
+        line["forms"] = run_forms(ctx, dev, stream, flush)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
+
+
+def _median_ms(fn, stream, flush, reps, warm=3):
+    import torch
+
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    ts = []
+    for k in range(reps):
+        flush.fill_(float(k))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        ts.append(a.elapsed_time(b))
+    return statistics.median(ts)
+
+
+def run_forms(ctx, dev, stream, flush):
+    """The three other forms of the path, each timed with CUDA events (L2 flushed):
+    adjoint (w4), batched views (w3) and the FP16/FP32 G-buffer precision pair."""
+    import torch
+
+    from helio_gb300 import frame as FR
+    from helio_gb300 import layouts as L
+    from helio_gb300 import native as N
+    from helio_gb300 import synthetic as S
+
+    sh = stream.cuda_stream
+    forms = {}
+
+    # ---- adjoint: w4, 1920x1080 FP32 G-buffer, 256 point lights ----
+    w = S.workload(4)
+    W, H = w.gbuffer.width, w.gbuffer.height
+    fp = N.froxel_params_from_numpy(L.froxel_params(*w.froxel_grid, W, H, w.camera.far))
+    F = fp.grid_x * fp.grid_y * fp.grid_z
+    df = FR.upload_workload(w, dev)
+    cap = F * max(df.n_lights, 1)
+    off = torch.zeros(F + 1, dtype=torch.int32, device=dev)
+    idx = torch.zeros(cap, dtype=torch.int32, device=dev)
+    rad = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
+    grid = N.froxel_grid_struct(idx, off, fp, cap)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(4)
+    d_rad = torch.randn((H, W, 4), dtype=torch.float32, device=dev, generator=gen)
+    d_l = torch.zeros((df.n_lights, 7), dtype=torch.float64, device=dev)
+    d_p = torch.zeros((H, W, 5), dtype=torch.float32, device=dev)
+
+    def fwd():
+        ctx.bin_froxels(df.camera, df.lights, df.n_lights, fp, off, idx, cap, sh)
+        ctx.shade(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, N.target_struct(rad), sh)
+
+    def adj():
+        ctx.shade_adjoint(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, d_rad, W * 16, d_l, d_p,
+                          sh)
+
+    t_f = _median_ms(fwd, stream, flush, 50)
+    t_a = _median_ms(adj, stream, flush, 50)
+    ctx.sync_status(sh)
+    first = d_l.clone()
+    adj()
+    torch.cuda.synchronize()
+    forms["adjoint"] = {
+        "workload": "w4: 1920x1080 FP32 G-buffer, 256 point lights, froxels 16x9x24",
+        "fwd_ms": round(t_f, 4), "adjoint_ms": round(t_a, 4),
+        "fwd_plus_adjoint_over_fwd": round((t_f + t_a) / t_f, 3),
+        "fwd_plus_adjoint_mpix_s": round(W * H / ((t_f + t_a) / 1e3) / 1e6, 1),
+        "deterministic": bool(torch.equal(first, d_l)),
+    }
+    del df, off, idx, rad, d_rad, d_l, d_p
+
+    # ---- batched: w3, 96 cube faces + 1080p + 720p, 2048 lights ----
+    views, lights = S.batched_views()
+    glb = L.make_globals(1, len(lights), ambient_color=(0.4, 0.45, 0.5), ambient_intensity=0.3)
+    d_lights, d_glb = FR.bytes_tensor(lights, dev), FR.bytes_tensor(glb, dev)
+    frames = [FR.upload(v.camera.record, glb, lights, v.gbuffer, dev) for v in views]
+    outs = [torch.zeros((f.height, f.width, 4), dtype=torch.float32, device=dev) for f in frames]
+    vs = [N.view_struct(f.camera, f.gbuffer, N.target_struct(o)) for f, o in zip(frames, outs)]
+    t0 = time.time()
+    cache = Path(tempfile.gettempdir()) / "helio_gb300_batch_tune.txt"
+    plan = ctx.batch_plan(vs, d_lights, len(lights), d_glb, autotune=True, cache_path=str(cache), stream=sh)
+    tune_s = time.time() - t0
+    t_b = _median_ms(lambda: plan.execute(sh), stream, flush, 20)
+    ctx.sync_status(sh)
+    per = []
+    big = max(plan.view_grid(i)[0] * plan.view_grid(i)[1] * plan.view_grid(i)[2] for i in range(len(frames)))
+    sizing = torch.zeros(big * len(lights), dtype=torch.int32, device=dev)
+    for i, f in enumerate(frames):
+        g = plan.view_grid(i)
+        p = N.froxel_params(*g, f.width, f.height, views[i].camera.far)
+        Fv = g[0] * g[1] * g[2]
+        o = torch.zeros(Fv + 1, dtype=torch.int32, device=dev)
+        ctx.bin_froxels(f.camera, d_lights, len(lights), p, o, sizing, sizing.numel(), sh)
+        c = max(1024, 2 * int(o[-1].item()))
+        ix = torch.zeros(c, dtype=torch.int32, device=dev)
+        per.append((f, p, o, ix, c, N.target_struct(outs[i])))
+    del sizing
+
+    def per_view():
+        for f, p, o, ix, c, t in per:
+            ctx.bin_froxels(f.camera, d_lights, len(lights), p, o, ix, c, sh)
+            ctx.shade(f.camera, d_glb, f.gbuffer, d_lights, len(lights), N.froxel_grid_struct(ix, o, p, c), t, sh)
+
+    t_v = _median_ms(per_view, stream, flush, 10)
+    ctx.sync_status(sh)
+    px = sum(f.width * f.height for f in frames)
+    forms["batched"] = {
+        "workload": "w3: 16 probes x 6 cube faces (128^2/256^2/512^2) + 1920x1080 + 1280x720, FP16 G-buffers, "
+                    "2048 lights",
+        "views": len(frames), "pixels": px, "batched_ms": round(t_b, 4), "per_view_launches_ms": round(t_v, 4),
+        "speedup": round(t_v / t_b, 2), "batched_mpix_s": round(px / (t_b / 1e3) / 1e6, 1),
+        "launches": {"batched": 5, "per_view": 5 * len(frames)}, "autotune_s": round(tune_s, 2),
+        "grids": sorted({(f.width, f.height) + plan.view_grid(i) for i, f in enumerate(frames)}),
+    }
+    plan.close()
+    return forms
 
 
 def main():
@@ -379,6 +499,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-forms", action="store_true", help="skip the adjoint / batched-views forms")
     args = ap.parse_args()
     if args.impl == "reference":
         # CPU arm: rank 0 alone runs; other ranks exit without work.

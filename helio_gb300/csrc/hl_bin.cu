@@ -60,12 +60,9 @@ __device__ __forceinline__ bool sphere_in_planes(const Planes& p, float cx, floa
     return true;
 }
 
-__global__ void __launch_bounds__(256) prep_bin_lights_kernel(const GpuCamera* __restrict__ cam,
-                                                              const GpuLight* __restrict__ lights, uint32_t n,
-                                                              uint32_t froxel_margin, BinLight* __restrict__ out) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const GpuLight& l = lights[i];
+// One light in the camera's view space, with its culling radius (widened for froxels).
+__device__ __forceinline__ BinLight prep_light(const GpuCamera* __restrict__ cam, const GpuLight& l,
+                                               uint32_t froxel_margin) {
     const float* v = cam->view;
     const float px = l.position_range[0], py = l.position_range[1], pz = l.position_range[2];
     BinLight b;
@@ -85,7 +82,15 @@ __global__ void __launch_bounds__(256) prep_bin_lights_kernel(const GpuCamera* _
     b.type = l.light_type;
     b.cone = (l.light_type == 2u) && (0.0f < b.cos_o) && (b.cos_o < l.inner_angle);
     b.pad = 0;
-    out[i] = b;
+    return b;
+}
+
+__global__ void __launch_bounds__(256) prep_bin_lights_kernel(const GpuCamera* __restrict__ cam,
+                                                              const GpuLight* __restrict__ lights, uint32_t n,
+                                                              uint32_t froxel_margin, BinLight* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = prep_light(cam, lights[i], froxel_margin);
 }
 
 // ----------------------------------------------------------------------------------
@@ -231,22 +236,26 @@ __device__ __forceinline__ bool light_meets_froxel(const BinLight& l, const Box&
     return true;
 }
 
+struct BinSmem {
+    uint32_t col[kColCap];
+    uint32_t warp_tot[kBinWarps];
+    uint32_t slice_run[kMaxSlices];
+};
+
+// One froxel column (col_id) of one view: count (FILL = false) or fill its slices.
 template <bool FILL>
-__global__ void __launch_bounds__(kBinThreads) bin_froxels_kernel(const GpuCamera* __restrict__ cam,
-                                                                   const BinLight* __restrict__ bl, uint32_t n,
-                                                                   hl_froxel_params p, const __grid_constant__ SliceTable tab,
-                                                                   uint32_t* __restrict__ counts,
-                                                                   const uint32_t* __restrict__ offsets,
-                                                                   uint32_t* __restrict__ indices, uint32_t capacity,
-                                                                   int* __restrict__ status) {
-    __shared__ uint32_t s_col[kColCap];
-    __shared__ uint32_t s_warp_tot[kBinWarps];
-    __shared__ uint32_t s_slice_run[kMaxSlices];
+__device__ __forceinline__ void bin_column(BinSmem& sm, const GpuCamera* __restrict__ cam,
+                                           const BinLight* __restrict__ bl, uint32_t n, const hl_froxel_params& p,
+                                           const float* __restrict__ tabz, uint32_t col_id,
+                                           uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets,
+                                           uint32_t* __restrict__ indices, uint32_t capacity, int* __restrict__ status) {
+    uint32_t* s_col = sm.col;
+    uint32_t* s_warp_tot = sm.warp_tot;
+    uint32_t* s_slice_run = sm.slice_run;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t col_id = blockIdx.x;
     const uint32_t fx = col_id % p.grid_x, fy = col_id / p.grid_x;
     const ColumnGeom g = column_geom(cam, p, fx, fy);
-    const float zlast = xmax(tab.z[p.grid_z], cam->forward_far[3]);
+    const float zlast = xmax(tabz[p.grid_z], cam->forward_far[3]);
     for (uint32_t s = threadIdx.x; s < p.grid_z; s += blockDim.x) s_slice_run[s] = 0;
 
     uint32_t col_len = 0;
@@ -279,8 +288,8 @@ __global__ void __launch_bounds__(kBinThreads) bin_froxels_kernel(const GpuCamer
         }
         // ---- one warp per slice: test the column list against the slice box ----
         for (uint32_t s = warp; s < p.grid_z; s += kBinWarps) {
-            const float z0 = tab.z[s];
-            const float z1 = (s + 1 == p.grid_z) ? zlast : tab.z[s + 1];
+            const float z0 = tabz[s];
+            const float z1 = (s + 1 == p.grid_z) ? zlast : tabz[s + 1];
             const Box b = froxel_box(g, z0, z1);
             const uint32_t f = col_id * p.grid_z + s;
             uint32_t run = s_slice_run[s];
@@ -313,10 +322,21 @@ __global__ void __launch_bounds__(kBinThreads) bin_froxels_kernel(const GpuCamer
     }
 }
 
+template <bool FILL>
+__global__ void __launch_bounds__(kBinThreads) bin_froxels_kernel(const GpuCamera* __restrict__ cam,
+                                                                   const BinLight* __restrict__ bl, uint32_t n,
+                                                                   hl_froxel_params p, const __grid_constant__ SliceTable tab,
+                                                                   uint32_t* __restrict__ counts,
+                                                                   const uint32_t* __restrict__ offsets,
+                                                                   uint32_t* __restrict__ indices, uint32_t capacity,
+                                                                   int* __restrict__ status) {
+    __shared__ BinSmem sm;
+    bin_column<FILL>(sm, cam, bl, n, p, tab.z, blockIdx.x, counts, offsets, indices, capacity, status);
+}
+
 // Exclusive scan of counts[F] into offsets[F+1] by one CTA of 1024 threads.
-__global__ void __launch_bounds__(1024) scan_counts_kernel(const uint32_t* __restrict__ counts, uint32_t F,
-                                                           uint32_t* __restrict__ offsets) {
-    __shared__ uint32_t s_warp[32];
+__device__ __forceinline__ void scan_counts(const uint32_t* __restrict__ counts, uint32_t F,
+                                            uint32_t* __restrict__ offsets, uint32_t* s_warp) {
     const uint32_t t = threadIdx.x;
     const uint32_t per = (F + 1023) / 1024;
     const uint32_t b = min(F, t * per), e = min(F, b + per);
@@ -348,6 +368,49 @@ __global__ void __launch_bounds__(1024) scan_counts_kernel(const uint32_t* __res
         run += counts[i];
     }
     if (t == 1023) offsets[F] = run;
+}
+
+__global__ void __launch_bounds__(1024) scan_counts_kernel(const uint32_t* __restrict__ counts, uint32_t F,
+                                                           uint32_t* __restrict__ offsets) {
+    __shared__ uint32_t s_warp[32];
+    scan_counts(counts, F, offsets, s_warp);
+}
+
+// ---- batched views: the same passes over every view of a batch in one launch each ----
+
+__device__ __forceinline__ uint32_t find_view(const BinViewDesc* __restrict__ d, uint32_t n_views, uint32_t col) {
+    uint32_t lo = 0, hi = n_views;  // largest v with d[v].col_start <= col
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (__ldg(&d[mid].col_start) <= col) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) prep_bin_lights_batched_kernel(const BinViewDesc* __restrict__ d,
+                                                                      const GpuLight* __restrict__ lights, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const BinViewDesc& v = d[blockIdx.y];
+    v.bl[i] = prep_light(static_cast<const GpuCamera*>(v.camera), lights[i], 1u);
+}
+
+template <bool FILL>
+__global__ void __launch_bounds__(kBinThreads) bin_froxels_batched_kernel(const BinViewDesc* __restrict__ d,
+                                                                           uint32_t n_views, uint32_t n,
+                                                                           int* __restrict__ status) {
+    __shared__ BinSmem sm;
+    const uint32_t v = find_view(d, n_views, blockIdx.x);
+    const BinViewDesc& vd = d[v];
+    const hl_froxel_params p = vd.p;
+    bin_column<FILL>(sm, static_cast<const GpuCamera*>(vd.camera), vd.bl, n, p, vd.tab.z, blockIdx.x - vd.col_start,
+                     vd.counts, vd.offsets, vd.indices, vd.capacity, status);
+}
+
+__global__ void __launch_bounds__(1024) scan_counts_batched_kernel(const BinViewDesc* __restrict__ d) {
+    __shared__ uint32_t s_warp[32];
+    const BinViewDesc& v = d[blockIdx.x];
+    scan_counts(v.counts, v.p.grid_x * v.p.grid_y * v.p.grid_z, v.offsets, s_warp);
 }
 
 }  // namespace
@@ -389,6 +452,24 @@ cudaError_t launch_bin_froxels(const void* camera, const BinLight* bl, uint32_t 
     if (e != cudaSuccess) return e;
     bin_froxels_kernel<true><<<cols, kBinThreads, 0, stream>>>(cam, bl, n, p, tab, nullptr, offsets, indices, capacity,
                                                                status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bin_froxels_batched(const BinViewDesc* descs, uint32_t n_views, uint32_t total_columns,
+                                       const void* lights, uint32_t n, int* status, cudaStream_t stream) {
+    if (n > 0) {
+        prep_bin_lights_batched_kernel<<<dim3((n + 255) / 256, n_views), 256, 0, stream>>>(
+            descs, static_cast<const GpuLight*>(lights), n);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    bin_froxels_batched_kernel<false><<<total_columns, kBinThreads, 0, stream>>>(descs, n_views, n, status);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    scan_counts_batched_kernel<<<n_views, 1024, 0, stream>>>(descs);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    bin_froxels_batched_kernel<true><<<total_columns, kBinThreads, 0, stream>>>(descs, n_views, n, status);
     return cudaGetLastError();
 }
 

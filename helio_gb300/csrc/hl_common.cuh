@@ -144,4 +144,17 @@ struct SliceTable {
 };
 constexpr uint32_t kMaxSlices = 128;
 
+// One view of a batch, as the batched froxel binning kernels read it.
+struct BinViewDesc {
+    const void* camera;         // GpuCameraUniforms
+    BinLight* bl;               // n_lights records in this view's space
+    uint32_t* counts;           // F per-froxel counts
+    uint32_t* offsets;          // F + 1
+    uint32_t* indices;          // capacity entries
+    hl_froxel_params p;
+    uint32_t capacity;
+    uint32_t col_start;         // first column of this view in the batch's column range
+    SliceTable tab;
+};
+
 }  // namespace hl

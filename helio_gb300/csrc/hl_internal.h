@@ -11,6 +11,7 @@ namespace hl {
 
 struct BinLight;
 struct SliceTable;
+struct BinViewDesc;
 
 // Device view of a G-buffer (validated by the API layer).
 struct GBufView {
@@ -40,12 +41,40 @@ cudaError_t launch_bin_froxels(const void* camera, const BinLight* bl, uint32_t 
                                const SliceTable& tab, uint32_t* counts_scratch, uint32_t* offsets,
                                uint32_t* indices, uint32_t capacity, int* status, cudaStream_t stream);
 
+// One view of a batch, as the batched shading kernel reads it (froxel grid).
+struct ShadeViewDesc {
+    const void* camera;
+    GBufView gb;
+    GridView grid;
+    TargetView out;
+    const float* tabz;     // the view's slice boundaries (device memory)
+    uint32_t tiles_x;      // 32x16 tiles per row
+    uint32_t tile_start;   // first CTA of this view in the batched launch
+};
+
+// Froxel binning of every view of a batch (descs: device array of n_views).
+cudaError_t launch_bin_froxels_batched(const BinViewDesc* descs, uint32_t n_views, uint32_t total_columns,
+                                       const void* lights, uint32_t n, int* status, cudaStream_t stream);
+
 // Shading. layout: HL_GBUF_*, grid_kind: HL_GRID_*, target_format: HL_TARGET_*.
 // stats != nullptr selects the pair-statistics variant (no radiance written).
 cudaError_t launch_shade(uint32_t layout, uint32_t grid_kind, uint32_t target_format, const void* camera,
                          const void* globals, const GBufView& gb, const void* lights, uint32_t n_lights,
                          const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats,
                          int* status, cudaStream_t stream);
+
+// Adjoint of shading. partials: grid_size * n_lights * 8 floats of scratch.
+uint32_t adjoint_grid_size(int device, uint32_t width, uint32_t height);
+cudaError_t launch_shade_adjoint(uint32_t layout, uint32_t grid_kind, const void* camera, const void* globals,
+                                 const GBufView& gb, const void* lights, uint32_t n_lights, const GridView& grid,
+                                 const SliceTable& tab, const void* d_radiance, uint64_t d_radiance_pitch,
+                                 float* partials, uint32_t grid_size, double* d_lights, float* d_pixels, int* status,
+                                 cudaStream_t stream);
+
+// Shading of every view of a batch in one launch (total_tiles CTAs).
+cudaError_t launch_shade_batched(uint32_t layout, uint32_t target_format, const ShadeViewDesc* descs,
+                                 uint32_t n_views, uint32_t total_tiles, const void* globals, const void* lights,
+                                 uint32_t n_lights, int* status, cudaStream_t stream);
 
 cudaError_t run_fp32_probe(int device, double* tflops);
 

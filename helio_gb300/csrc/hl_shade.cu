@@ -18,85 +18,15 @@
 #include "hl_common.cuh"
 #include "hl_internal.h"
 #include "hl_shade_math.cuh"
+#include "hl_texel.cuh"
 
 namespace hl {
 
 namespace {
 
 using namespace sm;
-
-__device__ __forceinline__ float h2f(uint16_t h) { return __half2float(__ushort_as_half(h)); }
-
-template <uint32_t LAYOUT>
-struct Texel {
-    float depth;
-    float ar, ag, ab, alpha;
-    float nx, ny, nz;
-    float ao, rough, metal;
-    float f0r, f0g, f0b;
-    float er, eg, eb;
-};
-
-template <uint32_t LAYOUT>
-__device__ __forceinline__ Texel<LAYOUT> load_texel(const GBufView& g, uint32_t x, uint32_t y) {
-    Texel<LAYOUT> t;
-    if (LAYOUT == HL_GBUF_REFERENCE) {
-        const uchar4 a = *reinterpret_cast<const uchar4*>(g.plane[0] + g.pitch[0] * y + 4ull * x);
-        const uint2 nr = *reinterpret_cast<const uint2*>(g.plane[1] + g.pitch[1] * y + 8ull * x);
-        const uchar4 o = *reinterpret_cast<const uchar4*>(g.plane[2] + g.pitch[2] * y + 4ull * x);
-        const uint2 e = *reinterpret_cast<const uint2*>(g.plane[3] + g.pitch[3] * y + 8ull * x);
-        t.depth = *reinterpret_cast<const float*>(g.plane[4] + g.pitch[4] * y + 4ull * x);
-        t.ar = div_(float(a.x), 255.0f);
-        t.ag = div_(float(a.y), 255.0f);
-        t.ab = div_(float(a.z), 255.0f);
-        t.alpha = div_(float(a.w), 255.0f);
-        t.nx = h2f(uint16_t(nr.x & 0xffffu));
-        t.ny = h2f(uint16_t(nr.x >> 16));
-        t.nz = h2f(uint16_t(nr.y & 0xffffu));
-        t.f0r = h2f(uint16_t(nr.y >> 16));
-        t.ao = div_(float(o.x), 255.0f);
-        t.rough = div_(float(o.y), 255.0f);
-        t.metal = div_(float(o.z), 255.0f);
-        t.f0g = div_(float(o.w), 255.0f);
-        t.er = h2f(uint16_t(e.x & 0xffffu));
-        t.eg = h2f(uint16_t(e.x >> 16));
-        t.eb = h2f(uint16_t(e.y & 0xffffu));
-        t.f0b = h2f(uint16_t(e.y >> 16));
-    } else if (LAYOUT == HL_GBUF_F32) {
-        const float4 a = *reinterpret_cast<const float4*>(g.plane[0] + g.pitch[0] * y + 16ull * x);
-        const float4 n = *reinterpret_cast<const float4*>(g.plane[1] + g.pitch[1] * y + 16ull * x);
-        t.depth = *reinterpret_cast<const float*>(g.plane[2] + g.pitch[2] * y + 4ull * x);
-        t.ar = a.x;
-        t.ag = a.y;
-        t.ab = a.z;
-        t.rough = a.w;
-        t.nx = n.x;
-        t.ny = n.y;
-        t.nz = n.z;
-        t.metal = n.w;
-    } else {
-        const uint2 a = *reinterpret_cast<const uint2*>(g.plane[0] + g.pitch[0] * y + 8ull * x);
-        const uint32_t on = *reinterpret_cast<const uint32_t*>(g.plane[1] + g.pitch[1] * y + 4ull * x);
-        const uint16_t m = *reinterpret_cast<const uint16_t*>(g.plane[2] + g.pitch[2] * y + 2ull * x);
-        t.depth = *reinterpret_cast<const float*>(g.plane[3] + g.pitch[3] * y + 4ull * x);
-        t.ar = h2f(uint16_t(a.x & 0xffffu));
-        t.ag = h2f(uint16_t(a.x >> 16));
-        t.ab = h2f(uint16_t(a.y & 0xffffu));
-        t.rough = h2f(uint16_t(a.y >> 16));
-        oct_decode(h2f(uint16_t(on & 0xffffu)), h2f(uint16_t(on >> 16)), t.nx, t.ny, t.nz);
-        t.metal = h2f(m);
-    }
-    if (LAYOUT != HL_GBUF_REFERENCE) {
-        t.alpha = 1.0f;
-        t.ao = 1.0f;
-        t.er = t.eg = t.eb = 0.0f;
-        t.f0r = metallic_f0(t.ar, t.metal);
-        t.f0g = metallic_f0(t.ag, t.metal);
-        t.f0b = metallic_f0(t.ab, t.metal);
-    }
-    return t;
-}
-
+using gbuf::Texel;
+using gbuf::load_texel;
 
 namespace sk {
 
@@ -252,11 +182,12 @@ __device__ __noinline__ void flush_batch(sk::Smem<NPX>& s, const uint32_t* queue
 }
 
 // TW x TH = 512 (froxel grid) or 256 (tile grid) pixels, 256 threads.
+// One tile (bx, by) of one view; tabz: the view's slice boundaries (froxel grid).
 template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, int TW, int TH>
-__global__ void __launch_bounds__(sk::kThreads, 2) shade_kernel(
-    const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const GBufView gb,
-    const GpuLight* __restrict__ lights, uint32_t n_lights, const GridView grid, const __grid_constant__ SliceTable tab,
-    const TargetView out, uint32_t* __restrict__ stats, int* __restrict__ status) {
+__device__ __forceinline__ void shade_tile(
+    const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const GBufView& gb,
+    const GpuLight* __restrict__ lights, uint32_t n_lights, const GridView& grid, const float* __restrict__ tabz,
+    const TargetView& out, uint32_t* __restrict__ stats, int* __restrict__ status, uint32_t bx, uint32_t by) {
     using namespace sk;
     constexpr bool FROXELS = (GRID == HL_GRID_FROXELS);
     constexpr int NPX = TW * TH;
@@ -268,13 +199,13 @@ __global__ void __launch_bounds__(sk::kThreads, 2) shade_kernel(
     Smem<NPX>& s = *reinterpret_cast<Smem<NPX>*>(smem_raw);
     uint32_t (*cnt)[NPX] = reinterpret_cast<uint32_t (*)[NPX]>(s.acc);  // statistics view
     const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const uint32_t x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
+    const uint32_t x0 = bx * TW, y0 = by * TH;
     const float W = float(gb.width), H = float(gb.height);
     const float camx = cam->position_near[0], camy = cam->position_near[1], camz = cam->position_near[2];
 
     for (uint32_t b = t; b < uint32_t(kBins); b += kThreads) s.hist[b] = 0;
     if (FROXELS)
-        for (uint32_t k = t; k <= grid.fp.grid_z; k += kThreads) s.tab[k] = tab.z[k];
+        for (uint32_t k = t; k <= grid.fp.grid_z; k += kThreads) s.tab[k] = tabz[k];
 #pragma unroll
     for (int k = 0; k < PPT; ++k)
         for (int c = 0; c < 6; ++c) s.acc[c][t + k * kThreads] = 0.0f;
@@ -291,7 +222,7 @@ __global__ void __launch_bounds__(sk::kThreads, 2) shade_kernel(
         ncols = ncx * ((ye * fp.grid_y) / fp.height - fy0 + 1);
         key_by_column = ncols * fp.grid_z <= uint32_t(kBins);
     } else {
-        const uint32_t tile = blockIdx.y * glb->num_tiles_x + blockIdx.x;
+        const uint32_t tile = by * glb->num_tiles_x + bx;
         if (tile < grid.tiles) {
             tile_len = __ldg(grid.counts + tile);
             if (tile_len > kMaxPerTile) {
@@ -544,6 +475,48 @@ __global__ void __launch_bounds__(sk::kThreads, 2) shade_kernel(
     }
 }
 
+template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, int TW, int TH>
+__global__ void __launch_bounds__(sk::kThreads, 2) shade_kernel(
+    const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const GBufView gb,
+    const GpuLight* __restrict__ lights, uint32_t n_lights, const GridView grid, const __grid_constant__ SliceTable tab,
+    const TargetView out, uint32_t* __restrict__ stats, int* __restrict__ status) {
+    shade_tile<LAYOUT, GRID, TARGET, STATS, TW, TH>(cam, glb, gb, lights, n_lights, grid, tab.z, out, stats, status,
+                                                    blockIdx.x, blockIdx.y);
+}
+
+// Every tile of every view of a batch (froxel grids, 32x16 tiles): CTA b lights tile
+// b - tile_start of the view whose [tile_start, next tile_start) holds b.
+template <uint32_t LAYOUT, uint32_t TARGET>
+__global__ void __launch_bounds__(sk::kThreads, 2) shade_batched_kernel(
+    const ShadeViewDesc* __restrict__ d, uint32_t n_views, const DeferredGlobals* __restrict__ glb,
+    const GpuLight* __restrict__ lights, uint32_t n_lights, int* __restrict__ status) {
+    uint32_t lo = 0, hi = n_views;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (__ldg(&d[mid].tile_start) <= blockIdx.x) lo = mid; else hi = mid;
+    }
+    const ShadeViewDesc& v = d[lo];
+    const uint32_t local = blockIdx.x - v.tile_start;
+    const GBufView gb = v.gb;
+    const GridView grid = v.grid;
+    const TargetView out = v.out;
+    shade_tile<LAYOUT, HL_GRID_FROXELS, TARGET, false, 32, 16>(static_cast<const GpuCamera*>(v.camera), glb, gb, lights,
+                                                               n_lights, grid, v.tabz, out, nullptr, status,
+                                                               local % v.tiles_x, local / v.tiles_x);
+}
+
+template <uint32_t LAYOUT, uint32_t TARGET>
+cudaError_t launch_batched(const ShadeViewDesc* descs, uint32_t n_views, uint32_t total_tiles, const void* globals,
+                           const void* lights, uint32_t n, int* status, cudaStream_t stream) {
+    auto kern = shade_batched_kernel<LAYOUT, TARGET>;
+    const int smem = int(sizeof(sk::Smem<32 * 16>));
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    kern<<<total_tiles, sk::kThreads, smem, stream>>>(descs, n_views, static_cast<const DeferredGlobals*>(globals),
+                                                      static_cast<const GpuLight*>(lights), n, status);
+    return cudaGetLastError();
+}
+
 template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS>
 cudaError_t launch_one(const void* camera, const void* globals, const GBufView& gb, const void* lights, uint32_t n,
                        const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats, int* status,
@@ -609,6 +582,29 @@ cudaError_t launch_shade(uint32_t layout, uint32_t grid_kind, uint32_t target_fo
         default:
             return dispatch_grid<HL_GBUF_F16>(grid_kind, target_format, camera, globals, gb, lights, n_lights, grid,
                                               tab, out, stats, status, stream);
+    }
+}
+
+cudaError_t launch_shade_batched(uint32_t layout, uint32_t target_format, const ShadeViewDesc* descs,
+                                 uint32_t n_views, uint32_t total_tiles, const void* globals, const void* lights,
+                                 uint32_t n_lights, int* status, cudaStream_t stream) {
+    const bool h = target_format == HL_TARGET_RGBA16F;
+    switch (layout) {
+        case HL_GBUF_REFERENCE:
+            return h ? launch_batched<HL_GBUF_REFERENCE, HL_TARGET_RGBA16F>(descs, n_views, total_tiles, globals, lights,
+                                                                           n_lights, status, stream)
+                     : launch_batched<HL_GBUF_REFERENCE, HL_TARGET_RGBA32F>(descs, n_views, total_tiles, globals, lights,
+                                                                           n_lights, status, stream);
+        case HL_GBUF_F32:
+            return h ? launch_batched<HL_GBUF_F32, HL_TARGET_RGBA16F>(descs, n_views, total_tiles, globals, lights,
+                                                                     n_lights, status, stream)
+                     : launch_batched<HL_GBUF_F32, HL_TARGET_RGBA32F>(descs, n_views, total_tiles, globals, lights,
+                                                                     n_lights, status, stream);
+        default:
+            return h ? launch_batched<HL_GBUF_F16, HL_TARGET_RGBA16F>(descs, n_views, total_tiles, globals, lights,
+                                                                     n_lights, status, stream)
+                     : launch_batched<HL_GBUF_F16, HL_TARGET_RGBA32F>(descs, n_views, total_tiles, globals, lights,
+                                                                     n_lights, status, stream);
     }
 }
 

@@ -463,6 +463,174 @@ HL_HD int eval(const Pixel& p, const PixelBrdf& b, const ShadeLight& l, float& o
     return kLit;
 }
 
+// Adjoint of one (pixel, light) pair of pbr_direct_light. Given w = dLoss/d(out.rgb),
+// adds dLoss/d(light position xyz, intensity, colour rgb) to gl[0..6] and
+// dLoss/d(pixel albedo rgb, roughness, metallic) to gp[0..4], with the pair's branch
+// decisions (range, NdL == 0, radiance < 0.002, clamps) held fixed. f0_from_albedo:
+// F0 = clamp(mix(0.04, albedo, metallic)) (FP32/FP16 layouts) so albedo and metallic
+// reach F0; the reference layout stores F0. BRDF terms are recomputed here, nothing
+// per pair is stored by the forward pass. Returns false when a cut applies.
+template <bool PRECISE>
+HL_HD bool eval_adjoint(const Pixel& p, const PixelBrdf& b, const ShadeLight& l, float wr, float wg, float wb,
+                        bool f0_from_albedo, float* gl, float* gp) {
+    // ---- forward, keeping the intermediates ----
+    float Lx, Ly, Lz, tx = 0, ty = 0, tz = 0, dist = 0, inv_d = 0, a0 = 0, fall = 1, nd = 0, spot = 1, dspot = 0;
+    float NdL, atten;
+    if (l.type == 0u) {
+        const float il = rsqrt_(fma_(l.dz, l.dz, fma_(l.dy, l.dy, l.dx * l.dx)));
+        Lx = -l.dx * il;
+        Ly = -l.dy * il;
+        Lz = -l.dz * il;
+        atten = 1.0f;
+        NdL = fma_(p.Nz, Lz, fma_(p.Ny, Ly, p.Nx * Lx));
+    } else {
+        float d2;
+        if (PRECISE) {
+            const DF ux = two_sum(l.px, -p.Px), uy = two_sum(l.py, -p.Py), uz = two_sum(l.pz, -p.Pz);
+            const DF sx = two_sum(ux.hi, ux.lo - p.Plx), sy = two_sum(uy.hi, uy.lo - p.Ply),
+                     sz = two_sum(uz.hi, uz.lo - p.Plz);
+            tx = sx.hi;
+            ty = sy.hi;
+            tz = sz.hi;
+        } else {
+            tx = (l.px - p.Px) - p.Plx;
+            ty = (l.py - p.Py) - p.Ply;
+            tz = (l.pz - p.Pz) - p.Plz;
+        }
+        d2 = fma_(tz, tz, fma_(ty, ty, tx * tx));
+        const float r2 = l.range * l.range;
+        if (d2 > r2) return false;
+        inv_d = rsqrt_(d2);
+        dist = d2 * inv_d;
+        Lx = tx * inv_d;
+        Ly = ty * inv_d;
+        Lz = tz * inv_d;
+        NdL = fma_(p.Nz, Lz, fma_(p.Ny, Ly, p.Nx * Lx));
+        a0 = rcpn_(d2 + 0.0001f);
+        nd = dist * rcpn_(l.range);
+        const float nd2 = nd * nd;
+        fall = fmax_(0.0f, fma_(-nd2, nd2, 1.0f));
+        if (l.type == 2u) {
+            const float cos_a = -fma_(Lz, l.dz, fma_(Ly, l.dy, Lx * l.dx));
+            const float span = l.cos_inner - l.cos_outer;
+            const float tt = div_(cos_a - l.cos_outer, span);
+            if (tt <= 0.0f) {
+                spot = 0.0f;
+            } else if (tt >= 1.0f) {
+                spot = 1.0f;
+            } else {
+                spot = tt * tt * fma_(-2.0f, tt, 3.0f);
+                dspot = div_(6.0f * tt * (1.0f - tt), span);
+            }
+        }
+        atten = a0 * fall * spot;
+    }
+    const float ia = l.intensity * atten;
+    const float rr = l.cr * ia, rg = l.cg * ia, rb = l.cb * ia;
+    if (!(NdL > 0.0f)) return false;
+    if (rr < kRadianceCut && rg < kRadianceCut && rb < kRadianceCut) return false;
+    const float hx = p.Vx + Lx, hy = p.Vy + Ly, hz = p.Vz + Lz;
+    const float ih = rsqrt_(fma_(hz, hz, fma_(hy, hy, hx * hx)));
+    const float Hx = hx * ih, Hy = hy * ih, Hz = hz * ih;
+    const float hdv = fma_(Hz, p.Vz, fma_(Hy, p.Vy, Hx * p.Vx));
+    const float x = clamp01(1.0f - fmax_(hdv, 0.0f));
+    const bool x_free = (hdv > 0.0f) && (x > 0.0f) && (x < 1.0f);
+    const float x2 = x * x;
+    const float p5 = x2 * x2 * x;
+    const float F[3] = {fma_(1.0f - p.f0r, p5, p.f0r), fma_(1.0f - p.f0g, p5, p.f0g), fma_(1.0f - p.f0b, p5, p.f0b)};
+    const float F0[3] = {p.f0r, p.f0g, p.f0b};
+    const float ndh = fma_(p.Nz, Hz, fma_(p.Ny, Hy, p.Nx * Hx));
+    float den = 1.0f;
+    if (ndh > 0.0f) {
+        const float cx = fma_(p.Ny, Hz, -p.Nz * Hy), cy = fma_(p.Nz, Hx, -p.Nx * Hz), cz = fma_(p.Nx, Hy, -p.Ny * Hx);
+        den = fma_(b.a2 * ndh, ndh, fma_(cz, cz, fma_(cy, cy, cx * cx)));
+    }
+    const float Q = fma_(kPi * den, den, 0.0001f);
+    const float D = divn_(b.a2, Q);
+    const float gld = fma_(NdL, b.omk, b.k + 0.0001f);
+    const float glv = divn_(NdL, gld);
+    const float G = b.gv * glv;
+    const float S = fma_(b.nv4, NdL, 0.0001f);
+    const float spec = divn_(D * G, S);
+    const float alb[3] = {p.dr * kPi, p.dg * kPi, p.db * kPi};
+    const float rad[3] = {rr, rg, rb};
+    const float w[3] = {wr, wg, wb};
+    const float col[3] = {l.cr, l.cg, l.cb};
+    // ---- adjoint ----
+    float dNdL = 0.0f, dspec = 0.0f, dp5 = 0.0f, dmetal = 0.0f, datten = 0.0f;
+    for (int c = 0; c < 3; ++c) {
+        const float kd = (1.0f - F[c]) * b.one_m_metal;
+        const float brdf = fma_(kd, alb[c] * kInvPi, spec * F[c]);
+        const float drad = w[c] * brdf * NdL;
+        dNdL = fma_(w[c] * brdf, rad[c], dNdL);
+        const float dbrdf = w[c] * rad[c] * NdL;
+        gp[c] += dbrdf * kd * kInvPi;
+        const float dkd = dbrdf * alb[c] * kInvPi;
+        const float dF = fma_(dbrdf, spec, -dkd * b.one_m_metal);
+        dmetal -= dkd * (1.0f - F[c]);
+        dspec = fma_(dbrdf, F[c], dspec);
+        dp5 = fma_(dF, 1.0f - F0[c], dp5);
+        if (f0_from_albedo) {
+            const float f0raw = fma_(alb[c], p.metal, 0.04f * (1.0f - p.metal));
+            if (f0raw > 0.0f && f0raw < 0.999f) {
+                const float dF0 = dF * (1.0f - p5);
+                gp[c] = fma_(dF0, p.metal, gp[c]);
+                dmetal = fma_(dF0, alb[c] - 0.04f, dmetal);
+            }
+        }
+        // rad_c = col_c * I * atten
+        gl[4 + c] = fma_(drad, ia, gl[4 + c]);
+        gl[3] = fma_(drad, col[c] * atten, gl[3]);
+        datten = fma_(drad, col[c] * l.intensity, datten);
+    }
+    gp[4] += dmetal;
+    // spec = D G / S
+    const float dD = dspec * G / S, dG = dspec * D / S, dS = -dspec * spec / S;
+    dNdL = fma_(dS, b.nv4, dNdL);
+    const float dglv = dG * b.gv, dgv = dG * glv;
+    dNdL = fma_(dglv, divn_(gld - NdL * b.omk, gld * gld), dNdL);
+    float dk = dglv * divn_(-NdL * (1.0f - NdL), gld * gld);
+    // gv = NdV / (NdV (1-k) + k + 1e-4), NdV of the pixel
+    const float gvd = fma_(p.NdV, b.omk, b.k + 0.0001f);
+    dk = fma_(dgv, divn_(-p.NdV * (1.0f - p.NdV), gvd * gvd), dk);
+    float drough = dk * (p.rough + 1.0f) * 0.25f;
+    // D = a2 / Q, Q = pi den^2 + 1e-4, den = NdH^2 (a2 - 1) + 1
+    float da2 = dD / Q;
+    const float dden = -dD * D / Q * 2.0f * kPi * den;
+    float dndh = 0.0f;
+    if (ndh > 0.0f) {
+        da2 = fma_(dden, ndh * ndh, da2);
+        dndh = dden * 2.0f * ndh * (b.a2 - 1.0f);
+    }
+    drough = fma_(da2, 4.0f * p.rough * p.rough * p.rough, drough);
+    gp[3] += drough;
+    // p5 = x^5, x = clamp(1 - max(H.V, 0))
+    const float dhdv = x_free ? -dp5 * 5.0f * x2 * x2 : 0.0f;
+    // H = normalize(V + L): dhv = (dH - H (dH.H)) / |hv|, dH = V dhdv + N dndh
+    const float dHx = fma_(p.Vx, dhdv, p.Nx * dndh), dHy = fma_(p.Vy, dhdv, p.Ny * dndh),
+                dHz = fma_(p.Vz, dhdv, p.Nz * dndh);
+    const float hdot = fma_(dHz, Hz, fma_(dHy, Hy, dHx * Hx));
+    float dLx = (dHx - Hx * hdot) * ih + p.Nx * dNdL;
+    float dLy = (dHy - Hy * hdot) * ih + p.Ny * dNdL;
+    float dLz = (dHz - Hz * hdot) * ih + p.Nz * dNdL;
+    if (l.type == 0u) return true;  // no dependence on the light position
+    // atten = a0 * fall * spot
+    float ddist = datten * spot * (fall * (-2.0f * dist) * a0 * a0);
+    if (fall > 0.0f) ddist = fma_(datten * spot * a0, -4.0f * nd * nd * nd * rcpn_(l.range), ddist);
+    if (l.type == 2u) {
+        const float dcos = datten * a0 * fall * dspot;  // cos_a = -L.dir
+        dLx = fma_(-l.dx, dcos, dLx);
+        dLy = fma_(-l.dy, dcos, dLy);
+        dLz = fma_(-l.dz, dcos, dLz);
+    }
+    // L = t / |t|: dt = (dL - L (dL.L)) / |t| + L ddist
+    const float ldot = fma_(dLz, Lz, fma_(dLy, Ly, dLx * Lx));
+    gl[0] += fma_(dLx - Lx * ldot, inv_d, Lx * ddist);
+    gl[1] += fma_(dLy - Ly * ldot, inv_d, Ly * ddist);
+    gl[2] += fma_(dLz - Lz * ldot, inv_d, Lz * ddist);
+    return true;
+}
+
 // Kahan (compensated) accumulation of one channel.
 HL_HD void kahan_add(float& sum, float& comp, float v) {
     const float y = add_(v, -comp);

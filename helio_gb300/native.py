@@ -273,6 +273,63 @@ class Context:
                                              n_lights, C.byref(grid), _ptr(d_radiance), int(d_radiance_pitch),
                                              _ptr(d_lights), _ptr(d_pixels), _stream(stream)), "hl_shade_adjoint")
 
+    def batch_plan(self, views, lights, n_lights, globals_, grid=None, autotune=False, cache_path=None,
+                   stream=None) -> "BatchPlan":
+        """Plan lighting every view of ``views`` (a list of ``View``) with one light buffer:
+        ``grid`` = (gx, gy, gz) for every view, or ``autotune`` to time candidate grids per
+        view size (results kept in ``cache_path`` if given)."""
+        arr = (View * len(views))(*views)
+        cfg = BatchConfig()
+        cfg.autotune = 1 if autotune else 0
+        cfg.grid_x, cfg.grid_y, cfg.grid_z = grid if grid is not None else (0, 0, 0)
+        cfg.cache_path = cache_path.encode() if cache_path else None
+        h = C.c_void_p()
+        self._check(self._l.hl_batch_plan_create(self._h, arr, len(views), _ptr(lights), n_lights, _ptr(globals_),
+                                                 C.byref(cfg), C.byref(h), _stream(stream)), "hl_batch_plan_create")
+        return BatchPlan(self, h, len(views))
+
+
+class BatchPlan:
+    """A plan of hl_batch_plan_create; ``execute`` replays its CUDA graph."""
+
+    def __init__(self, ctx: Context, handle, n_views: int):
+        self._ctx, self._h, self.n_views = ctx, handle, n_views
+
+    def execute(self, stream=None):
+        self._ctx._check(self._ctx._l.hl_batch_execute(self._ctx.handle, self._h, _stream(stream)), "hl_batch_execute")
+
+    def view_grid(self, view: int):
+        g = (C.c_uint32 * 3)()
+        st = self._ctx._l.hl_batch_plan_view_grid(self._h, view, g)
+        if st != HL_OK:
+            raise HelioError(st, f"hl_batch_plan_view_grid: {status_string(st)}")
+        return tuple(int(v) for v in g)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._ctx._l.hl_batch_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def view_struct(camera, gbuffer: GBuffer, target: Target) -> View:
+    v = View()
+    v.camera = _ptr(camera)
+    v.gbuffer = gbuffer
+    v.radiance = target
+    return v
+
 
 def tile_grid_struct(lists, counts) -> LightGrid:
     g = LightGrid()

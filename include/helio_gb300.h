@@ -248,14 +248,22 @@ hl_status hl_shade_stats(hl_ctx* ctx, const void* camera, const void* globals, c
  * Adjoint of the direct-lighting term (no reference counterpart)
  * -------------------------------------------------------------------------------*/
 
-/* Given dL/d(radiance) for every pixel (RGBA32F, alpha ignored), returns
+#define HL_ADJOINT_MAX_LIGHTS 65536u
+
+/* Given dL/d(radiance) for every pixel (RGBA32F with pitch d_radiance_pitch bytes,
+ * alpha ignored), returns
  *   d_lights[n_lights*7] (f64): d/d position.xyz, d/d intensity, d/d color.rgb
- *   d_pixels[W*H*5]      (f32): d/d albedo.rgb, d/d roughness, d/d metallic
- * for the radiance hl_shade computes on an HL_GBUF_F32 G-buffer with a froxel grid.
- * BRDF terms are recomputed, not stored. Light gradients are reduced per block in
- * f32 and across blocks in f64 in a fixed order, so results are deterministic.
- * The branch decisions (range, NdL == 0, radiance < 0.002) are held fixed. d_lights
- * and d_pixels are overwritten. */
+ *   d_pixels[H][W][5]    (f32, dense): d/d albedo.rgb, d/d roughness, d/d metallic
+ * for the radiance hl_shade computes with the same G-buffer (any layout; the pair terms
+ * are evaluated on the precise path) and light grid (tiles or froxels). The albedo
+ * gradient includes the hemisphere ambient term. BRDF terms are recomputed, not stored.
+ * Light gradients are reduced per block in f32 and across blocks in f64 in a fixed
+ * order, so results are deterministic. The branch decisions (range, NdL == 0,
+ * radiance < 0.002, clamps) are held fixed. d_lights and d_pixels are overwritten;
+ * sky pixels get zeros. Requires debug_mode == 0 and has_rc_gi == 0 in the globals
+ * (else hl_sync_status reports HL_ERR_NOT_SUPPORTED) and n_lights <=
+ * HL_ADJOINT_MAX_LIGHTS. Scratch: (#SMs x resident blocks) x n_lights x 32 bytes,
+ * grown in the context. */
 hl_status hl_shade_adjoint(hl_ctx* ctx, const void* camera, const void* globals,
                            const hl_gbuffer* gbuffer, const void* lights, uint32_t n_lights,
                            const hl_light_grid* grid, const float* d_radiance,
