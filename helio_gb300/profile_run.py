@@ -1,0 +1,79 @@
+"""A few frames of one workload through the C ABI, for profiler captures.
+
+    python -m helio_gb300.profile_run --workload 1 --frames 3            # bin + shade
+    python -m helio_gb300.profile_run --workload 4 --frames 3 --adjoint  # + adjoint
+    python -m helio_gb300.profile_run --batched --frames 3              # 98-view plan
+
+Every frame launches the same kernels as one bench step (froxel binning: 4 launches,
+shading: 1, adjoint: 2), so ``ncu -k <kernel> -s <n> -c 1`` can pick one warm launch.
+Prints one line with the device time of the last frame.
+"""
+from __future__ import annotations
+
+import argparse
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", type=int, default=1, choices=[0, 1, 2, 4])
+    ap.add_argument("--frames", type=int, default=3)
+    ap.add_argument("--adjoint", action="store_true")
+    ap.add_argument("--batched", action="store_true")
+    ap.add_argument("--scale", type=float, default=1.0)
+    args = ap.parse_args(argv)
+
+    import torch
+
+    from . import frame as FR
+    from . import layouts as L
+    from . import native as N
+    from . import synthetic as S
+
+    ctx = N.Context(0)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if args.batched:
+        views, lights = S.batched_views(args.scale)
+        glb = L.make_globals(1, len(lights), ambient_color=(0.4, 0.45, 0.5), ambient_intensity=0.3)
+        d_l, d_g = FR.bytes_tensor(lights), FR.bytes_tensor(glb)
+        frames = [FR.upload(v.camera.record, glb, lights, v.gbuffer) for v in views]
+        outs = [torch.zeros((f.height, f.width, 4), dtype=torch.float32, device="cuda") for f in frames]
+        vs = [N.view_struct(f.camera, f.gbuffer, N.target_struct(o)) for f, o in zip(frames, outs)]
+        plan = ctx.batch_plan(vs, d_l, len(lights), d_g, grid=(8, 8, 24))
+        for _ in range(args.frames):
+            ev0.record()
+            plan.execute()
+            ev1.record()
+        ctx.sync_status()
+        plan.close()
+        print(f"batched: {len(views)} views, {ev0.elapsed_time(ev1) * 1e3:.1f} us per frame", flush=True)
+        return
+    w = S.workload(args.workload, args.scale)
+    W, H = w.gbuffer.width, w.gbuffer.height
+    fp = N.froxel_params_from_numpy(L.froxel_params(*w.froxel_grid, W, H, w.camera.far))
+    F = fp.grid_x * fp.grid_y * fp.grid_z
+    df = FR.upload_workload(w)
+    cap = F * max(1, min(df.n_lights, 256))
+    off = torch.zeros(F + 1, dtype=torch.int32, device="cuda")
+    idx = torch.zeros(cap, dtype=torch.int32, device="cuda")
+    out = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    grid = N.froxel_grid_struct(idx, off, fp, cap)
+    if args.adjoint:
+        g = torch.Generator(device="cuda")
+        g.manual_seed(args.workload)
+        d_rad = torch.randn((H, W, 4), dtype=torch.float32, device="cuda", generator=g)
+        d_l = torch.zeros((max(df.n_lights, 1), 7), dtype=torch.float64, device="cuda")
+        d_p = torch.zeros((H, W, 5), dtype=torch.float32, device="cuda")
+    for _ in range(args.frames):
+        ev0.record()
+        ctx.bin_froxels(df.camera, df.lights, df.n_lights, fp, off, idx, cap)
+        ctx.shade(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, N.target_struct(out))
+        if args.adjoint:
+            ctx.shade_adjoint(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, d_rad, W * 16, d_l,
+                              d_p)
+        ev1.record()
+    ctx.sync_status()
+    print(f"w{args.workload}: {ev0.elapsed_time(ev1) * 1e3:.1f} us per frame", flush=True)
+
+
+if __name__ == "__main__":
+    main()
