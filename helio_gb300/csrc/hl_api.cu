@@ -36,9 +36,12 @@ hl_status shade_common(hl_ctx* ctx, const void* camera, const void* globals, con
     }
     DeviceGuard dg(ctx->device);
     if (!dg.ok) return fail(ctx, HL_ERR_CUDA, "cudaSetDevice(%d) failed", ctx->device);
+    if ((s = ensure(ctx, ctx->shade_cand, ctx->shade_cand_cap, n_lights > 0 ? n_lights : 1, "shade light table")) !=
+        HL_OK)
+        return s;
     cudaError_t e = hl::launch_shade(gbuffer->layout, grid->kind, stats ? HL_TARGET_RGBA32F : radiance->format, camera,
                                      globals, gv, lights, n_lights, grv, tab, tv, stats, ctx->d_status,
-                                     as_stream(stream));
+                                     ctx->shade_cand, as_stream(stream));
     if (e != cudaSuccess) return cuda_fail(ctx, e, "shade launch");
     return HL_OK;
 }
@@ -94,6 +97,7 @@ hl_status hl_destroy(hl_ctx* ctx) {
     cudaFree(ctx->bin_lights);
     cudaFree(ctx->froxel_counts);
     cudaFree(ctx->adjoint_partials);
+    cudaFree(ctx->shade_cand);
     delete ctx;
     return HL_OK;
 }

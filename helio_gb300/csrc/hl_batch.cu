@@ -3,10 +3,11 @@
 //
 // A plan owns, in one set of device buffers, every view's froxel lists and the
 // per-view descriptors the batched kernels read. Executing it replays a CUDA graph of
-// five launches whatever the number of views: light preparation for all views, froxel
-// counts, per-view scans, froxel fills, and one shading launch whose CTAs walk the
-// (view, 32x16 tile) work list. Per-view launches of hl_bin_froxels + hl_shade cost
-// five launches per view instead, most of them too small to fill the GPU.
+// six launches whatever the number of views: light preparation for binning in every
+// view, froxel counts, per-view scans, froxel fills, the shading light tables of every
+// view, and one shading launch whose CTAs walk the (view, 32x16 tile) work list.
+// Per-view launches of hl_bin_froxels + hl_shade cost six launches per view instead,
+// most of them too small to fill the GPU.
 //
 // Froxel grids are chosen per view size: given in the config, or by the autotuner,
 // which builds a one-class plan for each candidate grid of a view size, times its graph
@@ -37,6 +38,7 @@ struct hl_batch_plan {
     hl::BinViewDesc* d_bin = nullptr;
     hl::ShadeViewDesc* d_shade = nullptr;
     hl::BinLight* bl = nullptr;
+    float4* cand = nullptr;
     uint32_t* counts = nullptr;
     uint32_t* offsets = nullptr;
     uint32_t* indices = nullptr;
@@ -64,6 +66,7 @@ void free_plan(hl_batch_plan* p) {
     cudaFree(p->d_bin);
     cudaFree(p->d_shade);
     cudaFree(p->bl);
+    cudaFree(p->cand);
     cudaFree(p->counts);
     cudaFree(p->offsets);
     cudaFree(p->indices);
@@ -134,6 +137,7 @@ hl_status build_plan(hl_ctx* ctx, const std::vector<HostView>& views, const std:
     cudaError_t e = cudaMalloc(&p->d_bin, sizeof(hl::BinViewDesc) * V);
     if (e == cudaSuccess) e = cudaMalloc(&p->d_shade, sizeof(hl::ShadeViewDesc) * V);
     if (e == cudaSuccess) e = cudaMalloc(&p->bl, sizeof(hl::BinLight) * size_t(V) * std::max(n_lights, 1u));
+    if (e == cudaSuccess) e = cudaMalloc(&p->cand, sizeof(float4) * size_t(V) * std::max(n_lights, 1u));
     if (e == cudaSuccess) e = cudaMalloc(&p->counts, sizeof(uint32_t) * std::max<uint64_t>(f_base[V], 1));
     if (e == cudaSuccess) e = cudaMalloc(&p->offsets, sizeof(uint32_t) * o_base[V]);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->capture_stream, cudaStreamNonBlocking);
@@ -189,6 +193,7 @@ hl_status build_plan(hl_ctx* ctx, const std::vector<HostView>& views, const std:
         g.tiles = 0;
         g.fp = bd[v].p;
         sd[v].grid = g;
+        sd[v].cand = p->cand + size_t(v) * n_lights;
         sd[v].tabz = reinterpret_cast<const float*>(reinterpret_cast<const unsigned char*>(p->d_bin + v) +
                                                     offsetof(hl::BinViewDesc, tab));
     }

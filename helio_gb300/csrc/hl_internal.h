@@ -48,6 +48,7 @@ struct ShadeViewDesc {
     GridView grid;
     TargetView out;
     const float* tabz;     // the view's slice boundaries (device memory)
+    float4* cand;          // n_lights entries: the view's candidate-test light table
     uint32_t tiles_x;      // 32x16 tiles per row
     uint32_t tile_start;   // first CTA of this view in the batched launch
 };
@@ -58,10 +59,11 @@ cudaError_t launch_bin_froxels_batched(const BinViewDesc* descs, uint32_t n_view
 
 // Shading. layout: HL_GBUF_*, grid_kind: HL_GRID_*, target_format: HL_TARGET_*.
 // stats != nullptr selects the pair-statistics variant (no radiance written).
+// cand: n_lights float4 of scratch for the candidate-test light table.
 cudaError_t launch_shade(uint32_t layout, uint32_t grid_kind, uint32_t target_format, const void* camera,
                          const void* globals, const GBufView& gb, const void* lights, uint32_t n_lights,
                          const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats,
-                         int* status, cudaStream_t stream);
+                         int* status, float4* cand, cudaStream_t stream);
 
 // Adjoint of shading. partials: grid_size * n_lights * 8 floats of scratch.
 uint32_t adjoint_grid_size(int device, uint32_t width, uint32_t height);

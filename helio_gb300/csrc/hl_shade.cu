@@ -35,6 +35,7 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kQueue = 256;      // per-warp pair ring (up to 31 + kPipe * 32 pending)
 constexpr int kBins = 512;       // froxel keys of the pixel sort
 constexpr int kPipe = 4;         // list entries in flight per lane
+constexpr int kBoxMin = 8;       // shortest shared list worth a box cull
 
 // Pixel record fields (structure of arrays).
 enum Field : int {
@@ -53,6 +54,7 @@ struct Smem {
     uint32_t warp_tot[kWarps];
     float tab[kMaxSlices + 1];      // slice boundaries
     uint32_t n_valid;
+    uint16_t col_of[32], row_of[16];  // froxel column / row of the tile's pixel columns / rows
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -186,14 +188,16 @@ __device__ __noinline__ void flush_batch(sk::Smem<NPX>& s, const uint32_t* queue
 template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, int TW, int TH>
 __device__ __forceinline__ void shade_tile(
     const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const GBufView& gb,
-    const GpuLight* __restrict__ lights, uint32_t n_lights, const GridView& grid, const float* __restrict__ tabz,
-    const TargetView& out, uint32_t* __restrict__ stats, int* __restrict__ status, uint32_t bx, uint32_t by) {
+    const GpuLight* __restrict__ lights, const float4* __restrict__ cand, uint32_t n_lights, const GridView& grid,
+    const float* __restrict__ tabz, const TargetView& out, uint32_t* __restrict__ stats, int* __restrict__ status,
+    uint32_t bx, uint32_t by) {
     using namespace sk;
     constexpr bool FROXELS = (GRID == HL_GRID_FROXELS);
     constexpr int NPX = TW * TH;
     constexpr int PPT = NPX / kThreads;  // pixels per thread in set-up and output
     constexpr int NG = NPX / 32;         // groups of 32 sorted pixels
     static_assert(NPX % kThreads == 0 && (NG == kWarps || NG == 2 * kWarps), "256 or 512 pixels per tile");
+    static_assert(TW <= 32 && TH <= 16 && TW + TH <= kThreads, "column / row tables of the tile");
     constexpr bool PRECISE = (LAYOUT != HL_GBUF_F16);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem<NPX>& s = *reinterpret_cast<Smem<NPX>*>(smem_raw);
@@ -204,8 +208,14 @@ __device__ __forceinline__ void shade_tile(
     const float camx = cam->position_near[0], camy = cam->position_near[1], camz = cam->position_near[2];
 
     for (uint32_t b = t; b < uint32_t(kBins); b += kThreads) s.hist[b] = 0;
-    if (FROXELS)
+    if (FROXELS) {
         for (uint32_t k = t; k <= grid.fp.grid_z; k += kThreads) s.tab[k] = tabz[k];
+        // froxel column of each pixel column and row of the tile (one division each)
+        if (t < uint32_t(TW))
+            s.col_of[t] = uint16_t((uint64_t(x0 + t) * grid.fp.grid_x) / grid.fp.width);
+        else if (t < uint32_t(TW + TH))
+            s.row_of[t - TW] = uint16_t((uint64_t(y0 + t - TW) * grid.fp.grid_y) / grid.fp.height);
+    }
 #pragma unroll
     for (int k = 0; k < PPT; ++k)
         for (int c = 0; c < 6; ++c) s.acc[c][t + k * kThreads] = 0.0f;
@@ -235,6 +245,11 @@ __device__ __forceinline__ void shade_tile(
         }
     }
     __syncthreads();
+
+    // slices are exponential from slice_near to tab[grid_z]: slice ~ log2(d / near) * scale
+    const float slice_inv_near = FROXELS ? rcp_(grid.fp.slice_near) : 0.0f;
+    const float slice_scale =
+        FROXELS ? float(grid.fp.grid_z) * rcp_(__log2f(fmaxf(s.tab[grid.fp.grid_z] * slice_inv_near, 2.0f))) : 0.0f;
 
     // ---- 1. pixel set-up -------------------------------------------------------
     float rel[12], wrow[4];
@@ -287,11 +302,14 @@ __device__ __forceinline__ void shade_tile(
                     const float nr = cam->position_near[3], fr = cam->forward_far[3];
                     const float dv = div_(nr * fr, fma_(-tx.depth, fr - nr, fr));
                     const hl_froxel_params& fp = grid.fp;
-                    uint32_t sl = 0;
-                    for (uint32_t step = 64; step > 0; step >>= 1)
-                        if (sl + step < fp.grid_z && s.tab[sl + step] <= dv) sl += step;
-                    const uint32_t fx = (x * fp.grid_x) / fp.width;
-                    const uint32_t fy = (y * fp.grid_y) / fp.height;
+                    // largest sl < grid_z with tab[sl] <= dv: a guess from the exponential
+                    // slice spacing, then exact steps against the table
+                    const int guess = int(__log2f(dv * slice_inv_near) * slice_scale);
+                    uint32_t sl = uint32_t(min(max(guess, 0), int(fp.grid_z) - 1));
+                    while (sl + 1 < fp.grid_z && s.tab[sl + 1] <= dv) ++sl;
+                    while (sl > 0 && s.tab[sl] > dv) --sl;
+                    const uint32_t fx = s.col_of[x - x0];
+                    const uint32_t fy = s.row_of[y - y0];
                     const uint32_t f = (fy * fp.grid_x + fx) * fp.grid_z + sl;
                     b = __ldg(grid.counts + f);
                     const uint32_t e = __ldg(grid.counts + f + 1);
@@ -365,19 +383,71 @@ __device__ __forceinline__ void shade_tile(
             lb = s.base[i];
             ln = s.len[i];
         }
-        const uint32_t maxlen = __reduce_max_sync(0xffffffffu, ln);
+        // A group whose lanes all hold one list (common where depth is coherent) first
+        // culls that list against the box around its pixels, 32 lights at a time; only
+        // the survivors are tested per pixel. The box test is looser than the per-pixel
+        // test, so the queued pairs, and their order per pixel, are unchanged.
+        const uint32_t lb0 = __shfl_sync(0xffffffffu, lb, 0), ln0 = __shfl_sync(0xffffffffu, ln, 0);
+        const bool shared = ln0 >= uint32_t(kBoxMin) && __all_sync(0xffffffffu, !own || (lb == lb0 && ln == ln0));
+        const uint32_t maxlen = shared ? 0u : __reduce_max_sync(0xffffffffu, ln);
+        if (shared) {
+            float b0x = own ? px : 3.0e38f, b0y = own ? py : 3.0e38f, b0z = own ? pz : 3.0e38f;
+            float b1x = own ? px : -3.0e38f, b1y = own ? py : -3.0e38f, b1z = own ? pz : -3.0e38f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                b0x = fminf(b0x, __shfl_xor_sync(0xffffffffu, b0x, o));
+                b0y = fminf(b0y, __shfl_xor_sync(0xffffffffu, b0y, o));
+                b0z = fminf(b0z, __shfl_xor_sync(0xffffffffu, b0z, o));
+                b1x = fmaxf(b1x, __shfl_xor_sync(0xffffffffu, b1x, o));
+                b1y = fmaxf(b1y, __shfl_xor_sync(0xffffffffu, b1y, o));
+                b1z = fmaxf(b1z, __shfl_xor_sync(0xffffffffu, b1z, o));
+            }
+            // rounding of positions and differences: widen by 2^-18 of the magnitudes
+            const float mag = fmaxf(fmaxf(fmaxf(fabsf(b0x), fabsf(b1x)), fmaxf(fabsf(b0y), fabsf(b1y))),
+                                    fmaxf(fabsf(b0z), fabsf(b1z)));
+#pragma unroll 1
+            for (uint32_t j0 = 0; j0 < ln0; j0 += 32) {
+                const uint32_t j = j0 + lane;
+                const uint32_t lj = j < ln0 ? __ldg(grid.lists + lb0 + j) : 0xffffffffu;
+                const bool ok = lj < n_lights;
+                if (j < ln0 && !ok) raise_status(status, HL_ERR_DEVICE_BOUNDS);
+                const float4 c = ok ? __ldg(cand + lj) : make_float4(0, 0, 0, -1.0f);
+                bool keep = ok && c.w < 0.0f;
+                if (ok && c.w >= 0.0f) {
+                    const float e = (mag + fabsf(c.x) + fabsf(c.y) + fabsf(c.z)) * (1.0f / 262144.0f);
+                    const float dx = fmaxf(fmaxf(b0x - c.x, c.x - b1x) - e, 0.0f);
+                    const float dy = fmaxf(fmaxf(b0y - c.y, c.y - b1y) - e, 0.0f);
+                    const float dz = fmaxf(fmaxf(b0z - c.z, c.z - b1z) - e, 0.0f);
+                    keep = fma_(dz, dz, fma_(dy, dy, dx * dx)) <= c.w * (1.0f + 1.0f / 256.0f);
+                }
+                uint32_t m = __ballot_sync(0xffffffffu, keep);
+                while (m) {
+                    const int bl = __ffs(m) - 1;
+                    m &= m - 1;
+                    const uint32_t li = __shfl_sync(0xffffffffu, lj, bl);
+                    const float ax = __shfl_sync(0xffffffffu, c.x, bl), ay = __shfl_sync(0xffffffffu, c.y, bl),
+                                az = __shfl_sync(0xffffffffu, c.z, bl), aw = __shfl_sync(0xffffffffu, c.w, bl);
+                    const bool pass = own && (aw < 0.0f || candidate(px, py, pz, plx, ply, plz, nx, ny, nz, ax, ay, az,
+                                                                     aw, slack, !STATS));
+                    const uint32_t pm = __ballot_sync(0xffffffffu, pass);
+                    if (pass) queue[(head + qlen + __popc(pm & lanemask_lt())) & (kQueue - 1)] = (i << 23) | li;
+                    qlen += __popc(pm);
+                    __syncwarp();
+                    if (qlen >= 32) {
+                        flush_batch<LAYOUT, STATS, TW, NPX>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H);
+                        head += 32;
+                        qlen -= 32;
+                    }
+                }
+            }
+        }
         for (uint32_t j0 = 0; j0 < maxlen; j0 += kPipe) {
             uint32_t li[kPipe];
             float4 a[kPipe];
-            uint32_t ty[kPipe];
 #pragma unroll
             for (int u = 0; u < kPipe; ++u) li[u] = (j0 + u < ln) ? __ldg(grid.lists + lb + j0 + u) : 0xffffffffu;
 #pragma unroll
-            for (int u = 0; u < kPipe; ++u) {
-                const bool ok = li[u] < n_lights;
-                a[u] = ok ? __ldg(reinterpret_cast<const float4*>(lights + li[u])) : make_float4(0, 0, 0, 0);
-                ty[u] = ok ? __ldg(reinterpret_cast<const uint32_t*>(lights + li[u]) + 13) : 0u;
-            }
+            for (int u = 0; u < kPipe; ++u) a[u] = li[u] < n_lights ? __ldg(cand + li[u]) : make_float4(0, 0, 0, 0);
 #pragma unroll
             for (int u = 0; u < kPipe; ++u) {
                 if (j0 + u >= maxlen) break;  // warp-uniform
@@ -385,13 +455,11 @@ __device__ __forceinline__ void shade_tile(
                 if (j0 + u < ln) {
                     if (li[u] >= n_lights) {
                         raise_status(status, HL_ERR_DEVICE_BOUNDS);
-                    } else if (ty[u] == 0u) {
-                        pass = true;
+                    } else if (a[u].w < 0.0f) {
+                        pass = true;  // directional
                     } else {
-                        const float lx = PRECISE ? a[u].x : a[u].x - camx, ly = PRECISE ? a[u].y : a[u].y - camy,
-                                    lz = PRECISE ? a[u].z : a[u].z - camz;
-                        pass = candidate(px, py, pz, plx, ply, plz, nx, ny, nz, lx, ly, lz,
-                                         a[u].w * a[u].w * (1.0f + 1.0f / 512.0f), slack, !STATS);
+                        pass = candidate(px, py, pz, plx, ply, plz, nx, ny, nz, a[u].x, a[u].y, a[u].z, a[u].w, slack,
+                                         !STATS);
                     }
                 }
                 const uint32_t pm = __ballot_sync(0xffffffffu, pass);
@@ -479,9 +547,9 @@ template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, int TW, i
 __global__ void __launch_bounds__(sk::kThreads, 2) shade_kernel(
     const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const GBufView gb,
     const GpuLight* __restrict__ lights, uint32_t n_lights, const GridView grid, const __grid_constant__ SliceTable tab,
-    const TargetView out, uint32_t* __restrict__ stats, int* __restrict__ status) {
-    shade_tile<LAYOUT, GRID, TARGET, STATS, TW, TH>(cam, glb, gb, lights, n_lights, grid, tab.z, out, stats, status,
-                                                    blockIdx.x, blockIdx.y);
+    const TargetView out, uint32_t* __restrict__ stats, int* __restrict__ status, const float4* __restrict__ cand) {
+    shade_tile<LAYOUT, GRID, TARGET, STATS, TW, TH>(cam, glb, gb, lights, cand, n_lights, grid, tab.z, out, stats,
+                                                    status, blockIdx.x, blockIdx.y);
 }
 
 // Every tile of every view of a batch (froxel grids, 32x16 tiles): CTA b lights tile
@@ -501,8 +569,36 @@ __global__ void __launch_bounds__(sk::kThreads, 2) shade_batched_kernel(
     const GridView grid = v.grid;
     const TargetView out = v.out;
     shade_tile<LAYOUT, HL_GRID_FROXELS, TARGET, false, 32, 16>(static_cast<const GpuCamera*>(v.camera), glb, gb, lights,
-                                                               n_lights, grid, v.tabz, out, nullptr, status,
+                                                               v.cand, n_lights, grid, v.tabz, out, nullptr, status,
                                                                local % v.tiles_x, local / v.tiles_x);
+}
+
+// The light table of the candidate tests: position (camera-relative on the FP16
+// G-buffer's fast path, as the shading kernel computes it), and range^2 (1 + 2^-9), or
+// -1 for a directional light.
+__device__ __forceinline__ float4 cand_entry(const GpuCamera* __restrict__ cam, const GpuLight& l, bool relative) {
+    const float4 a = *reinterpret_cast<const float4*>(l.position_range);
+    float4 c;
+    c.x = relative ? a.x - cam->position_near[0] : a.x;
+    c.y = relative ? a.y - cam->position_near[1] : a.y;
+    c.z = relative ? a.z - cam->position_near[2] : a.z;
+    c.w = l.light_type == 0u ? -1.0f : a.w * a.w * (1.0f + 1.0f / 512.0f);
+    return c;
+}
+
+__global__ void __launch_bounds__(256) prep_cand_kernel(const GpuCamera* __restrict__ cam,
+                                                        const GpuLight* __restrict__ lights, uint32_t n,
+                                                        uint32_t relative, float4* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = cand_entry(cam, lights[i], relative != 0u);
+}
+
+__global__ void __launch_bounds__(256) prep_cand_batched_kernel(const ShadeViewDesc* __restrict__ d,
+                                                                const GpuLight* __restrict__ lights, uint32_t n,
+                                                                uint32_t relative) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const ShadeViewDesc& v = d[blockIdx.y];
+    if (i < n) v.cand[i] = cand_entry(static_cast<const GpuCamera*>(v.camera), lights[i], relative != 0u);
 }
 
 template <uint32_t LAYOUT, uint32_t TARGET>
@@ -512,6 +608,12 @@ cudaError_t launch_batched(const ShadeViewDesc* descs, uint32_t n_views, uint32_
     const int smem = int(sizeof(sk::Smem<32 * 16>));
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
+    if (n > 0) {
+        prep_cand_batched_kernel<<<dim3((n + 255) / 256, n_views), 256, 0, stream>>>(
+            descs, static_cast<const GpuLight*>(lights), n, LAYOUT == HL_GBUF_F16 ? 1u : 0u);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
     kern<<<total_tiles, sk::kThreads, smem, stream>>>(descs, n_views, static_cast<const DeferredGlobals*>(globals),
                                                       static_cast<const GpuLight*>(lights), n, status);
     return cudaGetLastError();
@@ -519,7 +621,7 @@ cudaError_t launch_batched(const ShadeViewDesc* descs, uint32_t n_views, uint32_
 
 template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS>
 cudaError_t launch_one(const void* camera, const void* globals, const GBufView& gb, const void* lights, uint32_t n,
-                       const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats, int* status,
+                       const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats, int* status, float4* cand,
                        cudaStream_t stream) {
     constexpr bool FROXELS = (GRID == HL_GRID_FROXELS);
     constexpr int TW = FROXELS ? 32 : 16, TH = 16;
@@ -533,37 +635,45 @@ cudaError_t launch_one(const void* camera, const void* globals, const GBufView& 
         if (e != cudaSuccess) return e;
         attr_devices |= 1ull << dev;
     }
+    if (n > 0) {
+        prep_cand_kernel<<<(n + 255) / 256, 256, 0, stream>>>(static_cast<const GpuCamera*>(camera),
+                                                              static_cast<const GpuLight*>(lights), n,
+                                                              LAYOUT == HL_GBUF_F16 ? 1u : 0u, cand);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
     const dim3 g((gb.width + TW - 1) / TW, (gb.height + TH - 1) / TH);
     kern<<<g, sk::kThreads, smem, stream>>>(static_cast<const GpuCamera*>(camera),
                                             static_cast<const DeferredGlobals*>(globals), gb,
-                                            static_cast<const GpuLight*>(lights), n, grid, tab, out, stats, status);
+                                            static_cast<const GpuLight*>(lights), n, grid, tab, out, stats, status,
+                                            cand);
     return cudaGetLastError();
 }
 
 template <uint32_t LAYOUT, uint32_t GRID>
 cudaError_t dispatch_target(uint32_t target, const void* camera, const void* globals, const GBufView& gb,
                             const void* lights, uint32_t n, const GridView& grid, const SliceTable& tab,
-                            const TargetView& out, uint32_t* stats, int* status, cudaStream_t stream) {
+                            const TargetView& out, uint32_t* stats, int* status, float4* cand, cudaStream_t stream) {
     if (stats)
         return launch_one<LAYOUT, GRID, HL_TARGET_RGBA32F, true>(camera, globals, gb, lights, n, grid, tab, out, stats,
-                                                                 status, stream);
+                                                                 status, cand, stream);
     if (target == HL_TARGET_RGBA16F)
         return launch_one<LAYOUT, GRID, HL_TARGET_RGBA16F, false>(camera, globals, gb, lights, n, grid, tab, out,
-                                                                  stats, status, stream);
+                                                                  stats, status, cand, stream);
     return launch_one<LAYOUT, GRID, HL_TARGET_RGBA32F, false>(camera, globals, gb, lights, n, grid, tab, out, stats,
-                                                              status, stream);
+                                                              status, cand, stream);
 }
 
 template <uint32_t LAYOUT>
 cudaError_t dispatch_grid(uint32_t grid_kind, uint32_t target, const void* camera, const void* globals,
                           const GBufView& gb, const void* lights, uint32_t n, const GridView& grid,
-                          const SliceTable& tab, const TargetView& out, uint32_t* stats, int* status,
+                          const SliceTable& tab, const TargetView& out, uint32_t* stats, int* status, float4* cand,
                           cudaStream_t stream) {
     if (grid_kind == HL_GRID_FROXELS)
         return dispatch_target<LAYOUT, HL_GRID_FROXELS>(target, camera, globals, gb, lights, n, grid, tab, out, stats,
-                                                        status, stream);
+                                                        status, cand, stream);
     return dispatch_target<LAYOUT, HL_GRID_TILES>(target, camera, globals, gb, lights, n, grid, tab, out, stats,
-                                                  status, stream);
+                                                  status, cand, stream);
 }
 
 }  // namespace
@@ -571,17 +681,17 @@ cudaError_t dispatch_grid(uint32_t grid_kind, uint32_t target, const void* camer
 cudaError_t launch_shade(uint32_t layout, uint32_t grid_kind, uint32_t target_format, const void* camera,
                          const void* globals, const GBufView& gb, const void* lights, uint32_t n_lights,
                          const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats,
-                         int* status, cudaStream_t stream) {
+                         int* status, float4* cand, cudaStream_t stream) {
     switch (layout) {
         case HL_GBUF_REFERENCE:
             return dispatch_grid<HL_GBUF_REFERENCE>(grid_kind, target_format, camera, globals, gb, lights, n_lights,
-                                                    grid, tab, out, stats, status, stream);
+                                                    grid, tab, out, stats, status, cand, stream);
         case HL_GBUF_F32:
             return dispatch_grid<HL_GBUF_F32>(grid_kind, target_format, camera, globals, gb, lights, n_lights, grid,
-                                              tab, out, stats, status, stream);
+                                              tab, out, stats, status, cand, stream);
         default:
             return dispatch_grid<HL_GBUF_F16>(grid_kind, target_format, camera, globals, gb, lights, n_lights, grid,
-                                              tab, out, stats, status, stream);
+                                              tab, out, stats, status, cand, stream);
     }
 }
 

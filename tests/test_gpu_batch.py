@@ -1,5 +1,5 @@
 """GPU tests of the batched-views plan (hl_batch_plan_create / hl_batch_execute): one
-graph of five launches lights every view against one light buffer. Each view's
+graph of six launches lights every view against one light buffer. Each view's
 radiance must be bit-identical to the single-view path (hl_bin_froxels + hl_shade with
 the grid the plan chose), since both run the same binning and shading code; a few views
 are also checked against the float64 oracle (FP16 G-buffer tolerance 2e-3)."""
