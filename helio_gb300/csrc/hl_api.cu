@@ -98,6 +98,7 @@ hl_status hl_destroy(hl_ctx* ctx) {
     cudaFree(ctx->froxel_counts);
     cudaFree(ctx->adjoint_partials);
     cudaFree(ctx->shade_cand);
+    cudaFree(ctx->frag_lights);
     delete ctx;
     return HL_OK;
 }
@@ -218,6 +219,56 @@ hl_status hl_shade_adjoint(hl_ctx* ctx, const void* camera, const void* globals,
                                              d_radiance, d_radiance_pitch, ctx->adjoint_partials, G, d_lights,
                                              d_pixels, ctx->d_status, as_stream(stream));
     return e == cudaSuccess ? HL_OK : cuda_fail(ctx, e, "shade adjoint launch");
+}
+
+hl_status hl_shade_fragments(hl_ctx* ctx, const void* camera, const hl_fragment_params* params, const void* fragments,
+                             uint32_t n_fragments, const void* lights, uint32_t n_lights,
+                             const uint32_t* light_entity_indices, const void* transforms, uint32_t n_transforms,
+                             const hl_light_grid* grid, float* out_rgba, void* stream) {
+    hl_status s = check_common(ctx, camera, lights, n_lights);
+    if (s != HL_OK) return s;
+    if (!params) return fail(ctx, HL_ERR_INVALID_ARGUMENT, "fragment params is NULL");
+    if (params->mode > HL_FRAGMENTS_TRANSPARENT)
+        return fail(ctx, HL_ERR_INVALID_ARGUMENT, "unknown fragment mode %u", params->mode);
+    if (n_fragments > 0 && (!fragments || !aligned(fragments, 16) || !out_rgba || !aligned(out_rgba, 16)))
+        return fail(ctx, HL_ERR_LAYOUT, "fragments / out_rgba NULL or not 16-byte aligned");
+    if (n_fragments > (1u << 30)) return fail(ctx, HL_ERR_SIZE, "%u fragments exceed 2^30", n_fragments);
+    if (light_entity_indices) {
+        if (params->mode != HL_FRAGMENTS_FORWARD)
+            return fail(ctx, HL_ERR_INVALID_ARGUMENT, "light entity indices are read in the forward mode only");
+        if (!aligned(light_entity_indices, 4) || (n_transforms > 0 && (!transforms || !aligned(transforms, 4))))
+            return fail(ctx, HL_ERR_LAYOUT, "entity indices / transforms NULL or not 4-byte aligned");
+    }
+    if (!grid || !grid->lists || !grid->counts) return fail(ctx, HL_ERR_INVALID_ARGUMENT, "light grid is NULL");
+    hl::GridView gv;
+    hl::SliceTable tab;
+    std::memset(&gv, 0, sizeof gv);
+    std::memset(&tab, 0, sizeof tab);
+    gv.lists = grid->lists;
+    gv.counts = grid->counts;
+    if (grid->kind == HL_GRID_TILES) {
+        // the fragments name their tiles through num_tiles_x; lists_capacity bounds them
+        if (grid->lists_capacity < hl::kMaxPerTile || params->num_tiles_x == 0)
+            return fail(ctx, HL_ERR_INVALID_ARGUMENT,
+                        "tile grid for fragments needs lists_capacity (tiles x 64) and num_tiles_x");
+        gv.tiles = grid->lists_capacity / hl::kMaxPerTile;
+        gv.lists_capacity = grid->lists_capacity;
+    } else if (grid->kind == HL_GRID_FROXELS) {
+        if ((s = check_froxel_params(ctx, &grid->froxel)) != HL_OK) return s;
+        gv.fp = grid->froxel;
+        gv.lists_capacity = grid->lists_capacity ? grid->lists_capacity : 0xFFFFFFFFu;
+        slice_table(grid->froxel, tab.z);
+    } else {
+        return fail(ctx, HL_ERR_INVALID_ARGUMENT, "unknown light grid kind %u", grid->kind);
+    }
+    DeviceGuard dg(ctx->device);
+    if (!dg.ok) return fail(ctx, HL_ERR_CUDA, "cudaSetDevice(%d) failed", ctx->device);
+    const size_t need = size_t(n_lights > 0 ? n_lights : 1) * hl::frag_light_bytes();
+    if ((s = ensure(ctx, ctx->frag_lights, ctx->frag_lights_cap, need, "fragment light records")) != HL_OK) return s;
+    cudaError_t e = hl::launch_shade_fragments(camera, *params, fragments, n_fragments, lights, n_lights,
+                                               light_entity_indices, transforms, n_transforms, grid->kind, gv, tab,
+                                               ctx->frag_lights, out_rgba, ctx->d_status, as_stream(stream));
+    return e == cudaSuccess ? HL_OK : cuda_fail(ctx, e, "shade fragments launch");
 }
 
 hl_status hl_probe_fp32_peak(hl_ctx* ctx, double* tflops) {

@@ -21,6 +21,8 @@ struct hl_ctx {
     uint32_t froxel_counts_cap = 0;
     float4* shade_cand = nullptr;       // candidate-test light table of hl_shade
     uint32_t shade_cand_cap = 0;
+    unsigned char* frag_lights = nullptr;  // light records of hl_shade_fragments
+    uint32_t frag_lights_cap = 0;
     float* adjoint_partials = nullptr;  // per-CTA light-gradient partials of hl_shade_adjoint
     uint32_t adjoint_partials_cap = 0;
     std::string last_error;

@@ -78,6 +78,15 @@ cudaError_t launch_shade_batched(uint32_t layout, uint32_t target_format, const 
                                  uint32_t n_views, uint32_t total_tiles, const void* globals, const void* lights,
                                  uint32_t n_lights, int* status, cudaStream_t stream);
 
+// Fragment lighting (Forward+ / transparent light loops). light_scratch: n_lights x
+// frag_light_bytes().
+size_t frag_light_bytes();
+cudaError_t launch_shade_fragments(const void* camera, const hl_fragment_params& prm, const void* frags, uint32_t n,
+                                   const void* lights, uint32_t n_lights, const uint32_t* entity,
+                                   const void* transforms, uint32_t n_xf, uint32_t grid_kind, const GridView& grid,
+                                   const SliceTable& tab, void* light_scratch, float* out, int* status,
+                                   cudaStream_t stream);
+
 cudaError_t run_fp32_probe(int device, double* tflops);
 
 }  // namespace hl

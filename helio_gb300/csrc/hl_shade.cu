@@ -54,6 +54,7 @@ struct Smem {
     uint32_t warp_tot[kWarps];
     float tab[kMaxSlices + 1];      // slice boundaries
     uint32_t n_valid;
+    uint32_t next_group;            // next group of sorted pixels to hand to a warp
     uint16_t col_of[32], row_of[16];  // froxel column / row of the tile's pixel columns / rows
 };
 
@@ -350,7 +351,10 @@ __device__ __forceinline__ void shade_tile(
         __syncthreads();
         s.hist[2 * t] = excl;
         s.hist[2 * t + 1] = excl + a;
-        if (t == 0) s.n_valid = total;
+        if (t == 0) {
+            s.n_valid = total;
+            s.next_group = 0;
+        }
     }
     __syncthreads();
 #pragma unroll
@@ -366,9 +370,15 @@ __device__ __forceinline__ void shade_tile(
     uint32_t head = 0;  // ring position of the oldest pending pair
 
 #pragma unroll 1
-    for (int gi = 0; gi < NG / kWarps; ++gi) {
-        // warp w takes group w and, with 16 groups, group 15 - w (a light and a heavy one)
-        const uint32_t g = gi == 0 ? warp : uint32_t(NG - 1) - warp;
+    for (;;) {
+        // warps take groups as they finish, last group first: the far slices sort last
+        // and hold the longest lists, so the long work starts early
+        uint32_t g = 0;
+        if (lane == 0) g = atomicAdd(&s.next_group, 1u);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= uint32_t(NG)) break;
+        g = uint32_t(NG - 1) - g;
+        if (g * 32u >= n_valid) continue;  // empty group
         const uint32_t gs = g * 32 + lane;
         const bool own = gs < n_valid;
         const uint32_t i = own ? s.order[gs] : 0u;

@@ -344,10 +344,11 @@ constexpr float kFastMinNdV = 1.0f / 8192.0f;
 
 // pbr_direct_light (deferred_lighting.wgsl:699-820) for a non-anisotropic, non-SSS
 // surface, sf = 1. Returns kCut (out* untouched) when a cut applies, kLit with the
-// contribution in out*, or — on the fast path with guard > 0 — kNeedsPrecise.
+// contribution in out*, or — on the fast path with guard > 0 — kNeedsPrecise. `cut` is
+// the radiance cut (0.002, :781); 0 disables it, as the Forward+ shader has none.
 template <bool PRECISE>
 HL_HD int eval(const Pixel& p, const PixelBrdf& b, const ShadeLight& l, float& outr, float& outg, float& outb,
-               float guard = 0.0f) {
+               float guard = 0.0f, float cut = kRadianceCut) {
     float Lx, Ly, Lz, rr, rg, rb;
     float NdL, d2_near = 0.0f, fall_near = 1.0f;
     if (l.type == 0u) {
@@ -427,7 +428,7 @@ HL_HD int eval(const Pixel& p, const PixelBrdf& b, const ShadeLight& l, float& o
             return kNeedsPrecise;
     }
     if (!(NdL > 0.0f)) return kCut;
-    if (rr < kRadianceCut && rg < kRadianceCut && rb < kRadianceCut) return kCut;
+    if (rr < cut && rg < cut && rb < cut) return kCut;
     // H = normalize(V + L)
     const float hx = p.Vx + Lx, hy = p.Vy + Ly, hz = p.Vz + Lz;
     const float ih = rsqrt_(fma_(hz, hz, fma_(hy, hy, hx * hx)));

@@ -127,6 +127,36 @@ FROXEL_PARAMS = np.dtype(
     ]
 )
 
+# One fragment for hl_shade_fragments (the inputs of the Forward+ and transparent
+# fragment shaders' light loops, forward_lit.wgsl:443-494, transparent_base.wgsl:181-220)
+FRAGMENT = np.dtype(
+    [
+        ("position", "<f4", (3,)),
+        ("pixel", "<u4"),
+        ("normal", "<f4", (3,)),
+        ("alpha", "<f4"),
+        ("albedo", "<f4", (3,)),
+        ("roughness", "<f4"),
+        ("f0", "<f4", (3,)),
+        ("metallic", "<f4"),
+        ("emissive", "<f4", (3,)),
+        ("ao", "<f4"),
+    ]
+)
+
+# The scene's Transform record (forward_lit.wgsl:118-122); rotation in degrees
+TRANSFORM = np.dtype([("position", "<f4", (3,)), ("rotation", "<f4", (3,)), ("scale", "<f4", (3,))])
+
+FRAGMENT_PARAMS = np.dtype(
+    [
+        ("mode", "<u4"),
+        ("num_tiles_x", "<u4"),
+        ("ambient_intensity", "<f4"),
+        ("ambient_color", "<f4", (3,)),
+    ]
+)
+FRAGMENTS_FORWARD, FRAGMENTS_TRANSPARENT = 0, 1
+
 # CSM split distances written into DeferredGlobals (libhelio/src/shadow.rs:13)
 CSM_SPLITS = (16.0, 80.0, 300.0, 1400.0)
 
@@ -137,6 +167,9 @@ EXPECTED_SIZES = {
     "LIGHT_CULL_PARAMS": 32,
     "GPU_MATERIAL": 96,
     "FROXEL_PARAMS": 32,
+    "FRAGMENT": 80,
+    "TRANSFORM": 36,
+    "FRAGMENT_PARAMS": 24,
 }
 
 for _name, _size in EXPECTED_SIZES.items():

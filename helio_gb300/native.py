@@ -78,11 +78,18 @@ class BatchConfig(C.Structure):
     ]
 
 
+class FragmentParams(C.Structure):
+    _fields_ = [("mode", C.c_uint32), ("num_tiles_x", C.c_uint32), ("ambient_intensity", C.c_float),
+                ("ambient_color", C.c_float * 3)]
+
+
+FRAGMENTS_FORWARD, FRAGMENTS_TRANSPARENT = 0, 1
+
 EXPORTS = [
     "hl_abi_version", "hl_status_string", "hl_create", "hl_destroy", "hl_last_error_message", "hl_sync_status",
     "hl_tile_count", "hl_bin_tiles_ref", "hl_froxel_slice_table", "hl_bin_froxels", "hl_shade", "hl_shade_stats",
     "hl_shade_adjoint", "hl_batch_plan_create", "hl_batch_execute", "hl_batch_plan_view_grid",
-    "hl_batch_plan_destroy", "hl_probe_fp32_peak", "hl_bin_froxels_noalloc",
+    "hl_batch_plan_destroy", "hl_probe_fp32_peak", "hl_bin_froxels_noalloc", "hl_shade_fragments",
 ]
 
 _lock = threading.Lock()
@@ -149,6 +156,8 @@ def _bind(l):
     l.hl_probe_fp32_peak.restype = i32
     l.hl_bin_froxels_noalloc.argtypes = [vp, vp, u32, P(FroxelParams), P(FroxelLists), vp]
     l.hl_bin_froxels_noalloc.restype = i32
+    l.hl_shade_fragments.argtypes = [vp, vp, P(FragmentParams), vp, u32, vp, u32, vp, vp, u32, P(LightGrid), vp, vp]
+    l.hl_shade_fragments.restype = i32
 
 
 def status_string(status: int) -> str:
@@ -272,6 +281,14 @@ class Context:
         self._check(self._l.hl_shade_adjoint(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer), _ptr(lights),
                                              n_lights, C.byref(grid), _ptr(d_radiance), int(d_radiance_pitch),
                                              _ptr(d_lights), _ptr(d_pixels), _stream(stream)), "hl_shade_adjoint")
+
+    def shade_fragments(self, camera, params: FragmentParams, fragments, n_fragments, lights, n_lights,
+                        grid: LightGrid, out_rgba, entity_indices=None, transforms=None, n_transforms=0, stream=None):
+        """Forward+ / transparent light loops over hl_fragment records (80 B each)."""
+        self._check(self._l.hl_shade_fragments(self._h, _ptr(camera), C.byref(params), _ptr(fragments), n_fragments,
+                                               _ptr(lights), n_lights, _ptr(entity_indices), _ptr(transforms),
+                                               n_transforms, C.byref(grid), _ptr(out_rgba), _stream(stream)),
+                    "hl_shade_fragments")
 
     def batch_plan(self, views, lights, n_lights, globals_, grid=None, autotune=False, cache_path=None,
                    stream=None) -> "BatchPlan":

@@ -271,6 +271,62 @@ hl_status hl_shade_adjoint(hl_ctx* ctx, const void* camera, const void* globals,
                            void* stream);
 
 /* ---------------------------------------------------------------------------------
+ * Fragment lighting: the other consumers of the light lists
+ * -------------------------------------------------------------------------------*/
+
+/* One fragment to light, 80 bytes, records 16-byte aligned. */
+typedef struct hl_fragment {
+    float position[3]; /* world position                                           */
+    uint32_t pixel;    /* x | (y << 16): its pixel, for the tile or froxel lookup   */
+    float normal[3];   /* world normal (normalised by the kernel)                  */
+    float alpha;
+    float albedo[3];
+    float roughness;
+    float f0[3];       /* specular F0 as the material resolved it (not clamped)     */
+    float metallic;
+    float emissive[3]; /* forward: emissive; transparent: the surface colour        */
+    float ao;
+} hl_fragment;
+
+#define HL_FRAGMENTS_FORWARD 0u     /* forward_lit.wgsl:443-494 (Forward+)          */
+#define HL_FRAGMENTS_TRANSPARENT 1u /* transparent_base.wgsl:181-220                */
+
+typedef struct hl_fragment_params {
+    uint32_t mode;            /* HL_FRAGMENTS_*                                        */
+    uint32_t num_tiles_x;     /* tile grid: tiles per row (the pass globals' value)    */
+    float ambient_intensity;  /* forward: globals.ambient_intensity                    */
+    float ambient_color[3];   /* forward: globals.ambient_color.rgb                    */
+} hl_fragment_params;
+
+/* Size of the scene's Transform record (position[3], rotation[3] in degrees as
+ * pitch x / yaw y / roll z, scale[3]; forward_lit.wgsl:118-122). */
+#define HL_SIZEOF_TRANSFORM 36u
+
+/* Lights `n_fragments` fragments from the tile or froxel lists of `grid` and writes
+ * out_rgba[i] (RGBA32F) for fragment i:
+ *   HL_FRAGMENTS_FORWARD      Lo + ambient_color * ambient_intensity * albedo * ao
+ *                             + emissive, alpha; fragments with alpha <= 0.001 are
+ *                             discarded (their output untouched); no 0.002 radiance
+ *                             cut. With light_entity_indices, light i's position and
+ *                             direction come from transforms[light_entity_indices[i]]
+ *                             (direction = rotation applied to -Z, Euler order Y X Z),
+ *                             as the Forward+ pass reads them; otherwise from the
+ *                             GpuLight records.
+ *   HL_FRAGMENTS_TRANSPARENT  emissive (the surface colour) + Lo, alpha; lights from
+ *                             the GpuLight records; the 0.002 radiance cut applies.
+ * Lo sums pbr_direct_light over the fragment's list in list order, skipping lights out
+ * of range. A tile grid takes the tile (y/16) * num_tiles_x + x/16 of the pixel; a froxel
+ * grid the pixel's column and the slice of the view depth -(view * position).z.
+ * Entity indices >= n_transforms and list entries >= n_lights are skipped and
+ * reported through hl_sync_status (HL_ERR_DEVICE_BOUNDS). No reference counterpart
+ * as one call: it replaces the light loops of the two fragment shaders named above. */
+hl_status hl_shade_fragments(hl_ctx* ctx, const void* camera, const hl_fragment_params* params,
+                             const void* fragments, uint32_t n_fragments, const void* lights,
+                             uint32_t n_lights, const uint32_t* light_entity_indices,
+                             const void* transforms, uint32_t n_transforms,
+                             const hl_light_grid* grid, float* out_rgba, void* stream);
+
+/* ---------------------------------------------------------------------------------
  * Batched views (no reference counterpart)
  * -------------------------------------------------------------------------------*/
 

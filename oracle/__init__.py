@@ -64,6 +64,10 @@ def _bind(l):
     l.oracle_shade_f64.argtypes = shade_args
     l.oracle_shade_f32.argtypes = shade_args
     l.oracle_shade_adjoint_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, f64p, f64p, f64p]
+    frag_args = [vp, vp, vp, u32, vp, u32, u32p, vp, u32, u32, u32p, u32p, vp, f64p]
+    l.oracle_shade_fragments_f64.argtypes = frag_args
+    l.oracle_shade_fragments_f32.argtypes = frag_args
+    l.oracle_light_dir_from_rotation.argtypes = [f32p, f64p]
     l.oracle_set_threads.argtypes = [C.c_int]
     l.oracle_num_threads.restype = C.c_int
     return l
@@ -163,6 +167,34 @@ def shade(camera_rec, globals_rec, gb, lights, grid, precision="f64", rows=None,
        _ptr(lts) if len(lts) else None, len(lts), kind, _ptr(lists), _ptr(counts),
        _ptr(params) if params is not None else None, _ptr(out), _ptr(pc) if pc is not None else None, r0, r1)
     return (out, pc) if pair_counts else out
+
+
+def shade_fragments(camera_rec, params, fragments, lights, grid, entity_indices=None, transforms=None,
+                    precision="f64"):
+    """Lit fragments (n, 4) float64 of the Forward+ (params mode 0) or transparent (mode 1)
+    light loop; discarded fragments (forward, alpha <= 0.001) are NaN. ``params``: one
+    FRAGMENT_PARAMS record; ``transforms``: TRANSFORM records indexed by
+    ``entity_indices`` (forward mode)."""
+    fr = np.ascontiguousarray(fragments)
+    out = np.full((len(fr), 4), np.nan, np.float64)
+    kind, lists, counts, fparams = _grid_args(grid)
+    lts = np.ascontiguousarray(lights)
+    ent = np.ascontiguousarray(entity_indices, np.uint32) if entity_indices is not None else None
+    xf = np.ascontiguousarray(transforms) if transforms is not None else None
+    fn = lib().oracle_shade_fragments_f64 if precision == "f64" else lib().oracle_shade_fragments_f32
+    fn(_ptr(np.ascontiguousarray(camera_rec)), _ptr(np.ascontiguousarray(params)), _ptr(fr) if len(fr) else None,
+       len(fr), _ptr(lts) if len(lts) else None, len(lts), _ptr(ent) if ent is not None else None,
+       _ptr(xf) if xf is not None and len(xf) else None, len(xf) if xf is not None else 0, kind, _ptr(lists),
+       _ptr(counts), _ptr(fparams) if fparams is not None else None, _ptr(out))
+    return out
+
+
+def light_dir_from_rotation(rotation_deg):
+    """Unit direction of a Transform rotation (degrees: pitch x, yaw y, roll z)."""
+    r = np.ascontiguousarray(rotation_deg, np.float32)
+    out = np.zeros(3, np.float64)
+    lib().oracle_light_dir_from_rotation(_ptr(r), _ptr(out))
+    return out
 
 
 def shade_adjoint(camera_rec, globals_rec, gb, lights, grid, weights):

@@ -504,7 +504,7 @@ template <class T> struct PairStats {
 // BRDF was evaluated (passed the NdL and radiance cuts).
 template <class T>
 bool pbr_direct_light(const RawLight& l, V3<T> P, V3<T> N, V3<T> V, V3<T> F0, V3<T> albedo, T rough,
-                      T metal, V3<T>& out) {
+                      T metal, V3<T>& out, bool radiance_cut = true) {
     V3<T> L, radiance;
     const V3<T> color = v3<T>(l.color[0], l.color[1], l.color[2]);
     const T intensity = T(l.intensity);
@@ -528,7 +528,10 @@ bool pbr_direct_light(const RawLight& l, V3<T> P, V3<T> N, V3<T> V, V3<T> F0, V3
     T NdL = tmax(dot(N, L), T(0));
     if (NdL == T(0)) { out = v3<T>(0, 0, 0); return false; }
     const T cut = T(0.002);
-    if (radiance.x < cut && radiance.y < cut && radiance.z < cut) { out = v3<T>(0, 0, 0); return false; }
+    if (radiance_cut && radiance.x < cut && radiance.y < cut && radiance.z < cut) {
+        out = v3<T>(0, 0, 0);
+        return false;
+    }
 
     V3<T> H = normalize(V + L);
     // fresnel_schlick (pbr_eval.wgsl:59-61)
@@ -669,6 +672,128 @@ void shade_impl(const void* camera, const void* globals, const GBufferDesc& g, c
                 pair_counts[pix * 3 + 2] = n_full;
             }
         }
+    }
+}
+
+// ---- fragment lighting (forward_lit.wgsl:443-494, transparent_base.wgsl:181-220) ----
+
+struct RawFragment {
+    float pos[3];
+    uint32_t pixel;
+    float normal[3], alpha;
+    float albedo[3], rough;
+    float f0[3], metal;
+    float emissive[3], ao;
+};
+static_assert(sizeof(RawFragment) == 80, "hl_fragment is 80 bytes");
+
+struct RawTransform {
+    float pos[3], rot[3], scale[3];
+};
+static_assert(sizeof(RawTransform) == 36, "Transform is 36 bytes (forward_lit.wgsl:118-122)");
+
+struct FragmentParams {
+    uint32_t mode, num_tiles_x;
+    float ambient_intensity, ambient_color[3];
+};
+
+// Light direction of a Transform rotation (forward_lit.wgsl:374-383): the rotation
+// q = qy(yaw) qx(pitch) qz(roll) of Euler order Y, X, Z applied to (0, 0, -1).
+template <class T> V3<T> light_dir_from_rotation(const float rot_deg[3]) {
+    const T deg = T(3.14159265358979323846) / T(180);
+    const T hp = T(rot_deg[0]) * deg * T(0.5), hy = T(rot_deg[1]) * deg * T(0.5), hr = T(rot_deg[2]) * deg * T(0.5);
+    struct Q { T x, y, z, w; };
+    auto mul = [](Q a, Q b) {
+        return Q{a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y, a.w * b.y - a.x * b.z + a.y * b.w + a.z * b.x,
+                 a.w * b.z + a.x * b.y - a.y * b.x + a.z * b.w, a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z};
+    };
+    const Q qy{T(0), std::sin(hy), T(0), std::cos(hy)};
+    const Q qx{std::sin(hp), T(0), T(0), std::cos(hp)};
+    const Q qz{T(0), T(0), std::sin(hr), std::cos(hr)};
+    const Q q = mul(mul(qy, qx), qz);
+    // v + w t + q.xyz x t with t = 2 q.xyz x v, v = (0, 0, -1)
+    const V3<T> qv = v3<T>(q.x, q.y, q.z), v = v3<T>(T(0), T(0), T(-1));
+    const V3<T> t = cross(qv, v) * T(2);
+    return normalize(v + t * q.w + cross(qv, t));
+}
+
+template <class T>
+void shade_fragments_impl(const void* camera, const FragmentParams& fp, const RawFragment* frags, uint32_t n,
+                          const void* lights, uint32_t n_lights, const uint32_t* entity, const RawTransform* xf,
+                          uint32_t n_xf, const GridDesc& grid, double* out_rgba /* n*4, untouched if discarded */) {
+    Cam<T> c = load_camera<T>(camera);
+    RawCamera rc;
+    std::memcpy(&rc, camera, sizeof rc);
+    std::vector<RawLight> L(n_lights);
+    std::vector<uint8_t> usable(n_lights, 1);
+    for (uint32_t i = 0; i < n_lights; ++i) {
+        L[i] = load_light(lights, i);
+        if (fp.mode == 0 && entity) {
+            if (entity[i] >= n_xf) {
+                usable[i] = 0;
+                continue;
+            }
+            const RawTransform& t = xf[entity[i]];
+            const V3<T> d = light_dir_from_rotation<T>(t.rot);
+            for (int k = 0; k < 3; ++k) L[i].pos[k] = t.pos[k];
+            L[i].dir[0] = float(d.x);
+            L[i].dir[1] = float(d.y);
+            L[i].dir[2] = float(d.z);
+        }
+    }
+    std::vector<float> tab;
+    if (grid.kind == 1) {
+        tab.resize(grid.froxel.gz + 1);
+        slice_table(grid.froxel, tab.data());
+    }
+    const V3<T> amb = v3<T>(T(fp.ambient_color[0]) * T(fp.ambient_intensity), T(fp.ambient_color[1]) * T(fp.ambient_intensity),
+                            T(fp.ambient_color[2]) * T(fp.ambient_intensity));
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t ii = 0; ii < int64_t(n); ++ii) {
+        const RawFragment& f = frags[ii];
+        if (fp.mode == 0 && !(f.alpha > 0.001f)) continue;  // discard
+        const uint32_t x = f.pixel & 0xFFFFu, y = f.pixel >> 16;
+        const V3<T> P = v3<T>(f.pos[0], f.pos[1], f.pos[2]);
+        const V3<T> N = normalize(v3<T>(f.normal[0], f.normal[1], f.normal[2]));
+        const V3<T> V = normalize(c.pos - P);
+        const V3<T> F0 = v3<T>(f.f0[0], f.f0[1], f.f0[2]);
+        const V3<T> albedo = v3<T>(f.albedo[0], f.albedo[1], f.albedo[2]);
+        const uint32_t* list = nullptr;
+        uint32_t count = 0;
+        if (grid.kind == 0) {
+            const uint32_t tile = (y / kTile) * fp.num_tiles_x + x / kTile;
+            count = grid.counts[tile];
+            list = grid.lists + size_t(tile) * kMaxPerTile;
+        } else {
+            // view depth -(view * P).z, column-major view matrix
+            const T zv = T(rc.view[2]) * P.x + T(rc.view[6]) * P.y + T(rc.view[10]) * P.z + T(rc.view[14]);
+            const uint32_t fr = froxel_of_pixel<T>(grid.froxel, tab.data(), x, y, -zv);
+            count = grid.counts[fr + 1] - grid.counts[fr];
+            list = grid.lists + grid.counts[fr];
+        }
+        V3<T> Lo = v3<T>(0, 0, 0);
+        for (uint32_t j = 0; j < count; ++j) {
+            const uint32_t idx = list[j];
+            if (idx >= n_lights || !usable[idx]) continue;
+            const RawLight& l = L[idx];
+            if (l.type != 0u) {
+                V3<T> dl = v3<T>(l.pos[0], l.pos[1], l.pos[2]) - P;
+                if (tsqrt(dot(dl, dl)) > T(l.range)) continue;
+            }
+            V3<T> contrib;
+            pbr_direct_light(l, P, N, V, F0, albedo, T(f.rough), T(f.metal), contrib, fp.mode != 0);
+            Lo = Lo + contrib;
+        }
+        V3<T> color;
+        if (fp.mode == 0)
+            color = Lo + (amb * albedo) * T(f.ao) + v3<T>(f.emissive[0], f.emissive[1], f.emissive[2]);
+        else
+            color = v3<T>(f.emissive[0], f.emissive[1], f.emissive[2]) + Lo;
+        double* o = out_rgba + size_t(ii) * 4;
+        o[0] = double(color.x);
+        o[1] = double(color.y);
+        o[2] = double(color.z);
+        o[3] = double(f.alpha);
     }
 }
 
@@ -946,6 +1071,35 @@ void oracle_shade_f32(const void* cam, const void* globals, uint32_t layout, uin
 
 // Adjoint on an F32 G-buffer with a froxel (or tile) grid. w: W*H*4 (alpha ignored).
 // d_lights: n*7 doubles (pos xyz, intensity, color rgb); d_pix: W*H*5 doubles.
+void oracle_shade_fragments_f64(const void* cam, const void* params, const void* frags, uint32_t n, const void* lights,
+                                uint32_t n_lights, const uint32_t* entity, const void* transforms, uint32_t n_xf,
+                                uint32_t grid_kind, const uint32_t* lists, const uint32_t* counts, const void* froxel,
+                                double* out_rgba) {
+    FragmentParams fp;
+    std::memcpy(&fp, params, sizeof fp);
+    GridDesc gr = make_grid(grid_kind, lists, counts, froxel);
+    shade_fragments_impl<double>(cam, fp, static_cast<const RawFragment*>(frags), n, lights, n_lights, entity,
+                                 static_cast<const RawTransform*>(transforms), n_xf, gr, out_rgba);
+}
+
+void oracle_shade_fragments_f32(const void* cam, const void* params, const void* frags, uint32_t n, const void* lights,
+                                uint32_t n_lights, const uint32_t* entity, const void* transforms, uint32_t n_xf,
+                                uint32_t grid_kind, const uint32_t* lists, const uint32_t* counts, const void* froxel,
+                                double* out_rgba) {
+    FragmentParams fp;
+    std::memcpy(&fp, params, sizeof fp);
+    GridDesc gr = make_grid(grid_kind, lists, counts, froxel);
+    shade_fragments_impl<float>(cam, fp, static_cast<const RawFragment*>(frags), n, lights, n_lights, entity,
+                                static_cast<const RawTransform*>(transforms), n_xf, gr, out_rgba);
+}
+
+void oracle_light_dir_from_rotation(const float* rot_deg, double* out) {
+    const V3<double> d = light_dir_from_rotation<double>(rot_deg);
+    out[0] = d.x;
+    out[1] = d.y;
+    out[2] = d.z;
+}
+
 void oracle_shade_adjoint_f64(const void* cam, const void* globals, uint32_t layout, uint32_t W, uint32_t H,
                               const void* const* planes, const uint64_t* pitch, const void* lights, uint32_t n,
                               uint32_t grid_kind, const uint32_t* lists, const uint32_t* counts, const void* froxel,

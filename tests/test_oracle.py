@@ -13,7 +13,8 @@ import oracle
 from helio_gb300 import layouts as L
 from helio_gb300 import synthetic as S
 
-from scenes import mixed_lights, overlapping_lights, point_light, spot_light, directional_light
+from scenes import (directional_light, fragment_params, fragments, mixed_lights, overlapping_lights,
+                    point_light, spot_light)
 
 GOLDEN = Path(__file__).resolve().parent / "golden" / "shade_golden.npz"
 PI = 3.14159265359
@@ -308,3 +309,78 @@ def test_adjoint_matches_finite_differences():
             hh = float(gp[plane][y, x, comp]) - float(gm[plane][y, x, comp])
             fd = (loss(lt, S.GBuffer(1, W, H, gp)) - loss(lt, S.GBuffer(1, W, H, gm))) / hh
             assert abs(fd - dp[y, x, c]) <= 2e-3 * max(abs(fd), abs(dp[y, x, c])) + 1e-6, (y, x, c, fd, dp[y, x, c])
+
+
+# ----------------------------------------------------------------------------------
+# fragment lighting (Forward+ and transparent light loops)
+# ----------------------------------------------------------------------------------
+
+
+@pytest.mark.parametrize("rot,want", [((0, 0, 0), (0, 0, -1)), ((0, 90, 0), (-1, 0, 0)), ((90, 0, 0), (0, 1, 0)),
+                                      ((0, 0, 90), (0, 0, -1)), ((0, 180, 0), (0, 0, 1)), ((-90, 0, 0), (0, -1, 0))])
+def test_light_direction_from_rotation(rot, want):
+    """Euler Y, X, Z (yaw, pitch, roll in degrees) applied to -Z (forward_lit.wgsl:374-383)."""
+    np.testing.assert_allclose(oracle.light_dir_from_rotation(rot), want, atol=1e-12)
+
+
+def _fragment_scene(seed=21, n=600, W=64, H=48):
+    cam = S.make_camera((0.2, 0.1, 0.3), (0.0, 0.0, -8.0), (0, 1, 0), 60.0, W, H)
+    lt = mixed_lights(cam, seed, n_point=20, n_spot=8, n_dir=1)
+    fr = fragments(cam, seed, n)
+    lists, counts = oracle.bin_tiles_ref(cam.record, lt, W, H)
+    return cam, lt, fr, ("tiles", lists, counts)
+
+
+def test_fragment_modes_agree_without_ambient_emission_or_cut():
+    """With no ambient, no emission and every radiance above the 0.002 cut, the forward
+    and transparent light loops are the same sum."""
+    cam, lt, fr, grid = _fragment_scene()
+    lt["color_intensity"][:, 3] = 1e4  # all radiances >> 0.002 inside the range
+    fr["emissive"] = 0.0
+    tx = L.tile_grid(cam.width, cam.height)[0]
+    fwd = oracle.shade_fragments(cam.record, fragment_params(L.FRAGMENTS_FORWARD, tx, 0.0), fr, lt, grid)
+    tra = oracle.shade_fragments(cam.record, fragment_params(L.FRAGMENTS_TRANSPARENT, tx, 0.0), fr, lt, grid)
+    keep = fr["alpha"] > 0.001
+    assert np.isnan(fwd[~keep]).all() and not np.isnan(tra).any()
+    assert (fwd[keep][:, :3] > 0).any()
+    np.testing.assert_allclose(fwd[keep], tra[keep], rtol=1e-12, atol=0)
+
+
+def test_fragment_forward_ambient_and_emission():
+    cam, lt, fr, grid = _fragment_scene()
+    tx = L.tile_grid(cam.width, cam.height)[0]
+    base = oracle.shade_fragments(cam.record, fragment_params(L.FRAGMENTS_FORWARD, tx, 0.0), fr, lt, grid)
+    amb = oracle.shade_fragments(cam.record, fragment_params(L.FRAGMENTS_FORWARD, tx, 0.8, (0.2, 0.4, 0.6)), fr, lt,
+                                 grid)
+    keep = fr["alpha"] > 0.001
+    want = (0.8 * np.array([0.2, 0.4, 0.6], np.float32).astype(np.float64) * fr["albedo"][keep] *
+            fr["ao"][keep][:, None])
+    np.testing.assert_allclose(amb[keep][:, :3] - base[keep][:, :3], want, rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(amb[keep][:, 3], fr["alpha"][keep])
+
+
+def test_fragment_forward_reads_light_transforms():
+    """Forward mode with entity indices reads positions and directions from the
+    transforms; with transforms equal to the records' own values nothing changes."""
+    cam, lt, fr, grid = _fragment_scene()
+    n = len(lt)
+    rng = np.random.default_rng(5)
+    rot = rng.uniform(-180, 180, (n, 3)).astype(np.float32)
+    dirs = np.stack([oracle.light_dir_from_rotation(r) for r in rot]).astype(np.float32)
+    lt["direction_outer"][:, :3] = dirs
+    perm = rng.permutation(n).astype(np.uint32)  # light i -> entity perm[i]
+    xf = np.zeros(n, L.TRANSFORM)
+    xf["position"][perm] = lt["position_range"][:, :3]
+    xf["rotation"][perm] = rot
+    tx = L.tile_grid(cam.width, cam.height)[0]
+    prm = fragment_params(L.FRAGMENTS_FORWARD, tx)
+    own = oracle.shade_fragments(cam.record, prm, fr, lt, grid)
+    via = oracle.shade_fragments(cam.record, prm, fr, lt, grid, entity_indices=perm, transforms=xf)
+    np.testing.assert_array_equal(np.isnan(own), np.isnan(via))
+    k = ~np.isnan(own[:, 0])
+    np.testing.assert_allclose(via[k], own[k], rtol=1e-12, atol=1e-300)
+    # an entity index out of range drops that light (here the directional light)
+    bad = perm.copy()
+    bad[int(np.flatnonzero(lt["light_type"] == L.LIGHT_DIRECTIONAL)[0])] = n + 7
+    dropped = oracle.shade_fragments(cam.record, prm, fr, lt, grid, entity_indices=bad, transforms=xf)
+    assert not np.allclose(dropped[k], own[k])
