@@ -98,6 +98,8 @@ hl_status hl_destroy(hl_ctx* ctx) {
     cudaFree(ctx->froxel_counts);
     cudaFree(ctx->adjoint_partials);
     cudaFree(ctx->shade_cand);
+    cudaFree(ctx->froxel_chain);
+    cudaFree(ctx->bin_state);
     cudaFree(ctx->frag_lights);
     delete ctx;
     return HL_OK;
@@ -162,19 +164,30 @@ hl_status hl_bin_froxels(hl_ctx* ctx, const void* camera, const void* lights, ui
     if ((s = check_froxel_params(ctx, p)) != HL_OK) return s;
     if (!out || !out->offsets) return fail(ctx, HL_ERR_INVALID_ARGUMENT, "froxel output offsets is NULL");
     if (out->capacity > 0 && !out->indices) return fail(ctx, HL_ERR_INVALID_ARGUMENT, "froxel indices is NULL");
-    const uint32_t F = p->grid_x * p->grid_y * p->grid_z;
     DeviceGuard dg(ctx->device);
     if (!dg.ok) return fail(ctx, HL_ERR_CUDA, "cudaSetDevice(%d) failed", ctx->device);
     if ((s = ensure(ctx, ctx->bin_lights, ctx->bin_lights_cap, n > 0 ? n : 1, "bin light scratch")) != HL_OK) return s;
-    if ((s = ensure(ctx, ctx->froxel_counts, ctx->froxel_counts_cap, F, "froxel count scratch")) != HL_OK) return s;
+    // single-pass binning state: chain words (zeroed when allocated: epoch 0 is never
+    // used) and the column ticket counter
+    const uint32_t cols = p->grid_x * p->grid_y;
+    unsigned long long* old_chain = ctx->froxel_chain;
+    if ((s = ensure(ctx, ctx->froxel_chain, ctx->froxel_chain_cap, cols, "froxel chain scratch")) != HL_OK) return s;
+    cudaStream_t st = as_stream(stream);
+    cudaError_t e = cudaSuccess;
+    if (ctx->froxel_chain != old_chain)
+        e = cudaMemsetAsync(ctx->froxel_chain, 0, sizeof(unsigned long long) * ctx->froxel_chain_cap, st);
+    if (e == cudaSuccess && !ctx->bin_state) {
+        e = cudaMalloc(&ctx->bin_state, sizeof(hl::BinChainState));
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->bin_state, 0, sizeof(hl::BinChainState), st);
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "froxel chain set-up");
     hl::SliceTable tab;
     std::memset(&tab, 0, sizeof tab);
     slice_table(*p, tab.z);
-    cudaStream_t st = as_stream(stream);
-    cudaError_t e = hl::launch_prep_bin_lights(camera, lights, n, true, ctx->bin_lights, st);
+    e = hl::launch_prep_bin_lights(camera, lights, n, true, ctx->bin_lights, st);
     if (e == cudaSuccess)
-        e = hl::launch_bin_froxels(camera, ctx->bin_lights, n, *p, tab, ctx->froxel_counts, out->offsets, out->indices,
-                                   out->capacity, ctx->d_status, st);
+        e = hl::launch_bin_froxels_fused(camera, ctx->bin_lights, n, *p, tab, out->offsets, out->indices,
+                                         out->capacity, ctx->d_status, ctx->froxel_chain, ctx->bin_state, st);
     return e == cudaSuccess ? HL_OK : cuda_fail(ctx, e, "bin_froxels launch");
 }
 

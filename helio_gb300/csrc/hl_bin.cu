@@ -334,6 +334,216 @@ __global__ void __launch_bounds__(kBinThreads) bin_froxels_kernel(const GpuCamer
     bin_column<FILL>(sm, cam, bl, n, p, tab.z, blockIdx.x, counts, offsets, indices, capacity, status);
 }
 
+// ---- single pass: count, chained scan across columns, fill — one launch ----------
+//
+// Each CTA takes a column by ticket (a device counter, so CTA k waits only for columns
+// that started before it), counts its slices, publishes its total, finds the entries
+// of all earlier columns by looking back along the chain of published totals
+// (decoupled look-back: a predecessor's inclusive prefix ends the walk, its bare total
+// is added and the walk goes on), publishes its own inclusive prefix, writes its
+// offsets and fills its lists. Chain words hold epoch << 32 | state << 30 | value; a
+// word of another launch's epoch reads as "not yet published". The ticket base and the
+// epoch live on the device and the last CTA of a launch advances them, so a launch
+// recorded in a CUDA graph can be replayed.
+constexpr uint32_t kFlagAggregate = 1u, kFlagPrefix = 2u;
+constexpr uint32_t kChainValueMax = (1u << 30) - 1u;
+constexpr uint32_t kLookbackSpins = 1u << 20;  // ~0.1 s of polling before HL_ERR_TIMEOUT
+
+struct FusedSmem {
+    BinSmem b;
+    uint32_t slice_dst[kMaxSlices];  // first entry of each slice of this column
+    uint32_t col, excl, total;
+};
+
+__device__ __forceinline__ unsigned long long ld_chain(const unsigned long long* p) {
+    return *reinterpret_cast<const volatile unsigned long long*>(p);
+}
+
+__device__ __forceinline__ void st_chain(unsigned long long* p, uint32_t epoch, uint32_t state, uint32_t value) {
+    __threadfence();
+    *reinterpret_cast<volatile unsigned long long*>(p) =
+        (static_cast<unsigned long long>(epoch) << 32) | (state << 30) | min(value, kChainValueMax);
+}
+
+// Gathers the next round of a column's candidate lights into sm.col (light-index order).
+__device__ __forceinline__ uint32_t gather_round(BinSmem& sm, const ColumnGeom& g, const BinLight* __restrict__ bl,
+                                                 uint32_t n, uint32_t& base) {
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t col_len = 0;
+    __syncthreads();
+    while (base < n && col_len + kBinThreads <= kColCap) {
+        const uint32_t i = base + threadIdx.x;
+        bool pass = false;
+        if (i < n) {
+            const BinLight l = bl[i];
+            pass = (l.type == 0u) || sphere_in_planes(g.planes, l.cx, l.cy, l.cz, l.r);
+        }
+        const uint32_t mask = __ballot_sync(0xffffffffu, pass);
+        if (lane == 0) sm.warp_tot[warp] = __popc(mask);
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+#pragma unroll
+        for (int w = 0; w < kBinWarps; ++w) {
+            const uint32_t t = sm.warp_tot[w];
+            before += (uint32_t(w) < warp) ? t : 0u;
+            total += t;
+        }
+        if (pass) sm.col[col_len + before + __popc(mask & lanemask_lt())] = i;
+        col_len += total;
+        base += kBinThreads;
+        __syncthreads();
+    }
+    return col_len;
+}
+
+// Tests a gathered round against every slice box of the column: counts into
+// sm.slice_run, and with FILL writes the lists from sm.slice_dst.
+template <bool FILL>
+__device__ __forceinline__ void test_slices(FusedSmem& fs, const ColumnGeom& g, const BinLight* __restrict__ bl,
+                                            const hl_froxel_params& p, const float* __restrict__ tabz, float zlast,
+                                            uint32_t col_len, uint32_t* __restrict__ indices, uint32_t capacity) {
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (uint32_t s = warp; s < p.grid_z; s += kBinWarps) {
+        const float z0 = tabz[s];
+        const float z1 = (s + 1 == p.grid_z) ? zlast : tabz[s + 1];
+        const Box b = froxel_box(g, z0, z1);
+        uint32_t run = fs.b.slice_run[s];
+        const uint32_t dst0 = FILL ? fs.slice_dst[s] : 0u;
+        for (uint32_t j0 = 0; j0 < col_len; j0 += 32) {
+            const uint32_t j = j0 + lane;
+            bool pass = false;
+            uint32_t li = 0;
+            if (j < col_len) {
+                li = fs.b.col[j];
+                pass = light_meets_froxel(bl[li], b);
+            }
+            const uint32_t mask = __ballot_sync(0xffffffffu, pass);
+            if (FILL && pass) {
+                const uint64_t dst = uint64_t(dst0) + run + __popc(mask & lanemask_lt());
+                if (dst < capacity) indices[dst] = li;
+            }
+            run += __popc(mask);
+        }
+        if (lane == 0) fs.b.slice_run[s] = run;
+    }
+}
+
+__global__ void __launch_bounds__(kBinThreads) bin_froxels_fused_kernel(
+    const GpuCamera* __restrict__ cam, const BinLight* __restrict__ bl, uint32_t n, hl_froxel_params p,
+    const __grid_constant__ SliceTable tab, uint32_t* __restrict__ offsets, uint32_t* __restrict__ indices,
+    uint32_t capacity, int* __restrict__ status, unsigned long long* __restrict__ chain,
+    BinChainState* __restrict__ state) {
+    __shared__ FusedSmem fs;
+    __shared__ uint32_t s_epoch;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t cols = p.grid_x * p.grid_y;
+    if (threadIdx.x == 0) {
+        // every CTA of the previous launch has finished before this one starts (stream
+        // order), so base and epoch are that launch's final values
+        const unsigned long long base = *reinterpret_cast<volatile unsigned long long*>(&state->base);
+        s_epoch = *reinterpret_cast<volatile uint32_t*>(&state->epoch) + 1u;
+        fs.col = uint32_t(atomicAdd(&state->ticket, 1ull) - base);
+    }
+    __syncthreads();
+    const uint32_t col = fs.col, epoch = s_epoch;
+    if (col >= cols) {  // launches overlapping on one context: refused
+        if (threadIdx.x == 0) raise_status(status, HL_ERR_DEVICE_BOUNDS);
+        return;
+    }
+    const ColumnGeom g = column_geom(cam, p, col % p.grid_x, col / p.grid_x);
+    const float zlast = xmax(tab.z[p.grid_z], cam->forward_far[3]);
+    for (uint32_t s = threadIdx.x; s < p.grid_z; s += blockDim.x) fs.b.slice_run[s] = 0;
+
+    // ---- 1. count ----
+    uint32_t base = 0, col_len = 0;
+    bool one_round = true;
+    for (bool first = true;; first = false) {
+        col_len = gather_round(fs.b, g, bl, n, base);
+        if (!first) one_round = false;
+        test_slices<false>(fs, g, bl, p, tab.z, zlast, col_len, indices, capacity);
+        if (base >= n) break;
+    }
+    __syncthreads();
+
+    // ---- 2. chained scan over columns ----
+    if (warp == 0) {
+        if (lane == 0) {
+            uint32_t acc = 0;
+            for (uint32_t s = 0; s < p.grid_z; ++s) {
+                fs.slice_dst[s] = acc;
+                acc += fs.b.slice_run[s];
+            }
+            fs.total = acc;
+            st_chain(chain + col, epoch, col == 0 ? kFlagPrefix : kFlagAggregate, acc);
+        }
+        __syncwarp();
+        uint32_t excl = 0;
+        int32_t pred = int32_t(col) - 1;
+        uint32_t spins = 0;
+        while (pred >= 0) {
+            const int32_t c = pred - int32_t(lane);
+            uint32_t st = kFlagPrefix, val = 0;  // before column 0: a prefix of 0
+            if (c >= 0) {
+                const unsigned long long w = ld_chain(chain + c);
+                st = uint32_t(w >> 32) == epoch ? (uint32_t(w) >> 30) : 0u;
+                val = uint32_t(w) & kChainValueMax;
+            }
+            const uint32_t pm = __ballot_sync(0xffffffffu, st == kFlagPrefix);
+            const int stop = pm ? __ffs(pm) - 1 : 31;  // lanes 0..stop are summed
+            const uint32_t upto = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
+            if (__ballot_sync(0xffffffffu, st == 0u) & upto) {
+                if (++spins > kLookbackSpins) {
+                    if (lane == 0) raise_status(status, HL_ERR_TIMEOUT);
+                    break;
+                }
+                __nanosleep(64);
+                continue;
+            }
+            excl += __reduce_add_sync(0xffffffffu, uint32_t(lane) <= uint32_t(stop) ? val : 0u);
+            if (pm) break;
+            pred -= 32;
+        }
+        if (lane == 0) {
+            if (col > 0) st_chain(chain + col, epoch, kFlagPrefix, excl + fs.total);
+            fs.excl = excl;
+            if (uint64_t(excl) + fs.total > capacity) raise_status(status, HL_ERR_CAPACITY);
+            if (uint64_t(excl) + fs.total > kChainValueMax) raise_status(status, HL_ERR_SIZE);
+        }
+    }
+    __syncthreads();
+    const uint32_t excl = fs.excl;
+    for (uint32_t s = threadIdx.x; s < p.grid_z; s += blockDim.x) {
+        fs.slice_dst[s] += excl;
+        offsets[col * p.grid_z + s] = fs.slice_dst[s];
+        fs.b.slice_run[s] = 0;
+    }
+    if (col == cols - 1 && threadIdx.x == 0) offsets[cols * p.grid_z] = excl + fs.total;
+    __syncthreads();
+
+    // ---- 3. fill (from the round still in shared memory when there was only one) ----
+    if (one_round) {
+        test_slices<true>(fs, g, bl, p, tab.z, zlast, col_len, indices, capacity);
+    } else {
+        base = 0;
+        for (;;) {
+            col_len = gather_round(fs.b, g, bl, n, base);
+            test_slices<true>(fs, g, bl, p, tab.z, zlast, col_len, indices, capacity);
+            if (base >= n) break;
+        }
+    }
+    // the last CTA to finish advances the ticket base and the epoch for the next launch
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&state->done, 1u) == cols - 1u) {
+            state->done = 0u;
+            state->base += cols;
+            state->epoch = epoch;
+            __threadfence();
+        }
+    }
+}
+
 // Exclusive scan of counts[F] into offsets[F+1] by one CTA of 1024 threads.
 __device__ __forceinline__ void scan_counts(const uint32_t* __restrict__ counts, uint32_t F,
                                             uint32_t* __restrict__ offsets, uint32_t* s_warp) {
@@ -470,6 +680,16 @@ cudaError_t launch_bin_froxels_batched(const BinViewDesc* descs, uint32_t n_view
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     bin_froxels_batched_kernel<true><<<total_columns, kBinThreads, 0, stream>>>(descs, n_views, n, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bin_froxels_fused(const void* camera, const BinLight* bl, uint32_t n, const hl_froxel_params& p,
+                                     const SliceTable& tab, uint32_t* offsets, uint32_t* indices, uint32_t capacity,
+                                     int* status, unsigned long long* chain, BinChainState* state,
+                                     cudaStream_t stream) {
+    const uint32_t cols = p.grid_x * p.grid_y;
+    bin_froxels_fused_kernel<<<cols, kBinThreads, 0, stream>>>(static_cast<const GpuCamera*>(camera), bl, n, p, tab,
+                                                               offsets, indices, capacity, status, chain, state);
     return cudaGetLastError();
 }
 

@@ -144,6 +144,14 @@ struct SliceTable {
 };
 constexpr uint32_t kMaxSlices = 128;
 
+// Device-side state of the single-pass froxel binning (zeroed when allocated).
+struct BinChainState {
+    unsigned long long ticket;  // column tickets handed out, over all launches
+    unsigned long long base;    // tickets handed out before the current launch
+    uint32_t epoch;             // epoch of the last finished launch
+    uint32_t done;              // CTAs of the current launch that have finished
+};
+
 // One view of a batch, as the batched froxel binning kernels read it.
 struct BinViewDesc {
     const void* camera;         // GpuCameraUniforms

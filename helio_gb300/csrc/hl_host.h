@@ -19,6 +19,9 @@ struct hl_ctx {
     uint32_t bin_lights_cap = 0;
     uint32_t* froxel_counts = nullptr;
     uint32_t froxel_counts_cap = 0;
+    unsigned long long* froxel_chain = nullptr;  // per-column words of the single-pass binning
+    uint32_t froxel_chain_cap = 0;
+    hl::BinChainState* bin_state = nullptr;      // ticket counter and epoch of the single-pass binning
     float4* shade_cand = nullptr;       // candidate-test light table of hl_shade
     uint32_t shade_cand_cap = 0;
     unsigned char* frag_lights = nullptr;  // light records of hl_shade_fragments

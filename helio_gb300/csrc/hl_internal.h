@@ -53,6 +53,14 @@ struct ShadeViewDesc {
     uint32_t tile_start;   // first CTA of this view in the batched launch
 };
 
+// Single-launch froxel binning (count, chained scan, fill). chain: one word per column
+// and state: both zeroed when allocated; launches sharing them must not overlap.
+struct BinChainState;
+cudaError_t launch_bin_froxels_fused(const void* camera, const BinLight* bl, uint32_t n, const hl_froxel_params& p,
+                                     const SliceTable& tab, uint32_t* offsets, uint32_t* indices, uint32_t capacity,
+                                     int* status, unsigned long long* chain, BinChainState* state,
+                                     cudaStream_t stream);
+
 // Froxel binning of every view of a batch (descs: device array of n_views).
 cudaError_t launch_bin_froxels_batched(const BinViewDesc* descs, uint32_t n_views, uint32_t total_columns,
                                        const void* lights, uint32_t n, int* status, cudaStream_t stream);

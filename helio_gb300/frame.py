@@ -69,3 +69,113 @@ def upload(camera_rec, globals_rec, lights, gbuffer, device="cuda") -> DeviceFra
 
 def upload_workload(w, device="cuda") -> DeviceFrame:
     return upload(w.camera.record, w.globals_, w.lights, w.gbuffer, device)
+
+
+# ----------------------------------------------------------------------------------
+# Frames from host memory, pipelined
+# ----------------------------------------------------------------------------------
+
+
+def _align(n: int, a: int = 256) -> int:
+    return (n + a - 1) // a * a
+
+
+class PackedFrame:
+    """One frame's inputs packed in one pinned host buffer (camera, globals, lights,
+    then each G-buffer plane at 256-byte offsets), so that its upload is one copy."""
+
+    def __init__(self, camera_rec, globals_rec, lights, gbuffer):
+        torch = _torch()
+        parts = [np.ascontiguousarray(camera_rec), np.ascontiguousarray(globals_rec),
+                 np.ascontiguousarray(lights) if len(lights) else np.zeros(1, L.GPU_LIGHT)]
+        parts += [np.ascontiguousarray(p) for p in gbuffer.planes]
+        self.offsets, off = [], 0
+        for a in parts:
+            self.offsets.append(off)
+            off = _align(off + a.nbytes)
+        self.nbytes = off
+        self.host = torch.empty(off, dtype=torch.uint8).pin_memory()
+        h = self.host.numpy()
+        for a, o in zip(parts, self.offsets):
+            h[o:o + a.nbytes] = np.frombuffer(a.tobytes(), np.uint8)
+        self.plane_specs = [(p.dtype, p.shape) for p in gbuffer.planes]
+        self.width, self.height, self.layout = gbuffer.width, gbuffer.height, gbuffer.layout
+        self.n_lights = len(lights)
+
+
+class HostFramePipeline:
+    """Lights frames that live in pinned host memory and returns their radiance to
+    pinned host memory: the upload of frame k+1, the binning and shading of frame k and
+    the download of frame k-1 run on three CUDA streams with two device buffer sets, so
+    copies overlap the kernels. Every frame still makes its own host->device copy of
+    all its inputs and its own device->host copy of its radiance (RGBA32F). Sky pixels
+    (depth 1) come back as zeros: the device targets are cleared once and shading never
+    writes them."""
+
+    def __init__(self, ctx: N.Context, like: PackedFrame, froxel_grid, slice_far, capacity=None, device="cuda"):
+        torch = _torch()
+        self.ctx = ctx
+        self.like = like
+        W, H = like.width, like.height
+        self.fp = N.froxel_params(*froxel_grid, W, H, slice_far)
+        F = froxel_grid[0] * froxel_grid[1] * froxel_grid[2]
+        self.capacity = capacity if capacity is not None else F * max(1, min(like.n_lights, 256))
+        self.slots = []
+        for _ in range(2):
+            buf = torch.empty(like.nbytes, dtype=torch.uint8, device=device)
+            planes = []
+            for (dt, shape), o in zip(like.plane_specs, like.offsets[3:]):
+                n = int(np.prod(shape)) * np.dtype(dt).itemsize
+                t = buf[o:o + n].view(getattr(torch, np.dtype(dt).name)).view(*shape)
+                planes.append(t)
+            slot = {
+                "buf": buf,
+                "camera": buf[like.offsets[0]:],
+                "globals": buf[like.offsets[1]:],
+                "lights": buf[like.offsets[2]:],
+                "gbuffer": N.gbuffer_struct(like.layout, W, H, planes),
+                "planes": planes,
+                "offsets": torch.empty(F + 1, dtype=torch.int32, device=device),
+                "indices": torch.empty(self.capacity, dtype=torch.int32, device=device),
+                # cleared once: sky pixels (depth 1) are never written, as in the reference
+                "target": torch.zeros((H, W, 4), dtype=torch.float32, device=device),
+                "up": torch.cuda.Event(), "done": torch.cuda.Event(), "down": torch.cuda.Event(),
+            }
+            slot["grid"] = N.froxel_grid_struct(slot["indices"], slot["offsets"], self.fp, self.capacity)
+            slot["tgt"] = N.target_struct(slot["target"])
+            self.slots.append(slot)
+        self.s_up, self.s_comp, self.s_down = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
+        self.k = 0
+
+    @property
+    def streams(self):
+        return self.s_up, self.s_comp, self.s_down
+
+    def submit(self, frame: PackedFrame, host_out):
+        """Enqueues one frame; ``host_out`` (pinned, H x W x 4 float32) receives its
+        radiance once the download stream has passed this frame."""
+        torch = _torch()
+        s = self.slots[self.k % 2]
+        first = self.k < 2
+        with torch.cuda.stream(self.s_up):
+            if not first:
+                self.s_up.wait_event(s["done"])  # kernels of frame k-2 are done with the inputs
+            s["buf"].copy_(frame.host, non_blocking=True)
+            s["up"].record(self.s_up)
+        self.s_comp.wait_event(s["up"])
+        if not first:
+            self.s_comp.wait_event(s["down"])  # frame k-2's radiance has been read
+        sh = self.s_comp.cuda_stream
+        n = frame.n_lights
+        self.ctx.bin_froxels(s["camera"], s["lights"], n, self.fp, s["offsets"], s["indices"], self.capacity, sh)
+        self.ctx.shade(s["camera"], s["globals"], s["gbuffer"], s["lights"], n, s["grid"], s["tgt"], sh)
+        s["done"].record(self.s_comp)
+        with torch.cuda.stream(self.s_down):
+            self.s_down.wait_event(s["done"])
+            host_out.copy_(s["target"], non_blocking=True)
+            s["down"].record(self.s_down)
+        self.k += 1
+
+    def synchronize(self):
+        for st in self.streams:
+            st.synchronize()

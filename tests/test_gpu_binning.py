@@ -111,3 +111,55 @@ def test_froxel_lists_large_light_count(ctx):
     off, idx, _ = gpu_bin_froxels(ctx, cam.record, lt, p, capacity=int(off_w[-1]))
     np.testing.assert_array_equal(off, off_w)
     np.testing.assert_array_equal(idx, idx_w)
+
+
+def test_froxel_lists_many_columns(ctx):
+    """32400 columns: far more CTAs than the GPU holds at once, so the single-pass
+    binning's chained scan runs across many waves of CTAs."""
+    W, H = 1920, 1080
+    cam = S.default_camera(W, H)
+    lt = mixed_lights(cam, 12, 300, 100, n_dir=1)
+    p = L.froxel_params(240, 135, 4, W, H, cam.far)
+    off_w, idx_w = oracle.bin_froxels(cam.record, lt, p, capacity=1 << 26)
+    off, idx, _ = gpu_bin_froxels(ctx, cam.record, lt, p, capacity=int(off_w[-1]) + 8)
+    np.testing.assert_array_equal(off, off_w)
+    np.testing.assert_array_equal(idx, idx_w)
+
+
+def test_froxel_binning_replays_in_a_cuda_graph(ctx):
+    """hl_bin_froxels keeps its launch-to-launch state on the device, so a launch
+    recorded in a CUDA graph gives the same lists on every replay, alternating with
+    direct calls on other grids."""
+    import torch
+
+    from helio_gb300 import frame as FR
+
+    w = S.workload(0, 0.5)
+    W, H = w.gbuffer.width, w.gbuffer.height
+    p_np = L.froxel_params(*w.froxel_grid, W, H, w.camera.far)
+    off_w, idx_w = oracle.bin_froxels(w.camera.record, w.lights, p_np, capacity=1 << 24)
+    p = N.froxel_params_from_numpy(p_np)
+    F = p.grid_x * p.grid_y * p.grid_z
+    cam, lt = FR.bytes_tensor(w.camera.record), FR.bytes_tensor(w.lights)
+    cap = int(off_w[-1]) + 64
+    off = torch.zeros(F + 1, dtype=torch.int32, device="cuda")
+    idx = torch.zeros(cap, dtype=torch.int32, device="cuda")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        ctx.bin_froxels(cam, lt, len(w.lights), p, off, idx, cap, s.cuda_stream)  # scratch allocated here
+    s.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        ctx.bin_froxels(cam, lt, len(w.lights), p, off, idx, cap, s.cuda_stream)
+    other = L.froxel_params(5, 3, 7, W, H, w.camera.far)
+    for _ in range(3):
+        off.fill_(-1)
+        idx.fill_(-1)
+        g.replay()
+        torch.cuda.synchronize()
+        ctx.sync_status()
+        np.testing.assert_array_equal(off.cpu().numpy().view(np.uint32), off_w)
+        np.testing.assert_array_equal(idx.cpu().numpy().view(np.uint32)[: off_w[-1]], idx_w)
+        o2, i2, _ = gpu_bin_froxels(ctx, w.camera.record, w.lights, other)  # a direct call in between
+        o2w, i2w = oracle.bin_froxels(w.camera.record, w.lights, other, capacity=1 << 24)
+        np.testing.assert_array_equal(o2, o2w)
