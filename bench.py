@@ -379,7 +379,7 @@ def run_ours(args, world, rank, local):
         line["error_vs_fp64_oracle"] = {k: (round(v, 9) if isinstance(v, float) else v) for k, v in e.items()}
         line["error_vs_fp64_oracle"]["lists_bit_exact"] = bool(np.array_equal(off_g, off_o))
     if rank == 0 and not args.no_forms:
-        line["forms"] = run_forms(ctx, dev, stream, flush)
+        line["forms"] = run_forms(ctx, dev, stream, flush, with_oracle=not args.no_cpu)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -403,7 +403,7 @@ def _median_ms(fn, stream, flush, reps, warm=3):
     return statistics.median(ts)
 
 
-def run_forms(ctx, dev, stream, flush):
+def run_forms(ctx, dev, stream, flush, with_oracle=True):
     """The three other forms of the path, each timed with CUDA events (L2 flushed):
     adjoint (w4), batched views (w3) and the FP16/FP32 G-buffer precision pair."""
     import torch
@@ -447,13 +447,35 @@ def run_forms(ctx, dev, stream, flush):
     first = d_l.clone()
     adj()
     torch.cuda.synchronize()
+    hbm_peak, _ = measured_peaks()
+    # algorithmic bytes of the adjoint: FP32 G-buffer read, dL/dradiance read, pixel gradients written
+    adj_bytes = W * H * (w.gbuffer.bytes_per_pixel + 16 + 20)
     forms["adjoint"] = {
         "workload": "w4: 1920x1080 FP32 G-buffer, 256 point lights, froxels 16x9x24",
         "fwd_ms": round(t_f, 4), "adjoint_ms": round(t_a, 4),
         "fwd_plus_adjoint_over_fwd": round((t_f + t_a) / t_f, 3),
         "fwd_plus_adjoint_mpix_s": round(W * H / ((t_f + t_a) / 1e3) / 1e6, 1),
         "deterministic": bool(torch.equal(first, d_l)),
+        "adjoint_hbm_frac": round(adj_bytes / (t_a / 1e3) / 1e9 / hbm_peak, 4),
     }
+    if with_oracle:
+        import oracle
+
+        p_np = L.froxel_params(*w.froxel_grid, W, H, w.camera.far)
+        off_h = off.cpu().numpy().view(np.uint32)
+        idx_h = idx.cpu().numpy().view(np.uint32)[: int(off_h[-1])]
+        o_l, o_p = oracle.shade_adjoint(w.camera.record, w.globals_, w.gbuffer, w.lights, ("froxels", idx_h, off_h, p_np),
+                                        d_rad.double().cpu().numpy())
+        g_l, g_p = d_l.cpu().numpy(), d_p.double().cpu().numpy()
+        sky = ~(w.gbuffer.planes[-1] < 1.0)
+        rel_l = (np.abs(g_l - o_l).max(0) / np.maximum(np.abs(o_l).max(0), 1e-30)).max()
+        ps = np.abs(o_p[~sky]).max(0)
+        rel_p = (np.abs(g_p[~sky] - o_p[~sky]) / (np.abs(o_p[~sky]) + 1e-3 * ps)).max(1)
+        forms["adjoint"]["error_vs_fp64_oracle"] = {
+            "light_grad_max_over_scale": float(f"{rel_l:.3e}"),
+            "pixel_grad_p9999": float(f"{np.quantile(rel_p, 0.9999):.3e}"),
+            "pixel_grad_max": float(f"{rel_p.max():.3e}"),
+        }
     del df, off, idx, rad, d_rad, d_l, d_p
 
     # ---- batched: w3, 96 cube faces + 1080p + 720p, 2048 lights ----
@@ -491,13 +513,33 @@ def run_forms(ctx, dev, stream, flush):
     t_v = _median_ms(per_view, stream, flush, 10)
     ctx.sync_status(sh)
     px = sum(f.width * f.height for f in frames)
+    plan.execute(sh)  # the plan's own radiance for the error check
+    torch.cuda.synchronize()
+    ctx.sync_status(sh)
+    batch_err = None
+    if with_oracle:
+        import oracle
+        from helio_gb300 import metrics
+
+        batch_err = {}
+        for vi in (0, 40, 97):  # a 128^2 face, a 512^2 face, the 1280x720 viewport
+            f, p, o, ix, c, _ = per[vi]
+            off_h = o.cpu().numpy().view(np.uint32)
+            idx_h = ix.cpu().numpy().view(np.uint32)[: int(off_h[-1])]
+            pn = L.froxel_params(p.grid_x, p.grid_y, p.grid_z, p.width, p.height, p.slice_far, p.slice_near)
+            ref = oracle.shade(views[vi].camera.record, glb, views[vi].gbuffer, lights, ("froxels", idx_h, off_h, pn))
+            e = metrics.radiance_error(outs[vi].cpu().numpy().astype(np.float64), ref)
+            batch_err[f"view{vi}_{f.width}x{f.height}"] = {"max": float(f"{e['max']:.3e}"),
+                                                          "p9999": float(f"{e['p9999']:.3e}")}
     forms["batched"] = {
         "workload": "w3: 16 probes x 6 cube faces (128^2/256^2/512^2) + 1920x1080 + 1280x720, FP16 G-buffers, "
                     "2048 lights",
         "views": len(frames), "pixels": px, "batched_ms": round(t_b, 4), "per_view_launches_ms": round(t_v, 4),
         "speedup": round(t_v / t_b, 2), "batched_mpix_s": round(px / (t_b / 1e3) / 1e6, 1),
-        "launches": {"batched": 6, "per_view": 6 * len(frames)}, "autotune_s": round(tune_s, 2),
+        "launches": {"batched": 6, "per_view": 4 * len(frames)}, "autotune_s": round(tune_s, 2),
         "grids": sorted({(f.width, f.height) + plan.view_grid(i) for i, f in enumerate(frames)}),
+        "hbm_frac": round(px * (18 + 16) / (t_b / 1e3) / 1e9 / measured_peaks()[0], 4),
+        "error_vs_fp64_oracle": batch_err,
     }
     plan.close()
     return forms
