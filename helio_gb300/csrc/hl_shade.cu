@@ -37,10 +37,13 @@ constexpr int kBins = 512;       // froxel keys of the pixel sort
 constexpr int kPipe = 4;         // list entries in flight per lane
 constexpr int kBoxMin = 8;       // shortest shared list worth a box cull
 
-// Pixel record fields (structure of arrays).
+// Pixel record fields (structure of arrays). N, V and the fast path's guard are not
+// stored: they are recomputed from these with the set-up's own operations, so the
+// record fits three CTAs per SM.
 enum Field : int {
-    F_PX, F_PY, F_PZ, F_PLX, F_PLY, F_PLZ, F_NX, F_NY, F_NZ, F_VX, F_VY, F_VZ, F_NDV, F_AR, F_AG, F_AB, F_ROUGH,
-    F_METAL, F_F0R, F_F0G, F_F0B, F_GV, F_GUARD, F_DEPTH, F_NRX, F_NRY, F_NRZ, F_INVN, F_COUNT
+    F_PX, F_PY, F_PZ, F_PLX, F_PLY, F_PLZ, F_NDV, F_AR, F_AG, F_AB, F_ROUGH, F_METAL, F_F0R, F_F0G, F_F0B, F_GV,
+    F_DEPTH,  // negative: the pixel was set up on the precise path (its guard is 0)
+    F_NRX, F_NRY, F_NRZ, F_INVN, F_COUNT
 };
 
 template <int NPX>
@@ -65,25 +68,57 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 }
 
 template <int NPX>
-__device__ __forceinline__ void store_pixel(Smem<NPX>& s, int i, const Pixel& p, const PixelBrdf& b, float guard,
+__device__ __forceinline__ void store_pixel(Smem<NPX>& s, int i, const Pixel& p, const PixelBrdf& b, bool precise,
                                             float depth, float ar, float ag, float ab) {
     s.px[F_PX][i] = p.Px; s.px[F_PY][i] = p.Py; s.px[F_PZ][i] = p.Pz;
     s.px[F_PLX][i] = p.Plx; s.px[F_PLY][i] = p.Ply; s.px[F_PLZ][i] = p.Plz;
-    s.px[F_NX][i] = p.Nx; s.px[F_NY][i] = p.Ny; s.px[F_NZ][i] = p.Nz;
-    s.px[F_VX][i] = p.Vx; s.px[F_VY][i] = p.Vy; s.px[F_VZ][i] = p.Vz; s.px[F_NDV][i] = p.NdV;
+    s.px[F_NDV][i] = p.NdV;
     s.px[F_AR][i] = ar; s.px[F_AG][i] = ag; s.px[F_AB][i] = ab;
     s.px[F_ROUGH][i] = p.rough; s.px[F_METAL][i] = p.metal;
     s.px[F_F0R][i] = p.f0r; s.px[F_F0G][i] = p.f0g; s.px[F_F0B][i] = p.f0b;
-    s.px[F_GV][i] = b.gv; s.px[F_GUARD][i] = guard; s.px[F_DEPTH][i] = depth;
+    s.px[F_GV][i] = b.gv; s.px[F_DEPTH][i] = precise ? -depth : depth;
     s.px[F_NRX][i] = p.nrx; s.px[F_NRY][i] = p.nry; s.px[F_NRZ][i] = p.nrz; s.px[F_INVN][i] = p.inv_n;
 }
 
+// The unit normal finish_pixel computed: the stored raw normal times its 1/|n|.
 template <int NPX>
-__device__ __forceinline__ void load_pixel(const Smem<NPX>& s, int i, Pixel& p, PixelBrdf& b) {
+__device__ __forceinline__ void pixel_normal(const Smem<NPX>& s, int i, float& nx, float& ny, float& nz) {
+    const float in = s.px[F_INVN][i];
+    nx = s.px[F_NRX][i] * in;
+    ny = s.px[F_NRY][i] * in;
+    nz = s.px[F_NRZ][i] * in;
+}
+
+// V as finish_pixel computed it: from the camera-relative position on the fast path
+// (camera at the origin; lo is 0 unless the pixel was set up precisely), from the
+// double-float difference to the camera otherwise.
+template <bool PRECISE>
+__device__ __forceinline__ void pixel_view(Pixel& p, float camx, float camy, float camz) {
+    float vx, vy, vz;
+    if (PRECISE) {
+        const DF ux = two_sum(camx, -p.Px), uy = two_sum(camy, -p.Py), uz = two_sum(camz, -p.Pz);
+        vx = two_sum(ux.hi, ux.lo - p.Plx).hi;
+        vy = two_sum(uy.hi, uy.lo - p.Ply).hi;
+        vz = two_sum(uz.hi, uz.lo - p.Plz).hi;
+    } else {
+        vx = -p.Px - p.Plx;
+        vy = -p.Py - p.Ply;
+        vz = -p.Pz - p.Plz;
+    }
+    const float iv = rsqrt_(fma_(vz, vz, fma_(vy, vy, vx * vx)));
+    p.Vx = vx * iv;
+    p.Vy = vy * iv;
+    p.Vz = vz * iv;
+}
+
+template <bool PRECISE, int NPX>
+__device__ __forceinline__ void load_pixel(const Smem<NPX>& s, int i, Pixel& p, PixelBrdf& b, float camx, float camy,
+                                           float camz) {
     p.Px = s.px[F_PX][i]; p.Py = s.px[F_PY][i]; p.Pz = s.px[F_PZ][i];
     p.Plx = s.px[F_PLX][i]; p.Ply = s.px[F_PLY][i]; p.Plz = s.px[F_PLZ][i];
-    p.Nx = s.px[F_NX][i]; p.Ny = s.px[F_NY][i]; p.Nz = s.px[F_NZ][i];
-    p.Vx = s.px[F_VX][i]; p.Vy = s.px[F_VY][i]; p.Vz = s.px[F_VZ][i]; p.NdV = s.px[F_NDV][i];
+    pixel_normal(s, i, p.Nx, p.Ny, p.Nz);
+    pixel_view<PRECISE>(p, camx, camy, camz);
+    p.NdV = s.px[F_NDV][i];
     p.dr = s.px[F_AR][i] * kInvPi; p.dg = s.px[F_AG][i] * kInvPi; p.db = s.px[F_AB][i] * kInvPi;
     p.rough = s.px[F_ROUGH][i]; p.metal = s.px[F_METAL][i];
     p.f0r = s.px[F_F0R][i]; p.f0g = s.px[F_F0G][i]; p.f0b = s.px[F_F0B][i];
@@ -139,7 +174,7 @@ __device__ __noinline__ void flush_batch(sk::Smem<NPX>& s, const uint32_t* queue
     if (act) {
         Pixel p;
         PixelBrdf pb;
-        load_pixel(s, q, p, pb);
+        load_pixel<PRECISE>(s, q, p, pb, cam->position_near[0], cam->position_near[1], cam->position_near[2]);
         const float4* gl = reinterpret_cast<const float4*>(lights + li);
         const float4 a = __ldg(gl + 0), b = __ldg(gl + 1), c = __ldg(gl + 2);
         const uint4 d = __ldg(reinterpret_cast<const uint4*>(gl + 3));
@@ -157,9 +192,10 @@ __device__ __noinline__ void flush_batch(sk::Smem<NPX>& s, const uint32_t* queue
         }
         l.px = ux.hi; l.py = uy.hi; l.pz = uz.hi;
         if (STATS) rng = in_range(p, l);
-        st = eval<PRECISE>(p, pb, l, cr, cg, cb, PRECISE ? 0.0f : s.px[F_GUARD][q]);
+        const float dq = s.px[F_DEPTH][q];
+        st = eval<PRECISE>(p, pb, l, cr, cg, cb, (PRECISE || dq < 0.0f) ? 0.0f : fast_guard(p));
         if (!PRECISE && st == kNeedsPrecise)
-            st = precise_pair(cam, x0 + q % TW, y0 + q / TW, W, H, s.px[F_DEPTH][q], p, s.px[F_AR][q], s.px[F_AG][q],
+            st = precise_pair(cam, x0 + q % TW, y0 + q / TW, W, H, dq, p, s.px[F_AR][q], s.px[F_AG][q],
                               s.px[F_AB][q], l, ux.lo, uy.lo, uz.lo, cr, cg, cb);
     }
     const bool lit = act && st == kLit;
@@ -270,7 +306,7 @@ __device__ __forceinline__ void shade_tile(
             valid[k] = tx.depth < 1.0f;
             if (valid[k]) {
                 Pixel p;
-                float guard = 0.0f;
+                bool precise_setup = PRECISE;
                 if (PRECISE) {
                     reconstruct<true>(cam->inv_view_proj, x, y, W, H, tx.depth, p.Px, p.Py, p.Pz, p.Plx, p.Ply, p.Plz);
                     finish_pixel<true>(p, tx.nx, tx.ny, tx.nz, tx.ar, tx.ag, tx.ab, tx.rough, tx.metal, tx.f0r, tx.f0g,
@@ -282,7 +318,6 @@ __device__ __forceinline__ void shade_tile(
                     p.Plx = p.Ply = p.Plz = 0.0f;
                     finish_pixel<false>(p, tx.nx, tx.ny, tx.nz, tx.ar, tx.ag, tx.ab, tx.rough, tx.metal, tx.f0r,
                                         tx.f0g, tx.f0b, 0.0f, 0.0f, 0.0f);
-                    guard = fast_guard(p);
                     if (p.NdV < kFastMinNdV) {
                         // grazing view: precise set-up, camera-relative double-float position
                         reconstruct<true>(cam->inv_view_proj, x, y, W, H, tx.depth, p.Px, p.Py, p.Pz, p.Plx, p.Ply,
@@ -293,10 +328,10 @@ __device__ __forceinline__ void shade_tile(
                         p.Px = bx.hi; p.Plx = bx.lo; p.Py = by.hi; p.Ply = by.lo; p.Pz = bz.hi; p.Plz = bz.lo;
                         finish_pixel<true>(p, tx.nx, tx.ny, tx.nz, tx.ar, tx.ag, tx.ab, tx.rough, tx.metal, tx.f0r,
                                            tx.f0g, tx.f0b, 0.0f, 0.0f, 0.0f);
-                        guard = 0.0f;
+                        precise_setup = true;
                     }
                 }
-                store_pixel(s, i, p, pixel_brdf(p), guard, tx.depth, tx.ar, tx.ag, tx.ab);
+                store_pixel(s, i, p, pixel_brdf(p), precise_setup, tx.depth, tx.ar, tx.ag, tx.ab);
                 uint32_t b = tile_base, n = tile_len;
                 if (FROXELS) {
                     // own froxel: column of (x, y), slice of the linear view depth
@@ -387,7 +422,7 @@ __device__ __forceinline__ void shade_tile(
         if (own) {
             px = s.px[F_PX][i]; py = s.px[F_PY][i]; pz = s.px[F_PZ][i];
             plx = s.px[F_PLX][i]; ply = s.px[F_PLY][i]; plz = s.px[F_PLZ][i];
-            nx = s.px[F_NX][i]; ny = s.px[F_NY][i]; nz = s.px[F_NZ][i];
+            pixel_normal(s, i, nx, ny, nz);
             // |N.t| within |P| 2^-20 of zero is left to the exact NdL cut
             slack = fma_(pz, pz, fma_(py, py, px * px)) * (1.0f / 1099511627776.0f);
             lb = s.base[i];
@@ -520,7 +555,8 @@ __device__ __forceinline__ void shade_tile(
             tx.alpha = 1.0f;
             tx.er = tx.eg = tx.eb = 0.0f;
         }
-        const float ny = s.px[F_NY][i];
+        float nxo, ny, nzo;
+        pixel_normal(s, i, nxo, ny, nzo);
         const float amb = glb->ambient_intensity;
         const float skr = glb->ambient_color[0] * amb, skg = glb->ambient_color[1] * amb,
                     skb = glb->ambient_color[2] * amb;
@@ -537,7 +573,7 @@ __device__ __forceinline__ void shade_tile(
         if (debug_mode == 1u || debug_mode == 2u || debug_mode == 4u || debug_mode == 20u || debug_mode == 21u) {
             c = make_float4(tx.ar, tx.ag, tx.ab, tx.alpha);
         } else if (debug_mode == 5u) {
-            c = make_float4(fma_(s.px[F_NX][i], 0.5f, 0.5f), fma_(ny, 0.5f, 0.5f), fma_(s.px[F_NZ][i], 0.5f, 0.5f),
+            c = make_float4(fma_(nxo, 0.5f, 0.5f), fma_(ny, 0.5f, 0.5f), fma_(nzo, 0.5f, 0.5f),
                             1.0f);
         }
         unsigned char* row = out.data + out.pitch * y;
@@ -554,7 +590,7 @@ __device__ __forceinline__ void shade_tile(
 }
 
 template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, int TW, int TH>
-__global__ void __launch_bounds__(sk::kThreads, 2) shade_kernel(
+__global__ void __launch_bounds__(sk::kThreads, 3) shade_kernel(
     const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const GBufView gb,
     const GpuLight* __restrict__ lights, uint32_t n_lights, const GridView grid, const __grid_constant__ SliceTable tab,
     const TargetView out, uint32_t* __restrict__ stats, int* __restrict__ status, const float4* __restrict__ cand) {
@@ -565,7 +601,7 @@ __global__ void __launch_bounds__(sk::kThreads, 2) shade_kernel(
 // Every tile of every view of a batch (froxel grids, 32x16 tiles): CTA b lights tile
 // b - tile_start of the view whose [tile_start, next tile_start) holds b.
 template <uint32_t LAYOUT, uint32_t TARGET>
-__global__ void __launch_bounds__(sk::kThreads, 2) shade_batched_kernel(
+__global__ void __launch_bounds__(sk::kThreads, 3) shade_batched_kernel(
     const ShadeViewDesc* __restrict__ d, uint32_t n_views, const DeferredGlobals* __restrict__ glb,
     const GpuLight* __restrict__ lights, uint32_t n_lights, int* __restrict__ status) {
     uint32_t lo = 0, hi = n_views;
