@@ -34,21 +34,27 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kQueue = 256;      // per-warp pair ring (up to 31 + kPipe * 32 pending)
 constexpr int kBins = 512;       // froxel keys of the pixel sort
-constexpr int kPipe = 4;         // list entries in flight per lane
+constexpr int kPipe = 4;         // list entries in flight per lane (fast path; 2 on the precise path)
 constexpr int kBoxMin = 8;       // shortest shared list worth a box cull
 
-// Pixel record fields (structure of arrays). N, V and the fast path's guard are not
-// stored: they are recomputed from these with the set-up's own operations, so the
-// record fits three CTAs per SM.
+// Pixel record fields (structure of arrays). N, 1/|n|, V, F0 (except for the reference
+// layout, which stores its own), the view's Schlick-GGX term and the fast path's guard
+// are not stored: they are recomputed from these with the set-up's own operations, so a
+// record of 16 fields (19 for the reference layout) keeps three CTAs on an SM.
 enum Field : int {
-    F_PX, F_PY, F_PZ, F_PLX, F_PLY, F_PLZ, F_NDV, F_AR, F_AG, F_AB, F_ROUGH, F_METAL, F_F0R, F_F0G, F_F0B, F_GV,
+    F_PX, F_PY, F_PZ, F_PLX, F_PLY, F_PLZ, F_NDV, F_AR, F_AG, F_AB, F_ROUGH, F_METAL,
     F_DEPTH,  // negative: the pixel was set up on the precise path (its guard is 0)
-    F_NRX, F_NRY, F_NRZ, F_INVN, F_COUNT
+    F_NRX, F_NRY, F_NRZ,
+    F_F0R, F_F0G, F_F0B,  // reference layout only
+    F_COUNT
 };
 
-template <int NPX>
+template <uint32_t LAYOUT>
+__host__ __device__ constexpr int record_fields() { return LAYOUT == HL_GBUF_REFERENCE ? int(F_COUNT) : int(F_F0R); }
+
+template <int NPX, int NF>
 struct Smem {
-    float px[F_COUNT][NPX];
+    float px[NF][NPX];
     float acc[6][NPX];              // Kahan (sum, compensation) x RGB; statistics reuse it
     uint32_t base[NPX], len[NPX];   // each pixel's light list
     uint32_t hist[kBins];
@@ -67,26 +73,30 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
-template <int NPX>
-__device__ __forceinline__ void store_pixel(Smem<NPX>& s, int i, const Pixel& p, const PixelBrdf& b, bool precise,
-                                            float depth, float ar, float ag, float ab) {
+template <int NPX, int NF>
+__device__ __forceinline__ void store_pixel(Smem<NPX, NF>& s, int i, const Pixel& p, bool precise, float depth,
+                                            float ar, float ag, float ab) {
     s.px[F_PX][i] = p.Px; s.px[F_PY][i] = p.Py; s.px[F_PZ][i] = p.Pz;
     s.px[F_PLX][i] = p.Plx; s.px[F_PLY][i] = p.Ply; s.px[F_PLZ][i] = p.Plz;
     s.px[F_NDV][i] = p.NdV;
     s.px[F_AR][i] = ar; s.px[F_AG][i] = ag; s.px[F_AB][i] = ab;
     s.px[F_ROUGH][i] = p.rough; s.px[F_METAL][i] = p.metal;
-    s.px[F_F0R][i] = p.f0r; s.px[F_F0G][i] = p.f0g; s.px[F_F0B][i] = p.f0b;
-    s.px[F_GV][i] = b.gv; s.px[F_DEPTH][i] = precise ? -depth : depth;
-    s.px[F_NRX][i] = p.nrx; s.px[F_NRY][i] = p.nry; s.px[F_NRZ][i] = p.nrz; s.px[F_INVN][i] = p.inv_n;
+    s.px[F_DEPTH][i] = precise ? -depth : depth;
+    s.px[F_NRX][i] = p.nrx; s.px[F_NRY][i] = p.nry; s.px[F_NRZ][i] = p.nrz;
+    if (NF > int(F_F0R)) {
+        s.px[F_F0R][i] = p.f0r; s.px[F_F0G][i] = p.f0g; s.px[F_F0B][i] = p.f0b;
+    }
 }
 
-// The unit normal finish_pixel computed: the stored raw normal times its 1/|n|.
-template <int NPX>
-__device__ __forceinline__ void pixel_normal(const Smem<NPX>& s, int i, float& nx, float& ny, float& nz) {
-    const float in = s.px[F_INVN][i];
-    nx = s.px[F_NRX][i] * in;
-    ny = s.px[F_NRY][i] * in;
-    nz = s.px[F_NRZ][i] * in;
+// The unit normal finish_pixel computed, from the stored raw normal.
+template <int NPX, int NF>
+__device__ __forceinline__ void pixel_normal(const Smem<NPX, NF>& s, int i, float& nx, float& ny, float& nz,
+                                             float& in) {
+    const float rx = s.px[F_NRX][i], ry = s.px[F_NRY][i], rz = s.px[F_NRZ][i];
+    in = rsqrt_(fma_(rz, rz, fma_(ry, ry, rx * rx)));
+    nx = rx * in;
+    ny = ry * in;
+    nz = rz * in;
 }
 
 // V as finish_pixel computed it: from the camera-relative position on the fast path
@@ -111,26 +121,27 @@ __device__ __forceinline__ void pixel_view(Pixel& p, float camx, float camy, flo
     p.Vz = vz * iv;
 }
 
-template <bool PRECISE, int NPX>
-__device__ __forceinline__ void load_pixel(const Smem<NPX>& s, int i, Pixel& p, PixelBrdf& b, float camx, float camy,
-                                           float camz) {
+template <uint32_t LAYOUT, int NPX, int NF>
+__device__ __forceinline__ void load_pixel(const Smem<NPX, NF>& s, int i, Pixel& p, PixelBrdf& b, float camx,
+                                           float camy, float camz) {
+    constexpr bool PRECISE = (LAYOUT != HL_GBUF_F16);
     p.Px = s.px[F_PX][i]; p.Py = s.px[F_PY][i]; p.Pz = s.px[F_PZ][i];
     p.Plx = s.px[F_PLX][i]; p.Ply = s.px[F_PLY][i]; p.Plz = s.px[F_PLZ][i];
-    pixel_normal(s, i, p.Nx, p.Ny, p.Nz);
+    p.nrx = s.px[F_NRX][i]; p.nry = s.px[F_NRY][i]; p.nrz = s.px[F_NRZ][i];
+    pixel_normal(s, i, p.Nx, p.Ny, p.Nz, p.inv_n);
     pixel_view<PRECISE>(p, camx, camy, camz);
     p.NdV = s.px[F_NDV][i];
-    p.dr = s.px[F_AR][i] * kInvPi; p.dg = s.px[F_AG][i] * kInvPi; p.db = s.px[F_AB][i] * kInvPi;
+    const float ar = s.px[F_AR][i], ag = s.px[F_AG][i], ab = s.px[F_AB][i];
+    p.dr = ar * kInvPi; p.dg = ag * kInvPi; p.db = ab * kInvPi;
     p.rough = s.px[F_ROUGH][i]; p.metal = s.px[F_METAL][i];
-    p.f0r = s.px[F_F0R][i]; p.f0g = s.px[F_F0G][i]; p.f0b = s.px[F_F0B][i];
-    p.nrx = s.px[F_NRX][i]; p.nry = s.px[F_NRY][i]; p.nrz = s.px[F_NRZ][i]; p.inv_n = s.px[F_INVN][i];
-    const float a = p.rough * p.rough;  // pixel_brdf, with the view's Schlick-GGX stored
-    b.a2 = a * a;
-    const float r1 = p.rough + 1.0f;
-    b.k = (r1 * r1) * 0.125f;
-    b.omk = 1.0f - b.k;
-    b.gv = s.px[F_GV][i];
-    b.one_m_metal = 1.0f - p.metal;
-    b.nv4 = 4.0f * p.NdV;
+    if (NF > int(F_F0R)) {
+        p.f0r = s.px[F_F0R][i]; p.f0g = s.px[F_F0G][i]; p.f0b = s.px[F_F0B][i];
+    } else {  // the metallic workflow's F0, clamped as finish_pixel clamps it
+        p.f0r = fmin_(fmax_(metallic_f0(ar, p.metal), 0.0f), 0.999f);
+        p.f0g = fmin_(fmax_(metallic_f0(ag, p.metal), 0.0f), 0.999f);
+        p.f0b = fmin_(fmax_(metallic_f0(ab, p.metal), 0.0f), 0.999f);
+    }
+    b = pixel_brdf(p);
 }
 
 }  // namespace sk
@@ -159,7 +170,7 @@ __device__ __noinline__ int precise_pair(const GpuCamera* cam, uint32_t x, uint3
 // them into the per-pixel Kahan accumulators in queue order. Out of line so that the
 // BRDF code exists once in the kernel.
 template <uint32_t LAYOUT, bool STATS, int TW, int NPX>
-__device__ __noinline__ void flush_batch(sk::Smem<NPX>& s, const uint32_t* queue, uint32_t head, uint32_t nb,
+__device__ __noinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>()>& s, const uint32_t* queue, uint32_t head, uint32_t nb,
                                          uint32_t lane, const GpuCamera* cam, const GpuLight* lights, uint32_t x0,
                                          uint32_t y0, float W, float H) {
     using namespace sk;
@@ -174,7 +185,7 @@ __device__ __noinline__ void flush_batch(sk::Smem<NPX>& s, const uint32_t* queue
     if (act) {
         Pixel p;
         PixelBrdf pb;
-        load_pixel<PRECISE>(s, q, p, pb, cam->position_near[0], cam->position_near[1], cam->position_near[2]);
+        load_pixel<LAYOUT>(s, q, p, pb, cam->position_near[0], cam->position_near[1], cam->position_near[2]);
         const float4* gl = reinterpret_cast<const float4*>(lights + li);
         const float4 a = __ldg(gl + 0), b = __ldg(gl + 1), c = __ldg(gl + 2);
         const uint4 d = __ldg(reinterpret_cast<const uint4*>(gl + 3));
@@ -237,7 +248,8 @@ __device__ __forceinline__ void shade_tile(
     static_assert(TW <= 32 && TH <= 16 && TW + TH <= kThreads, "column / row tables of the tile");
     constexpr bool PRECISE = (LAYOUT != HL_GBUF_F16);
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    Smem<NPX>& s = *reinterpret_cast<Smem<NPX>*>(smem_raw);
+    constexpr int NF = record_fields<LAYOUT>();
+    Smem<NPX, NF>& s = *reinterpret_cast<Smem<NPX, NF>*>(smem_raw);
     uint32_t (*cnt)[NPX] = reinterpret_cast<uint32_t (*)[NPX]>(s.acc);  // statistics view
     const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const uint32_t x0 = bx * TW, y0 = by * TH;
@@ -331,7 +343,7 @@ __device__ __forceinline__ void shade_tile(
                         precise_setup = true;
                     }
                 }
-                store_pixel(s, i, p, pixel_brdf(p), precise_setup, tx.depth, tx.ar, tx.ag, tx.ab);
+                store_pixel(s, i, p, precise_setup, tx.depth, tx.ar, tx.ag, tx.ab);
                 uint32_t b = tile_base, n = tile_len;
                 if (FROXELS) {
                     // own froxel: column of (x, y), slice of the linear view depth
@@ -422,7 +434,8 @@ __device__ __forceinline__ void shade_tile(
         if (own) {
             px = s.px[F_PX][i]; py = s.px[F_PY][i]; pz = s.px[F_PZ][i];
             plx = s.px[F_PLX][i]; ply = s.px[F_PLY][i]; plz = s.px[F_PLZ][i];
-            pixel_normal(s, i, nx, ny, nz);
+            float in_;
+            pixel_normal(s, i, nx, ny, nz, in_);
             // |N.t| within |P| 2^-20 of zero is left to the exact NdL cut
             slack = fma_(pz, pz, fma_(py, py, px * px)) * (1.0f / 1099511627776.0f);
             lb = s.base[i];
@@ -486,15 +499,16 @@ __device__ __forceinline__ void shade_tile(
                 }
             }
         }
-        for (uint32_t j0 = 0; j0 < maxlen; j0 += kPipe) {
-            uint32_t li[kPipe];
-            float4 a[kPipe];
+        constexpr int PIPE = PRECISE ? 2 : kPipe;  // the precise path keeps fewer loads in flight (registers)
+        for (uint32_t j0 = 0; j0 < maxlen; j0 += PIPE) {
+            uint32_t li[PIPE];
+            float4 a[PIPE];
 #pragma unroll
-            for (int u = 0; u < kPipe; ++u) li[u] = (j0 + u < ln) ? __ldg(grid.lists + lb + j0 + u) : 0xffffffffu;
+            for (int u = 0; u < PIPE; ++u) li[u] = (j0 + u < ln) ? __ldg(grid.lists + lb + j0 + u) : 0xffffffffu;
 #pragma unroll
-            for (int u = 0; u < kPipe; ++u) a[u] = li[u] < n_lights ? __ldg(cand + li[u]) : make_float4(0, 0, 0, 0);
+            for (int u = 0; u < PIPE; ++u) a[u] = li[u] < n_lights ? __ldg(cand + li[u]) : make_float4(0, 0, 0, 0);
 #pragma unroll
-            for (int u = 0; u < kPipe; ++u) {
+            for (int u = 0; u < PIPE; ++u) {
                 if (j0 + u >= maxlen) break;  // warp-uniform
                 bool pass = false;
                 if (j0 + u < ln) {
@@ -556,7 +570,8 @@ __device__ __forceinline__ void shade_tile(
             tx.er = tx.eg = tx.eb = 0.0f;
         }
         float nxo, ny, nzo;
-        pixel_normal(s, i, nxo, ny, nzo);
+        float in_;
+        pixel_normal(s, i, nxo, ny, nzo, in_);
         const float amb = glb->ambient_intensity;
         const float skr = glb->ambient_color[0] * amb, skg = glb->ambient_color[1] * amb,
                     skb = glb->ambient_color[2] * amb;
@@ -651,7 +666,7 @@ template <uint32_t LAYOUT, uint32_t TARGET>
 cudaError_t launch_batched(const ShadeViewDesc* descs, uint32_t n_views, uint32_t total_tiles, const void* globals,
                            const void* lights, uint32_t n, int* status, cudaStream_t stream) {
     auto kern = shade_batched_kernel<LAYOUT, TARGET>;
-    const int smem = int(sizeof(sk::Smem<32 * 16>));
+    const int smem = int(sizeof(sk::Smem<32 * 16, sk::record_fields<LAYOUT>()>));
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     if (n > 0) {
@@ -672,7 +687,7 @@ cudaError_t launch_one(const void* camera, const void* globals, const GBufView& 
     constexpr bool FROXELS = (GRID == HL_GRID_FROXELS);
     constexpr int TW = FROXELS ? 32 : 16, TH = 16;
     auto kern = shade_kernel<LAYOUT, GRID, TARGET, STATS, TW, TH>;
-    const int smem = int(sizeof(sk::Smem<TW * TH>));
+    const int smem = int(sizeof(sk::Smem<TW * TH, sk::record_fields<LAYOUT>()>));
     static unsigned long long attr_devices = 0;  // devices on which the smem limit is raised
     int dev = 0;
     cudaGetDevice(&dev);
