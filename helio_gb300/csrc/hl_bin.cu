@@ -88,6 +88,7 @@ __device__ __forceinline__ BinLight prep_light(const GpuCamera* __restrict__ cam
 __global__ void __launch_bounds__(256) prep_bin_lights_kernel(const GpuCamera* __restrict__ cam,
                                                               const GpuLight* __restrict__ lights, uint32_t n,
                                                               uint32_t froxel_margin, BinLight* __restrict__ out) {
+    pdl_launch_dependents();  // the binning kernel sets its column up meanwhile
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     out[i] = prep_light(cam, lights[i], froxel_margin);
@@ -349,9 +350,12 @@ constexpr uint32_t kFlagAggregate = 1u, kFlagPrefix = 2u;
 constexpr uint32_t kChainValueMax = (1u << 30) - 1u;
 constexpr uint32_t kLookbackSpins = 1u << 20;  // ~0.1 s of polling before HL_ERR_TIMEOUT
 
+constexpr uint32_t kMaskCap = 4096;  // (slice, 32-light chunk) results kept from the count for the fill
+
 struct FusedSmem {
     BinSmem b;
     uint32_t slice_dst[kMaxSlices];  // first entry of each slice of this column
+    uint32_t mask[kMaskCap];         // ballot of chunk c of slice s at [s * chunks + c]
     uint32_t col, excl, total;
 };
 
@@ -397,32 +401,56 @@ __device__ __forceinline__ uint32_t gather_round(BinSmem& sm, const ColumnGeom& 
 }
 
 // Tests a gathered round against every slice box of the column: counts into
-// sm.slice_run, and with FILL writes the lists from sm.slice_dst.
+// sm.slice_run, and with FILL writes the lists from sm.slice_dst. A warp takes a slice
+// and four 32-light chunks at a time, their light loads in flight together. With MASKS
+// the count keeps each chunk's ballot and the fill replays them instead of testing again.
 template <bool FILL>
 __device__ __forceinline__ void test_slices(FusedSmem& fs, const ColumnGeom& g, const BinLight* __restrict__ bl,
                                             const hl_froxel_params& p, const float* __restrict__ tabz, float zlast,
-                                            uint32_t col_len, uint32_t* __restrict__ indices, uint32_t capacity) {
+                                            uint32_t col_len, uint32_t* __restrict__ indices, uint32_t capacity,
+                                            bool masks) {
+    constexpr uint32_t kU = 4;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t chunks = (col_len + 31) / 32;
     for (uint32_t s = warp; s < p.grid_z; s += kBinWarps) {
-        const float z0 = tabz[s];
-        const float z1 = (s + 1 == p.grid_z) ? zlast : tabz[s + 1];
-        const Box b = froxel_box(g, z0, z1);
         uint32_t run = fs.b.slice_run[s];
         const uint32_t dst0 = FILL ? fs.slice_dst[s] : 0u;
-        for (uint32_t j0 = 0; j0 < col_len; j0 += 32) {
-            const uint32_t j = j0 + lane;
-            bool pass = false;
-            uint32_t li = 0;
-            if (j < col_len) {
-                li = fs.b.col[j];
-                pass = light_meets_froxel(bl[li], b);
+        uint32_t* sm_mask = fs.mask + s * chunks;
+        if (FILL && masks) {
+            for (uint32_t c = 0; c < chunks; ++c) {
+                const uint32_t mask = sm_mask[c];
+                if ((mask >> lane) & 1u) {
+                    const uint64_t dst = uint64_t(dst0) + run + __popc(mask & lanemask_lt());
+                    if (dst < capacity) indices[dst] = fs.b.col[c * 32 + lane];
+                }
+                run += __popc(mask);
             }
-            const uint32_t mask = __ballot_sync(0xffffffffu, pass);
-            if (FILL && pass) {
-                const uint64_t dst = uint64_t(dst0) + run + __popc(mask & lanemask_lt());
-                if (dst < capacity) indices[dst] = li;
+        } else {
+            const float z0 = tabz[s];
+            const float z1 = (s + 1 == p.grid_z) ? zlast : tabz[s + 1];
+            const Box b = froxel_box(g, z0, z1);
+            for (uint32_t c0 = 0; c0 < chunks; c0 += kU) {
+                uint32_t li[kU];
+                BinLight l[kU];
+#pragma unroll
+                for (uint32_t u = 0; u < kU; ++u) {
+                    const uint32_t j = (c0 + u) * 32 + lane;
+                    li[u] = j < col_len ? fs.b.col[j] : 0xffffffffu;
+                    if (li[u] != 0xffffffffu) l[u] = bl[li[u]];
+                }
+#pragma unroll
+                for (uint32_t u = 0; u < kU; ++u) {
+                    if (c0 + u >= chunks) break;  // warp-uniform
+                    const bool pass = li[u] != 0xffffffffu && light_meets_froxel(l[u], b);
+                    const uint32_t mask = __ballot_sync(0xffffffffu, pass);
+                    if (FILL && pass) {
+                        const uint64_t dst = uint64_t(dst0) + run + __popc(mask & lanemask_lt());
+                        if (dst < capacity) indices[dst] = li[u];
+                    }
+                    if (!FILL && masks && lane == 0) sm_mask[c0 + u] = mask;
+                    run += __popc(mask);
+                }
             }
-            run += __popc(mask);
         }
         if (lane == 0) fs.b.slice_run[s] = run;
     }
@@ -453,14 +481,18 @@ __global__ void __launch_bounds__(kBinThreads) bin_froxels_fused_kernel(
     const ColumnGeom g = column_geom(cam, p, col % p.grid_x, col / p.grid_x);
     const float zlast = xmax(tab.z[p.grid_z], cam->forward_far[3]);
     for (uint32_t s = threadIdx.x; s < p.grid_z; s += blockDim.x) fs.b.slice_run[s] = 0;
+    pdl_launch_dependents();  // the shading launch's light table and pixel set-up may start
+    pdl_wait();               // the view-space lights are written
 
     // ---- 1. count ----
     uint32_t base = 0, col_len = 0;
-    bool one_round = true;
+    bool one_round = true, masks = false;
     for (bool first = true;; first = false) {
         col_len = gather_round(fs.b, g, bl, n, base);
         if (!first) one_round = false;
-        test_slices<false>(fs, g, bl, p, tab.z, zlast, col_len, indices, capacity);
+        // a column gathered in one round keeps its chunk ballots when they fit
+        masks = one_round && base >= n && p.grid_z * ((col_len + 31) / 32) <= kMaskCap;
+        test_slices<false>(fs, g, bl, p, tab.z, zlast, col_len, indices, capacity, masks);
         if (base >= n) break;
     }
     __syncthreads();
@@ -522,12 +554,12 @@ __global__ void __launch_bounds__(kBinThreads) bin_froxels_fused_kernel(
 
     // ---- 3. fill (from the round still in shared memory when there was only one) ----
     if (one_round) {
-        test_slices<true>(fs, g, bl, p, tab.z, zlast, col_len, indices, capacity);
+        test_slices<true>(fs, g, bl, p, tab.z, zlast, col_len, indices, capacity, masks);
     } else {
         base = 0;
         for (;;) {
             col_len = gather_round(fs.b, g, bl, n, base);
-            test_slices<true>(fs, g, bl, p, tab.z, zlast, col_len, indices, capacity);
+            test_slices<true>(fs, g, bl, p, tab.z, zlast, col_len, indices, capacity, false);
             if (base >= n) break;
         }
     }
@@ -688,6 +720,12 @@ cudaError_t launch_bin_froxels_fused(const void* camera, const BinLight* bl, uin
                                      int* status, unsigned long long* chain, BinChainState* state,
                                      cudaStream_t stream) {
     const uint32_t cols = p.grid_x * p.grid_y;
+    // as a dependent launch only right after this call's light preparation: two binning
+    // launches of one context must never overlap (ticket and epoch)
+    if (n > 0)
+        return launch_pdl(bin_froxels_fused_kernel, dim3(cols), dim3(kBinThreads), 0, stream,
+                          static_cast<const GpuCamera*>(camera), bl, n, p, tab, offsets, indices, capacity, status,
+                          chain, state);
     bin_froxels_fused_kernel<<<cols, kBinThreads, 0, stream>>>(static_cast<const GpuCamera*>(camera), bl, n, p, tab,
                                                                offsets, indices, capacity, status, chain, state);
     return cudaGetLastError();

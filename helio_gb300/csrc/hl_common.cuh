@@ -89,6 +89,32 @@ __device__ __forceinline__ void raise_status(int* status, int code) {
 }
 
 // ----------------------------------------------------------------------------------
+// Programmatic dependent launch. A kernel launched with launch_pdl may have its CTAs
+// start while the previous kernel of the stream still runs, once that kernel has called
+// pdl_launch_dependents; pdl_wait then blocks until the previous kernel has completed
+// and its writes are visible. For a kernel launched without the attribute both are
+// no-ops. A kernel reads nothing its predecessor writes before its pdl_wait.
+// ----------------------------------------------------------------------------------
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                              Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
+// ----------------------------------------------------------------------------------
 // Correctly rounded f32 operations: with these the binning kernels reproduce the
 // declared operation order bit for bit (no FMA contraction, IEEE division and sqrt).
 // ----------------------------------------------------------------------------------

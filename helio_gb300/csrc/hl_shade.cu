@@ -282,6 +282,7 @@ __device__ __forceinline__ void shade_tile(
         key_by_column = ncols * fp.grid_z <= uint32_t(kBins);
     } else {
         const uint32_t tile = by * glb->num_tiles_x + bx;
+        pdl_wait();  // the lists are written
         if (tile < grid.tiles) {
             tile_len = __ldg(grid.counts + tile);
             if (tile_len > kMaxPerTile) {
@@ -359,6 +360,7 @@ __device__ __forceinline__ void shade_tile(
                     const uint32_t fx = s.col_of[x - x0];
                     const uint32_t fy = s.row_of[y - y0];
                     const uint32_t f = (fy * fp.grid_x + fx) * fp.grid_z + sl;
+                    pdl_wait();  // the lists are written (the texel loads above overlap the binning)
                     b = __ldg(grid.counts + f);
                     const uint32_t e = __ldg(grid.counts + f + 1);
                     if (b <= e && e <= grid.lists_capacity) {
@@ -376,6 +378,7 @@ __device__ __forceinline__ void shade_tile(
             }
         }
     }
+    pdl_wait();  // every thread: the walk reads the lists and the light table
     __syncthreads();
     {   // exclusive scan of the froxel-key histogram, two bins per thread
         const uint32_t a = s.hist[2 * t], b = s.hist[2 * t + 1];
@@ -647,11 +650,16 @@ __device__ __forceinline__ float4 cand_entry(const GpuCamera* __restrict__ cam, 
     return c;
 }
 
+// Launched as a dependent of whatever precedes it (the binning, in a frame): it reads
+// only the camera and the lights, and waits for its predecessor before it ends, so the
+// shading kernel that waits for it also waits for the lists.
 __global__ void __launch_bounds__(256) prep_cand_kernel(const GpuCamera* __restrict__ cam,
                                                         const GpuLight* __restrict__ lights, uint32_t n,
                                                         uint32_t relative, float4* __restrict__ out) {
+    pdl_launch_dependents();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = cand_entry(cam, lights[i], relative != 0u);
+    pdl_wait();
 }
 
 __global__ void __launch_bounds__(256) prep_cand_batched_kernel(const ShadeViewDesc* __restrict__ d,
@@ -697,18 +705,15 @@ cudaError_t launch_one(const void* camera, const void* globals, const GBufView& 
         attr_devices |= 1ull << dev;
     }
     if (n > 0) {
-        prep_cand_kernel<<<(n + 255) / 256, 256, 0, stream>>>(static_cast<const GpuCamera*>(camera),
-                                                              static_cast<const GpuLight*>(lights), n,
-                                                              LAYOUT == HL_GBUF_F16 ? 1u : 0u, cand);
-        cudaError_t e = cudaGetLastError();
+        cudaError_t e = launch_pdl(prep_cand_kernel, dim3((n + 255) / 256), dim3(256), 0, stream,
+                                   static_cast<const GpuCamera*>(camera), static_cast<const GpuLight*>(lights), n,
+                                   LAYOUT == HL_GBUF_F16 ? 1u : 0u, cand);
         if (e != cudaSuccess) return e;
     }
     const dim3 g((gb.width + TW - 1) / TW, (gb.height + TH - 1) / TH);
-    kern<<<g, sk::kThreads, smem, stream>>>(static_cast<const GpuCamera*>(camera),
-                                            static_cast<const DeferredGlobals*>(globals), gb,
-                                            static_cast<const GpuLight*>(lights), n, grid, tab, out, stats, status,
-                                            cand);
-    return cudaGetLastError();
+    return launch_pdl(kern, g, dim3(sk::kThreads), smem, stream, static_cast<const GpuCamera*>(camera),
+                      static_cast<const DeferredGlobals*>(globals), gb, static_cast<const GpuLight*>(lights), n, grid,
+                      tab, out, stats, status, static_cast<const float4*>(cand));
 }
 
 template <uint32_t LAYOUT, uint32_t GRID>
