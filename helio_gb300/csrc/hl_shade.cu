@@ -32,9 +32,9 @@ namespace sk {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kQueue = 256;      // per-warp pair ring (up to 31 + kPipe * 32 pending)
+constexpr int kQueue = 128;      // per-warp pair ring (up to 31 + kPipe * 32 pending)
 constexpr int kBins = 512;       // froxel keys of the pixel sort
-constexpr int kPipe = 4;         // list entries in flight per lane (fast path; 2 on the precise path)
+constexpr int kPipe = 3;         // list entries in flight per lane (fast path; 2 on the precise path)
 constexpr int kBoxMin = 8;       // shortest shared list worth a box cull
 
 // Pixel record fields (structure of arrays). N, 1/|n|, V, F0 (except for the reference
@@ -52,20 +52,29 @@ enum Field : int {
 template <uint32_t LAYOUT>
 __host__ __device__ constexpr int record_fields() { return LAYOUT == HL_GBUF_REFERENCE ? int(F_COUNT) : int(F_F0R); }
 
+static_assert(31 + 32 * kPipe <= kQueue, "pair ring too small");
+
 template <int NPX, int NF>
 struct Smem {
     float px[NF][NPX];
     float acc[6][NPX];              // Kahan (sum, compensation) x RGB; statistics reuse it
     uint32_t base[NPX], len[NPX];   // each pixel's light list
-    uint32_t hist[kBins];
+    union {
+        struct {                    // set-up and sort only
+            uint32_t hist[kBins];
+            float tab[kMaxSlices + 1];        // slice boundaries
+            uint16_t col_of[32], row_of[16];  // froxel column / row of the tile's pixel columns / rows
+        } sort;
+        uint32_t queue[kWarps][kQueue];  // walk only: ring of (pixel << 23) | light index
+    } u;
     uint16_t order[NPX];            // pixels sorted by froxel
-    uint32_t queue[kWarps][kQueue]; // ring of (pixel << 23) | light index
     uint32_t warp_tot[kWarps];
-    float tab[kMaxSlices + 1];      // slice boundaries
     uint32_t n_valid;
     uint32_t next_group;            // next group of sorted pixels to hand to a warp
-    uint16_t col_of[32], row_of[16];  // froxel column / row of the tile's pixel columns / rows
 };
+// Three CTAs of the FP16 / FP32 record fit in a 164 KB shared-memory carve-out, which
+// leaves 92 KB of the SM's 256 KB to L1 for the light tables and lists.
+static_assert(3 * (sizeof(Smem<512, int(F_F0R)>) + 1024) <= 164 * 1024, "shading CTA shared memory");
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
@@ -256,14 +265,14 @@ __device__ __forceinline__ void shade_tile(
     const float W = float(gb.width), H = float(gb.height);
     const float camx = cam->position_near[0], camy = cam->position_near[1], camz = cam->position_near[2];
 
-    for (uint32_t b = t; b < uint32_t(kBins); b += kThreads) s.hist[b] = 0;
+    for (uint32_t b = t; b < uint32_t(kBins); b += kThreads) s.u.sort.hist[b] = 0;
     if (FROXELS) {
-        for (uint32_t k = t; k <= grid.fp.grid_z; k += kThreads) s.tab[k] = tabz[k];
+        for (uint32_t k = t; k <= grid.fp.grid_z; k += kThreads) s.u.sort.tab[k] = tabz[k];
         // froxel column of each pixel column and row of the tile (one division each)
         if (t < uint32_t(TW))
-            s.col_of[t] = uint16_t((uint64_t(x0 + t) * grid.fp.grid_x) / grid.fp.width);
+            s.u.sort.col_of[t] = uint16_t((uint64_t(x0 + t) * grid.fp.grid_x) / grid.fp.width);
         else if (t < uint32_t(TW + TH))
-            s.row_of[t - TW] = uint16_t((uint64_t(y0 + t - TW) * grid.fp.grid_y) / grid.fp.height);
+            s.u.sort.row_of[t - TW] = uint16_t((uint64_t(y0 + t - TW) * grid.fp.grid_y) / grid.fp.height);
     }
 #pragma unroll
     for (int k = 0; k < PPT; ++k)
@@ -299,7 +308,7 @@ __device__ __forceinline__ void shade_tile(
     // slices are exponential from slice_near to tab[grid_z]: slice ~ log2(d / near) * scale
     const float slice_inv_near = FROXELS ? rcp_(grid.fp.slice_near) : 0.0f;
     const float slice_scale =
-        FROXELS ? float(grid.fp.grid_z) * rcp_(__log2f(fmaxf(s.tab[grid.fp.grid_z] * slice_inv_near, 2.0f))) : 0.0f;
+        FROXELS ? float(grid.fp.grid_z) * rcp_(__log2f(fmaxf(s.u.sort.tab[grid.fp.grid_z] * slice_inv_near, 2.0f))) : 0.0f;
 
     // ---- 1. pixel set-up -------------------------------------------------------
     float rel[12], wrow[4];
@@ -355,10 +364,10 @@ __device__ __forceinline__ void shade_tile(
                     // slice spacing, then exact steps against the table
                     const int guess = int(__log2f(dv * slice_inv_near) * slice_scale);
                     uint32_t sl = uint32_t(min(max(guess, 0), int(fp.grid_z) - 1));
-                    while (sl + 1 < fp.grid_z && s.tab[sl + 1] <= dv) ++sl;
-                    while (sl > 0 && s.tab[sl] > dv) --sl;
-                    const uint32_t fx = s.col_of[x - x0];
-                    const uint32_t fy = s.row_of[y - y0];
+                    while (sl + 1 < fp.grid_z && s.u.sort.tab[sl + 1] <= dv) ++sl;
+                    while (sl > 0 && s.u.sort.tab[sl] > dv) --sl;
+                    const uint32_t fx = s.u.sort.col_of[x - x0];
+                    const uint32_t fy = s.u.sort.row_of[y - y0];
                     const uint32_t f = (fy * fp.grid_x + fx) * fp.grid_z + sl;
                     pdl_wait();  // the lists are written (the texel loads above overlap the binning)
                     b = __ldg(grid.counts + f);
@@ -374,14 +383,14 @@ __device__ __forceinline__ void shade_tile(
                 s.base[i] = b;
                 s.len[i] = n;
                 if (STATS) cnt[3][i] = n;
-                slot[k] = atomicAdd(&s.hist[key[k]], 1u);
+                slot[k] = atomicAdd(&s.u.sort.hist[key[k]], 1u);
             }
         }
     }
     pdl_wait();  // every thread: the walk reads the lists and the light table
     __syncthreads();
     {   // exclusive scan of the froxel-key histogram, two bins per thread
-        const uint32_t a = s.hist[2 * t], b = s.hist[2 * t + 1];
+        const uint32_t a = s.u.sort.hist[2 * t], b = s.u.sort.hist[2 * t + 1];
         uint32_t v = a + b;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -399,8 +408,8 @@ __device__ __forceinline__ void shade_tile(
         }
         const uint32_t excl = before + v - (a + b);
         __syncthreads();
-        s.hist[2 * t] = excl;
-        s.hist[2 * t + 1] = excl + a;
+        s.u.sort.hist[2 * t] = excl;
+        s.u.sort.hist[2 * t + 1] = excl + a;
         if (t == 0) {
             s.n_valid = total;
             s.next_group = 0;
@@ -409,13 +418,13 @@ __device__ __forceinline__ void shade_tile(
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < PPT; ++k)
-        if (valid[k]) s.order[s.hist[key[k]] + slot[k]] = uint16_t(t + k * kThreads);
+        if (valid[k]) s.order[s.u.sort.hist[key[k]] + slot[k]] = uint16_t(t + k * kThreads);
     __syncthreads();
 
     // ---- 2-4. groups of 32 sorted pixels walk their lists --------------------------
     const uint32_t n_valid = s.n_valid;
     uint32_t qlen = 0;
-    uint32_t* queue = s.queue[warp];
+    uint32_t* queue = s.u.queue[warp];
 
     uint32_t head = 0;  // ring position of the oldest pending pair
 
