@@ -48,3 +48,57 @@ def test_pipeline_matches_device_path(ctx):
     ctx.sync_status()
     for k in range(6):
         assert np.array_equal(outs[k].numpy(), want[k % 2]), f"frame {k}"
+
+
+def test_dependent_launch_orders(ctx):
+    """The binning, light-table and shading launches start while their predecessor runs
+    (programmatic dependent launches) and wait before reading its outputs. Back-to-back
+    calls in any order on one stream, with no synchronisation between them, must give
+    the results of the same calls synchronised one by one: binning after binning with
+    and without lights, shading twice in a row, shading right after a binning without
+    lights, and a second scene binned into the same buffers in between."""
+    import torch
+
+    a = S.workload(1, 0.5)
+    b = S.workload(1, 0.5)
+    b.lights["position_range"][:, 0] += 1.5  # a second light set of the same shape
+    W, H = a.gbuffer.width, a.gbuffer.height
+    p = N.froxel_params(*a.froxel_grid, W, H, a.camera.far)
+    F = p.grid_x * p.grid_y * p.grid_z
+    cap = F * 256
+    da, db = FR.upload_workload(a), FR.upload_workload(b)
+    off = torch.zeros(F + 1, dtype=torch.int32, device="cuda")
+    idx = torch.zeros(cap, dtype=torch.int32, device="cuda")
+    grid = N.froxel_grid_struct(idx, off, p, cap)
+    outs = [torch.zeros((H, W, 4), dtype=torch.float32, device="cuda") for _ in range(4)]
+
+    def run(sync):
+        for o in outs:
+            o.zero_()
+        steps = [
+            lambda: ctx.bin_froxels(da.camera, da.lights, 0, p, off, idx, cap),
+            lambda: ctx.bin_froxels(da.camera, da.lights, 0, p, off, idx, cap),
+            lambda: ctx.shade(da.camera, da.globals_, da.gbuffer, da.lights, 0, grid, N.target_struct(outs[0])),
+            lambda: ctx.bin_froxels(db.camera, db.lights, db.n_lights, p, off, idx, cap),
+            lambda: ctx.shade(db.camera, db.globals_, db.gbuffer, db.lights, db.n_lights, grid,
+                              N.target_struct(outs[1])),
+            lambda: ctx.bin_froxels(da.camera, da.lights, da.n_lights, p, off, idx, cap),
+            lambda: ctx.shade(da.camera, da.globals_, da.gbuffer, da.lights, da.n_lights, grid,
+                              N.target_struct(outs[2])),
+            lambda: ctx.shade(da.camera, da.globals_, da.gbuffer, da.lights, da.n_lights, grid,
+                              N.target_struct(outs[3])),
+        ]
+        for f in steps:
+            f()
+            if sync:
+                torch.cuda.synchronize()
+        ctx.sync_status()
+        return [o.cpu().numpy() for o in outs] + [off.cpu().numpy(), idx[: int(off[-1])].cpu().numpy()]
+
+    want = run(True)
+    assert np.any(want[1] != want[2]), "the two scenes must differ"
+    assert np.array_equal(want[2], want[3])
+    for _ in range(5):
+        got = run(False)
+        for g, w in zip(got, want):
+            assert np.array_equal(g, w)
