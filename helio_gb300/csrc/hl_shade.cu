@@ -7,9 +7,9 @@
 //     memory, with its light list (its froxel's list, or the tile's reference list);
 //  2. pixels are counting-sorted by froxel (slice, column), so a group of 32 pixels
 //     mostly shares one list; each warp takes a light and a heavy group;
-//  3. each lane walks its own pixel's list in list order, four entries at a time with the
-//     loads of the next entries in flight, and tests each light for range and the NdL
-//     sign; passing (pixel, light) pairs go to a per-warp queue;
+//  3. each lane walks its own pixel's list in list order, three entries at a time (two
+//     on the precise path) with their loads in flight together, and tests each light
+//     for range and the NdL sign; passing (pixel, light) pairs go to a per-warp queue;
 //  4. queued pairs are evaluated 32 at a time, one per lane, so the full BRDF of
 //     pbr_direct_light runs with all lanes busy, and are added into per-pixel Kahan
 //     accumulators in queue order, which is list order for every pixel, as the

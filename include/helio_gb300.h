@@ -14,7 +14,10 @@
  *     GpuCameraUniforms (368 B, libhelio/src/camera.rs:12-29), DeferredGlobals
  *     (112 B, helio-pass-deferred-light/src/lib.rs:17-52).
  *   - `stream` is a cudaStream_t passed as void* (0 = legacy default stream).
- *     All work is enqueued asynchronously on it.
+ *     All work is enqueued asynchronously on it. hl_bin_froxels and hl_shade enqueue
+ *     some kernels as programmatic dependent launches: they may start while this
+ *     library's preceding kernel on the stream still runs, and read nothing it writes
+ *     before it completes. Work of the caller's between two calls is ordered as usual.
  *   - Argument errors are returned synchronously. Device-side conditions (an
  *     out-of-range light index, froxel index capacity exceeded, a bounded wait that
  *     gave up) raise a flag in the context that hl_sync_status() reports.
