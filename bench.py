@@ -147,9 +147,17 @@ def max_over_ranks(world, v: float) -> float:
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(world, pixels_per_step: int, steps: int, seconds: float):
+    """Whole-job Mpix/s of ``world`` independent replicas, each lighting ``steps`` frames
+    of ``pixels_per_step`` pixels: all ranks' pixels over the slowest rank's time.
+    Returns (Mpix/s, slowest rank's seconds)."""
+    t = max_over_ranks(world, seconds)
+    return pixels_per_step * steps * world / t / 1e6, t
 
 
 # ----------------------------------------------------------------------------------
@@ -260,8 +268,7 @@ def run_ours(args, world, rank, local):
     step_ms = [ev[k][0].elapsed_time(ev[k][2]) for k in range(args.steps)]
     bin_ms = [ev[k][0].elapsed_time(ev[k][1]) for k in range(args.steps)]
     shade_ms = [ev[k][1].elapsed_time(ev[k][2]) for k in range(args.steps)]
-    t_total = max_over_ranks(world, sum(step_ms) / 1e3)
-    value = W * H * args.steps * world / t_total / 1e6
+    value, t_total = replica_throughput(world, W * H, args.steps, sum(step_ms) / 1e3)
     ms_per_step = t_total * 1e3 / args.steps
     clk = clocks.summary()
 
@@ -288,8 +295,7 @@ def run_ours(args, world, rank, local):
     pipe.synchronize()
     torch.cuda.synchronize()
     barrier(world)
-    e2e_t = max_over_ranks(world, e0.elapsed_time(e1) / 1e3)
-    e2e_value = W * H * args.steps * world / e2e_t / 1e6
+    e2e_value, e2e_t = replica_throughput(world, W * H, args.steps, e0.elapsed_time(e1) / 1e3)
     ctx.sync_status(sh)
     e2e_check = bool(np.array_equal(host_outs[(args.steps - 1) % 2].numpy(), target.cpu().numpy()))
 
