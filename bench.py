@@ -410,8 +410,9 @@ def _median_ms(fn, stream, flush, reps, warm=3):
 
 
 def run_forms(ctx, dev, stream, flush, with_oracle=True):
-    """The three other forms of the path, each timed with CUDA events (L2 flushed):
-    adjoint (w4), batched views (w3) and the FP16/FP32 G-buffer precision pair."""
+    """The other forms of the path, each timed with CUDA events (L2 flushed): adjoint
+    (w4), batched views (w3), and the fragment light loops (Forward+ and transparent)
+    over w1's lists."""
     import torch
 
     from helio_gb300 import frame as FR
@@ -548,6 +549,52 @@ def run_forms(ctx, dev, stream, flush, with_oracle=True):
         "error_vs_fp64_oracle": batch_err,
     }
     plan.close()
+
+    # ---- fragments: Forward+ and transparent light loops over w1's froxel lists ----
+    w = S.workload(1)
+    W, H = w.gbuffer.width, w.gbuffer.height
+    p_np = L.froxel_params(*w.froxel_grid, W, H, w.camera.far)
+    fp = N.froxel_params_from_numpy(p_np)
+    F = fp.grid_x * fp.grid_y * fp.grid_z
+    df = FR.upload_workload(w, dev)
+    cap = F * 64
+    off = torch.zeros(F + 1, dtype=torch.int32, device=dev)
+    idx = torch.zeros(cap, dtype=torch.int32, device=dev)
+    ctx.bin_froxels(df.camera, df.lights, df.n_lights, fp, off, idx, cap, sh)
+    ctx.sync_status(sh)
+    grid = N.froxel_grid_struct(idx, off, fp, cap)
+    n_frag = W * H
+    fr = S.make_fragments(w.camera, 11, n_frag, raster_order=True)
+    d_fr = FR.bytes_tensor(fr, dev)
+    out = torch.zeros((n_frag, 4), dtype=torch.float32, device=dev)
+    hbm_peak, _ = measured_peaks()
+    frag = {"workload": "w1 camera, lights and froxel lists; one fragment per pixel (view depth U[2, 14], "
+                        "raster order), 80 B hl_fragment records, RGBA32F out", "fragments": n_frag}
+    sel = np.random.default_rng(12).choice(n_frag, 65536, replace=False)
+    off_h = off.cpu().numpy().view(np.uint32)
+    idx_h = idx.cpu().numpy().view(np.uint32)[: int(off_h[-1])]
+    for mode, name in ((L.FRAGMENTS_FORWARD, "forward"), (L.FRAGMENTS_TRANSPARENT, "transparent")):
+        prm = S.fragment_params(mode, L.tile_grid(W, H)[0])
+        fpar = N.FragmentParams(int(prm["mode"][0]), int(prm["num_tiles_x"][0]), float(prm["ambient_intensity"][0]),
+                                (N.C.c_float * 3)(*[float(v) for v in prm["ambient_color"][0]]))
+        t_f = _median_ms(lambda: ctx.shade_fragments(df.camera, fpar, d_fr, n_frag, df.lights, df.n_lights, grid, out,
+                                                     stream=sh), stream, flush, 20)
+        ctx.sync_status(sh)
+        entry = {"ms": round(t_f, 4), "mfrag_s": round(n_frag / t_f / 1e3, 1),
+                 "hbm_frac": round(n_frag * (80 + 16) / (t_f / 1e3) / 1e9 / hbm_peak, 4)}
+        if with_oracle:
+            import oracle
+
+            want = oracle.shade_fragments(w.camera.record, prm, fr[sel], w.lights, ("froxels", idx_h, off_h, p_np))
+            got = out.cpu().numpy().astype(np.float64)[sel]
+            keep = ~np.isnan(want[:, 0])
+            g, o = got[keep][:, :3], want[keep][:, :3]
+            rel = (np.abs(g - o) / np.maximum(np.abs(o), 1e-6 * np.abs(o).max())).max(1)
+            entry["error_vs_fp64_oracle"] = {"sample": int(keep.sum()), "max": float(f"{rel.max():.3e}"),
+                                             "p9999": float(f"{np.quantile(rel, 0.9999):.3e}"),
+                                             "over_1e-3": int((rel > 1e-3).sum())}
+        frag[name] = entry
+    forms["fragments"] = frag
     return forms
 
 

@@ -406,3 +406,48 @@ def batched_views(scale: float = 1.0, layout: int = LAYOUT_F16):
         views.append(View(cam, make_gbuffer(cam, layout, seed=3000 + vi)))
         vi += 1
     return views, lights
+
+
+def make_fragments(cam: Camera, seed: int, n: int, discard_frac: float = 0.05, raster_order: bool = False) -> np.ndarray:
+    """``n`` hl_fragment records (layouts.FRAGMENT) at random pixels of ``cam``'s viewport,
+    view depth U[2, 14], each the world point under its pixel centre (f32), with random
+    normals facing the camera and random materials; about ``discard_frac`` of them have
+    alpha <= 0.001. ``raster_order`` sorts them by pixel, as a rasteriser emits them."""
+    W, H = cam.width, cam.height
+    u = lambda k, lo=0.0, hi=1.0: uniform(seed, 300 + k, n, lo, hi)
+    x = np.minimum((u(0) * W).astype(np.int64), W - 1)
+    y = np.minimum((u(1) * H).astype(np.int64), H - 1)
+    d = u(2, 2.0, 14.0)
+    z = (cam.far / (cam.far - cam.near)) * (1.0 - cam.near / d)
+    ndc = np.stack([(x + 0.5) / W * 2 - 1, 1 - (y + 0.5) / H * 2, z, np.ones(n)])
+    h = cam.inv_view_proj @ ndc
+    P = (h[:3] / h[3]).T
+    V = np.asarray(cam.eye, np.float64)[None, :] - P
+    V /= np.linalg.norm(V, axis=1, keepdims=True)
+    Nr = np.stack([u(3, -1, 1), u(4, -1, 1), u(5, -1, 1)], 1) + 1.2 * V
+    Nr /= np.linalg.norm(Nr, axis=1, keepdims=True)
+    fr = np.zeros(n, L.FRAGMENT)
+    fr["position"] = P.astype(np.float32)
+    fr["pixel"] = (x | (y << 16)).astype(np.uint32)
+    fr["normal"] = Nr.astype(np.float32)
+    fr["alpha"] = np.where(u(6) < discard_frac, 0.0005, u(7, 0.2, 1.0)).astype(np.float32)
+    albedo = np.stack([u(8), u(9), u(10)], 1)
+    metal = (u(11) < 0.3).astype(np.float64)
+    fr["albedo"] = albedo.astype(np.float32)
+    fr["roughness"] = u(12, 0.05, 1.0).astype(np.float32)
+    fr["metallic"] = metal.astype(np.float32)
+    fr["f0"] = np.clip(0.04 * (1 - metal[:, None]) + albedo * metal[:, None], 0, 0.999).astype(np.float32)
+    fr["emissive"] = np.stack([u(13, 0, 0.2), u(14, 0, 0.2), u(15, 0, 0.2)], 1).astype(np.float32)
+    fr["ao"] = u(16, 0.5, 1.0).astype(np.float32)
+    if raster_order:
+        fr = fr[np.argsort(y * W + x, kind="stable")]
+    return fr
+
+
+def fragment_params(mode: int, num_tiles_x: int, ambient_intensity: float = 0.4,
+                    ambient_color=(0.5, 0.55, 0.6)) -> np.ndarray:
+    """One layouts.FRAGMENT_PARAMS record."""
+    p = np.zeros(1, L.FRAGMENT_PARAMS)
+    p["mode"], p["num_tiles_x"] = mode, num_tiles_x
+    p["ambient_intensity"], p["ambient_color"] = ambient_intensity, ambient_color
+    return p
