@@ -242,7 +242,10 @@ __device__ __noinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>
 
 // TW x TH = 512 (froxel grid) or 256 (tile grid) pixels, 256 threads.
 // One tile (bx, by) of one view; tabz: the view's slice boundaries (froxel grid).
-template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, int TW, int TH>
+// PREFETCH: the kernel's grid is this view's tiles (bx, by); before the walk the CTA asks
+// L2 for the G-buffer of the tile three CTAs per SM further on, the one likely to start
+// on an SM as the current wave drains, so its set-up loads hit L2.
+template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, int TW, int TH, bool PREFETCH = false>
 __device__ __forceinline__ void shade_tile(
     const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const GBufView& gb,
     const GpuLight* __restrict__ lights, const float4* __restrict__ cand, uint32_t n_lights, const GridView& grid,
@@ -420,6 +423,14 @@ __device__ __forceinline__ void shade_tile(
     for (int k = 0; k < PPT; ++k)
         if (valid[k]) s.order[s.u.sort.hist[key[k]] + slot[k]] = uint16_t(t + k * kThreads);
     __syncthreads();
+
+    if (PREFETCH) {
+        uint32_t nsm;
+        asm("mov.u32 %0, %%nsmid;" : "=r"(nsm));
+        const uint32_t next = by * gridDim.x + bx + 3u * nsm;
+        if (next < gridDim.x * gridDim.y)
+            gbuf::prefetch_tile<LAYOUT>(gb, (next % gridDim.x) * TW, (next / gridDim.x) * TH, TW, TH, t, kThreads);
+    }
 
     // ---- 2-4. groups of 32 sorted pixels walk their lists --------------------------
     const uint32_t n_valid = s.n_valid;
@@ -621,8 +632,8 @@ __global__ void __launch_bounds__(sk::kThreads, 3) shade_kernel(
     const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const GBufView gb,
     const GpuLight* __restrict__ lights, uint32_t n_lights, const GridView grid, const __grid_constant__ SliceTable tab,
     const TargetView out, uint32_t* __restrict__ stats, int* __restrict__ status, const float4* __restrict__ cand) {
-    shade_tile<LAYOUT, GRID, TARGET, STATS, TW, TH>(cam, glb, gb, lights, cand, n_lights, grid, tab.z, out, stats,
-                                                    status, blockIdx.x, blockIdx.y);
+    shade_tile<LAYOUT, GRID, TARGET, STATS, TW, TH, true>(cam, glb, gb, lights, cand, n_lights, grid, tab.z, out,
+                                                          stats, status, blockIdx.x, blockIdx.y);
 }
 
 // Every tile of every view of a batch (froxel grids, 32x16 tiles): CTA b lights tile

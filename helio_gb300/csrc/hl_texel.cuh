@@ -86,5 +86,44 @@ __device__ __forceinline__ Texel<LAYOUT> load_texel(const GBufView& g, uint32_t 
     return t;
 }
 
+// Planes of each layout and their bytes per texel.
+template <uint32_t LAYOUT>
+__host__ __device__ constexpr int plane_count() {
+    return LAYOUT == HL_GBUF_REFERENCE ? 5 : LAYOUT == HL_GBUF_F32 ? 3 : 4;
+}
+template <uint32_t LAYOUT>
+__host__ __device__ constexpr uint32_t plane_bpp(int p) {
+    return LAYOUT == HL_GBUF_REFERENCE ? (p == 1 || p == 3 ? 8u : 4u)
+         : LAYOUT == HL_GBUF_F32       ? (p < 2 ? 16u : 4u)
+                                       : (p == 0 ? 8u : p == 2 ? 2u : 4u);
+}
+
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// Asks L2 for the rows of a w x h pixel block at (x0, y0) of one plane (bpp bytes per
+// pixel): one prefetch per 128-byte step of each row, all inside the block's bytes.
+// Thread t of n takes every n-th (row, step).
+__device__ __forceinline__ void prefetch_block(const unsigned char* plane, uint64_t pitch, uint32_t bpp,
+                                               uint32_t width, uint32_t height, uint32_t x0, uint32_t y0, uint32_t w,
+                                               uint32_t h, uint32_t t, uint32_t n) {
+    if (x0 >= width || y0 >= height) return;
+    const uint32_t xe = min(x0 + w, width), ye = min(y0 + h, height);
+    const uint32_t b0 = x0 * bpp, b1 = xe * bpp;
+    const uint32_t steps = (b1 - b0 + 127u) / 128u + 1u;  // the last step reaches the block's last byte
+    for (uint32_t i = t; i < (ye - y0) * steps; i += n) {
+        const unsigned char* row = plane + pitch * (y0 + i / steps);
+        prefetch_l2(row + min(b0 + 128u * (i % steps), b1 - 1u));
+    }
+}
+
+// The G-buffer rows of a w x h tile at (x0, y0), every plane of the layout.
+template <uint32_t LAYOUT>
+__device__ __forceinline__ void prefetch_tile(const GBufView& g, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h,
+                                              uint32_t t, uint32_t n) {
+#pragma unroll
+    for (int p = 0; p < plane_count<LAYOUT>(); ++p)
+        prefetch_block(g.plane[p], g.pitch[p], plane_bpp<LAYOUT>(p), g.width, g.height, x0, y0, w, h, t, n);
+}
+
 }  // namespace gbuf
 }  // namespace hl
