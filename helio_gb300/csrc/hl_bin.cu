@@ -163,6 +163,7 @@ __global__ void __launch_bounds__(kBinThreads) bin_tiles_ref_kernel(const GpuCam
 // Froxel clustering
 // ----------------------------------------------------------------------------------
 constexpr int kColCap = 4096;  // column-list entries held in shared memory per round
+constexpr uint32_t kGatherU = 4;  // 256-light sub-rounds per gather step
 
 struct ColumnGeom {
     Planes planes;
@@ -239,7 +240,7 @@ __device__ __forceinline__ bool light_meets_froxel(const BinLight& l, const Box&
 
 struct BinSmem {
     uint32_t col[kColCap];
-    uint32_t warp_tot[kBinWarps];
+    uint32_t warp_tot[kGatherU * kBinWarps];
     uint32_t slice_run[kMaxSlices];
 };
 
@@ -369,32 +370,46 @@ __device__ __forceinline__ void st_chain(unsigned long long* p, uint32_t epoch, 
         (static_cast<unsigned long long>(epoch) << 32) | (state << 30) | min(value, kChainValueMax);
 }
 
-// Gathers the next round of a column's candidate lights into sm.col (light-index order).
+// Appends to sm.col, in light-index order, the lights from `base` on that may touch the
+// column (directional, or a sphere not outside its four planes), until the lights run out
+// or the next step could overflow kColCap. A step tests kGatherU x 256 lights, their
+// loads in flight together, with two barriers.
 __device__ __forceinline__ uint32_t gather_round(BinSmem& sm, const ColumnGeom& g, const BinLight* __restrict__ bl,
                                                  uint32_t n, uint32_t& base) {
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t col_len = 0;
     __syncthreads();
-    while (base < n && col_len + kBinThreads <= kColCap) {
-        const uint32_t i = base + threadIdx.x;
-        bool pass = false;
-        if (i < n) {
-            const BinLight l = bl[i];
-            pass = (l.type == 0u) || sphere_in_planes(g.planes, l.cx, l.cy, l.cz, l.r);
-        }
-        const uint32_t mask = __ballot_sync(0xffffffffu, pass);
-        if (lane == 0) sm.warp_tot[warp] = __popc(mask);
-        __syncthreads();
-        uint32_t before = 0, total = 0;
+    while (base < n && col_len + kGatherU * kBinThreads <= kColCap) {
+        bool pass[kGatherU];
+        uint32_t mask[kGatherU];
 #pragma unroll
-        for (int w = 0; w < kBinWarps; ++w) {
-            const uint32_t t = sm.warp_tot[w];
-            before += (uint32_t(w) < warp) ? t : 0u;
-            total += t;
+        for (uint32_t u = 0; u < kGatherU; ++u) {
+            const uint32_t i = base + u * kBinThreads + threadIdx.x;
+            pass[u] = false;
+            if (i < n) {
+                const BinLight l = bl[i];
+                pass[u] = (l.type == 0u) || sphere_in_planes(g.planes, l.cx, l.cy, l.cz, l.r);
+            }
         }
-        if (pass) sm.col[col_len + before + __popc(mask & lanemask_lt())] = i;
-        col_len += total;
-        base += kBinThreads;
+#pragma unroll
+        for (uint32_t u = 0; u < kGatherU; ++u) {
+            mask[u] = __ballot_sync(0xffffffffu, pass[u]);
+            if (lane == 0) sm.warp_tot[u * kBinWarps + warp] = __popc(mask[u]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (uint32_t u = 0; u < kGatherU; ++u) {
+            uint32_t before = 0, total = 0;
+#pragma unroll
+            for (int w = 0; w < kBinWarps; ++w) {
+                const uint32_t t = sm.warp_tot[u * kBinWarps + w];
+                before += (uint32_t(w) < warp) ? t : 0u;
+                total += t;
+            }
+            if (pass[u]) sm.col[col_len + before + __popc(mask[u] & lanemask_lt())] = base + u * kBinThreads + threadIdx.x;
+            col_len += total;
+        }
+        base += kGatherU * kBinThreads;
         __syncthreads();
     }
     return col_len;
