@@ -3,6 +3,7 @@
     python -m helio_gb300.profile_run --workload 1 --frames 3            # bin + shade
     python -m helio_gb300.profile_run --workload 4 --frames 3 --adjoint  # + adjoint
     python -m helio_gb300.profile_run --batched --frames 3              # 98-view plan
+    python -m helio_gb300.profile_run --workload 1 --frames 3 --fragments  # + fragment loop
 
 Every frame launches the same kernels as one bench step (froxel binning: 4 launches,
 shading: 1, adjoint: 2), so ``ncu -k <kernel> -s <n> -c 1`` can pick one warm launch.
@@ -19,6 +20,8 @@ def main(argv=None):
     ap.add_argument("--frames", type=int, default=3)
     ap.add_argument("--adjoint", action="store_true")
     ap.add_argument("--batched", action="store_true")
+    ap.add_argument("--fragments", action="store_true",
+                    help="also light one raster-ordered fragment per pixel (transparent mode)")
     ap.add_argument("--scale", type=float, default=1.0)
     args = ap.parse_args(argv)
 
@@ -63,6 +66,13 @@ def main(argv=None):
         d_rad = torch.randn((H, W, 4), dtype=torch.float32, device="cuda", generator=g)
         d_l = torch.zeros((max(df.n_lights, 1), 7), dtype=torch.float64, device="cuda")
         d_p = torch.zeros((H, W, 5), dtype=torch.float32, device="cuda")
+    if args.fragments:
+        fr = S.make_fragments(w.camera, 11, W * H, raster_order=True)
+        d_fr = FR.bytes_tensor(fr)
+        f_out = torch.zeros((len(fr), 4), dtype=torch.float32, device="cuda")
+        prm = S.fragment_params(L.FRAGMENTS_TRANSPARENT, L.tile_grid(W, H)[0])
+        fpar = N.FragmentParams(int(prm["mode"][0]), int(prm["num_tiles_x"][0]), float(prm["ambient_intensity"][0]),
+                                (N.C.c_float * 3)(*[float(v) for v in prm["ambient_color"][0]]))
     for _ in range(args.frames):
         ev0.record()
         ctx.bin_froxels(df.camera, df.lights, df.n_lights, fp, off, idx, cap)
@@ -70,6 +80,8 @@ def main(argv=None):
         if args.adjoint:
             ctx.shade_adjoint(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, d_rad, W * 16, d_l,
                               d_p)
+        if args.fragments:
+            ctx.shade_fragments(df.camera, fpar, d_fr, len(fr), df.lights, df.n_lights, grid, f_out)
         ev1.record()
     ctx.sync_status()
     print(f"w{args.workload}: {ev0.elapsed_time(ev1) * 1e3:.1f} us per frame", flush=True)
