@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(256) prep_frag_lights_kernel(const GpuLight* _
 }
 
 template <uint32_t MODE, uint32_t GRID>
-__global__ void __launch_bounds__(256) shade_fragments_kernel(
+__global__ void __launch_bounds__(256, 4) shade_fragments_kernel(
     const GpuCamera* __restrict__ cam, const hl_fragment_params prm, const float4* __restrict__ frags, uint32_t n,
     const FragLight* __restrict__ fl, uint32_t n_lights, const GridView grid, const __grid_constant__ SliceTable tab,
     float4* __restrict__ out, int* __restrict__ status) {
