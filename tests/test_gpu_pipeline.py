@@ -102,3 +102,39 @@ def test_dependent_launch_orders(ctx):
         got = run(False)
         for g, w in zip(got, want):
             assert np.array_equal(g, w)
+
+
+def test_frame_replays_in_a_cuda_graph(ctx):
+    """A whole frame (hl_bin_froxels + hl_shade, whose kernels are chained as dependent
+    launches) recorded in a CUDA graph gives the radiance of direct calls on every replay."""
+    import torch
+
+    w = S.workload(1, 0.5)
+    want = _device_radiance(ctx, w)
+    df = FR.upload_workload(w)
+    W, H = w.gbuffer.width, w.gbuffer.height
+    p = N.froxel_params(*w.froxel_grid, W, H, w.camera.far)
+    F = p.grid_x * p.grid_y * p.grid_z
+    cap = F * 64
+    off = torch.zeros(F + 1, dtype=torch.int32, device="cuda")
+    idx = torch.zeros(cap, dtype=torch.int32, device="cuda")
+    out = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    grid, tgt = N.froxel_grid_struct(idx, off, p, cap), N.target_struct(out)
+    s = torch.cuda.Stream()
+
+    def frame():
+        ctx.bin_froxels(df.camera, df.lights, df.n_lights, p, off, idx, cap, s.cuda_stream)
+        ctx.shade(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, tgt, s.cuda_stream)
+
+    with torch.cuda.stream(s):
+        frame()  # scratch allocated outside the capture
+    s.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        frame()
+    for _ in range(3):
+        out.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        ctx.sync_status()
+        assert np.array_equal(out.cpu().numpy(), want)
