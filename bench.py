@@ -595,6 +595,49 @@ def run_forms(ctx, dev, stream, flush, with_oracle=True):
                                              "over_1e-3": int((rel > 1e-3).sum())}
         frag[name] = entry
     forms["fragments"] = frag
+
+    # ---- the same w1 frame into an RGBA16F target (the reference's pre_aa format) ----
+    out32 = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
+    out16 = torch.zeros((H, W, 4), dtype=torch.float16, device=dev)
+    t16 = N.target_struct(out16, N.TARGET_RGBA16F)
+
+    def frame16():
+        ctx.bin_froxels(df.camera, df.lights, df.n_lights, fp, off, idx, cap, sh)
+        ctx.shade(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, t16, sh)
+
+    t_16 = _median_ms(frame16, stream, flush, 50)
+    ctx.shade(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, N.target_struct(out32), sh)
+    ctx.sync_status(sh)
+    a32, a16 = out32[..., :3].double(), out16[..., :3].double()
+    floor = 1e-6 * float(a32.abs().max())  # the error metric's floor of 1e-6 x the image maximum
+    rel16 = ((a16 - a32).abs().amax(-1) / a32.abs().amax(-1).clamp_min(floor)).flatten()
+    pf = FR.PackedFrame(w.camera.record, w.globals_, w.lights, w.gbuffer)
+    pipe = FR.HostFramePipeline(ctx, pf, w.froxel_grid, w.camera.far, capacity=cap, device=dev,
+                                target_format=N.TARGET_RGBA16F)
+    host16 = [torch.empty((H, W, 4), dtype=torch.float16).pin_memory() for _ in range(2)]
+    for k in range(3):
+        pipe.submit(pf, host16[k % 2])
+    pipe.synchronize()
+    s_up, s_comp, s_down = pipe.streams
+    steps16 = 200
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s_up)
+    for k in range(steps16):
+        pipe.submit(pf, host16[k % 2])
+    e1.record(s_down)
+    pipe.synchronize()
+    torch.cuda.synchronize()
+    t_e2e16 = e0.elapsed_time(e1) / steps16
+    forms["pre_aa_rgba16f"] = {
+        "workload": WORKLOAD + ", radiance into an RGBA16F target (the reference's pre_aa format)",
+        "frame_ms": round(t_16, 4), "mpix_s": round(W * H / t_16 / 1e3, 1),
+        "e2e": {"mpix_s": round(W * H / t_e2e16 / 1e3, 1), "steps": steps16, "h2d_bytes_per_step": int(pf.nbytes),
+                "d2h_bytes_per_step": int(host16[0].numel() * host16[0].element_size())},
+        "rel_vs_rgba32f": {"max": float(f"{float(rel16.max()):.3e}"),
+                           "p9999": float(f"{float(torch.quantile(rel16[::16].float(), 0.9999)):.3e}")},
+        "result_matches_device_run": bool(torch.equal(host16[(steps16 - 1) % 2], out16.cpu())),
+    }
     return forms
 
 

@@ -108,14 +108,18 @@ class HostFramePipeline:
     pinned host memory: the upload of frame k+1, the binning and shading of frame k and
     the download of frame k-1 run on three CUDA streams with two device buffer sets, so
     copies overlap the kernels. Every frame still makes its own host->device copy of
-    all its inputs and its own device->host copy of its radiance (RGBA32F). Sky pixels
-    (depth 1) come back as zeros: the device targets are cleared once and shading never
-    writes them."""
+    all its inputs and its own device->host copy of its radiance (RGBA32F, or RGBA16F
+    like the reference's pre_aa target with ``target_format=N.TARGET_RGBA16F``). Sky
+    pixels (depth 1) come back as zeros: the device targets are cleared once and shading
+    never writes them."""
 
-    def __init__(self, ctx: N.Context, like: PackedFrame, froxel_grid, slice_far, capacity=None, device="cuda"):
+    def __init__(self, ctx: N.Context, like: PackedFrame, froxel_grid, slice_far, capacity=None, device="cuda",
+                 target_format=N.TARGET_RGBA32F):
         torch = _torch()
         self.ctx = ctx
         self.like = like
+        self.target_format = target_format
+        self.target_dtype = torch.float32 if target_format == N.TARGET_RGBA32F else torch.float16
         W, H = like.width, like.height
         self.fp = N.froxel_params(*froxel_grid, W, H, slice_far)
         F = froxel_grid[0] * froxel_grid[1] * froxel_grid[2]
@@ -138,11 +142,11 @@ class HostFramePipeline:
                 "offsets": torch.empty(F + 1, dtype=torch.int32, device=device),
                 "indices": torch.empty(self.capacity, dtype=torch.int32, device=device),
                 # cleared once: sky pixels (depth 1) are never written, as in the reference
-                "target": torch.zeros((H, W, 4), dtype=torch.float32, device=device),
+                "target": torch.zeros((H, W, 4), dtype=self.target_dtype, device=device),
                 "up": torch.cuda.Event(), "done": torch.cuda.Event(), "down": torch.cuda.Event(),
             }
             slot["grid"] = N.froxel_grid_struct(slot["indices"], slot["offsets"], self.fp, self.capacity)
-            slot["tgt"] = N.target_struct(slot["target"])
+            slot["tgt"] = N.target_struct(slot["target"], target_format)
             self.slots.append(slot)
         self.s_up, self.s_comp, self.s_down = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
         self.k = 0
@@ -152,8 +156,9 @@ class HostFramePipeline:
         return self.s_up, self.s_comp, self.s_down
 
     def submit(self, frame: PackedFrame, host_out):
-        """Enqueues one frame; ``host_out`` (pinned, H x W x 4 float32) receives its
-        radiance once the download stream has passed this frame."""
+        """Enqueues one frame; ``host_out`` (pinned, H x W x 4, float32 or float16 as the
+        target format) receives its radiance once the download stream has passed this
+        frame."""
         torch = _torch()
         s = self.slots[self.k % 2]
         first = self.k < 2
