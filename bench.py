@@ -638,7 +638,75 @@ def run_forms(ctx, dev, stream, flush, with_oracle=True):
                            "p9999": float(f"{float(torch.quantile(rel16[::16].float(), 0.9999)):.3e}")},
         "result_matches_device_run": bool(torch.equal(host16[(steps16 - 1) % 2], out16.cpu())),
     }
+
+    # ---- the G-buffer pass's fragment stage, and a reference-layout frame it feeds ----
+    forms["gbuffer_write"] = gbuffer_write_form(ctx, dev, stream, flush, w, df, fp, off, idx, cap, grid, with_oracle)
     return forms
+
+
+def gbuffer_write_form(ctx, dev, stream, flush, w, df, fp, off, idx, cap, grid, with_oracle=True):
+    """hl_write_gbuffer over a 1920x1080 material scene (64 materials, 24 textures, all
+    eight targets), and the frame write -> froxel binning -> shading of the written
+    HL_GBUF_REFERENCE G-buffer (28 B/px) with w1's camera and lights. Algorithmic bytes
+    of the write: the 64-byte surface record of every pixel read, 48 bytes of targets
+    per written pixel; material and texture reads (L2-resident tables) not counted."""
+    import torch
+
+    from helio_gb300 import frame as FR
+    from helio_gb300 import native as N
+    from helio_gb300 import synthetic as S
+
+    sh = stream.cuda_stream
+    W, H = w.gbuffer.width, w.gbuffer.height
+    scene = S.material_scene(w.camera, 1001)
+    ds = FR.upload_material_scene(scene, dev)
+    planes, tg = FR.gbuffer_targets(W, H, optional=True, fill=0, device=dev)
+    t_w = _median_ms(lambda: ds.write(ctx, tg, sh), stream, flush, 50)
+    ctx.sync_status(sh)
+    written = (planes[1].view(torch.int16) != 0).any(-1)  # a written normal is a unit vector
+    n_written = int(written.sum())
+    alg = W * H * 64 + n_written * 48
+    hbm_peak, _ = measured_peaks()
+    entry = {"workload": "1920x1080 material scene (64 materials, 24 textures RGBA8 sRGB/unorm, RGBA16F, "
+                         "RGBA32F, 128-512 texels, repeat/clamp/mirror, linear/nearest), 64 B surface records, "
+                         "all eight targets", "pixels": W * H, "written": n_written,
+             "ms": round(t_w, 4), "mpix_s": round(W * H / t_w / 1e3, 1), "algorithmic_bytes": alg,
+             "hbm_frac": round(alg / (t_w / 1e3) / 1e9 / hbm_peak, 4)}
+    if with_oracle:
+        import oracle
+
+        want, wr, _ = oracle.write_gbuffer(scene.globals_, scene.surfaces, scene.materials, scene.material_textures,
+                                           scene.textures)
+        wt = want[wr]
+        host = [p.cpu().numpy() for p in planes]
+        u8_err = max(float(np.abs(host[i][wr].astype(np.float64) - np.clip(wt[:, s], 0, 1) * 255.0).max())
+                     for i, s in ((0, slice(0, 4)), (2, slice(8, 12))))
+        off16 = 0
+        unit = np.array([2e-6, 2e-6, 2e-6, 0.0])  # absolute f32 error of unit-normal components
+        for i, s, fl in ((1, slice(4, 8), unit), (3, slice(12, 16), 0.0), (4, slice(16, 18), 0.0),
+                         (7, slice(18, 20), 0.0)):
+            g, o = host[i][wr].astype(np.float64), wt[:, s]
+            off16 += int((np.abs(g - o) > 2.0 ** -11 * np.maximum(np.abs(o), 2.0 ** -14) + 1e-5 * np.abs(o)
+                          + fl).sum())
+        entry["error_vs_fp64_oracle"] = {"written_mask_equal": bool(np.array_equal(wr, written.cpu().numpy())),
+                                         "unorm8_max_abs_byte_error": round(u8_err, 4),
+                                         "f16_values_beyond_half_ulp": off16}
+    depth = torch.where(written, ds.depth, torch.ones_like(ds.depth))  # discarded fragments write no depth
+    gbs = FR.reference_gbuffer(planes, depth)
+    rad = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
+    tgt = N.target_struct(rad)
+
+    def frame():
+        ds.write(ctx, tg, sh)
+        ctx.bin_froxels(df.camera, df.lights, df.n_lights, fp, off, idx, cap, sh)
+        ctx.shade(df.camera, df.globals_, gbs, df.lights, df.n_lights, grid, tgt, sh)
+
+    t_f = _median_ms(frame, stream, flush, 50)
+    ctx.sync_status(sh)
+    entry["reference_layout_frame"] = {
+        "steps": "hl_write_gbuffer + hl_bin_froxels + hl_shade (HL_GBUF_REFERENCE, 28 B/px), w1 lights",
+        "ms": round(t_f, 4), "mpix_s": round(W * H / t_f / 1e3, 1)}
+    return entry
 
 
 def main():

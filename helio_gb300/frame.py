@@ -72,6 +72,71 @@ def upload_workload(w, device="cuda") -> DeviceFrame:
 
 
 # ----------------------------------------------------------------------------------
+# The G-buffer pass's inputs and targets
+# ----------------------------------------------------------------------------------
+
+
+@dataclass
+class DeviceMaterialScene:
+    """A synthetic.MaterialScene on the device, with the C-ABI texture table."""
+    width: int
+    height: int
+    globals_: object
+    surfaces: object
+    materials: object
+    material_textures: object
+    n_materials: int
+    textures: list
+    texture_table: list
+    depth: object
+
+    @property
+    def surfaces_pitch(self) -> int:
+        return int(self.surfaces.stride(0) * self.surfaces.element_size())
+
+    def write(self, ctx: N.Context, targets: N.GBufferTargets, stream=None):
+        """hl_write_gbuffer of this scene into ``targets``."""
+        ctx.write_gbuffer(self.globals_, self.surfaces, self.surfaces_pitch, self.materials,
+                          self.material_textures, self.n_materials, self.texture_table, targets, stream)
+
+
+def upload_material_scene(scene, device="cuda") -> DeviceMaterialScene:
+    H, W = scene.surfaces.shape
+    srf = bytes_tensor(scene.surfaces, device).view(H, W * L.SURFACE.itemsize)
+    texs = [plane_tensor(t[0], device) for t in scene.textures]
+    table = [N.texture_struct(d, fmt, au, av, flt) for d, (_, fmt, au, av, flt) in zip(texs, scene.textures)]
+    return DeviceMaterialScene(W, H, bytes_tensor(scene.globals_, device), srf, bytes_tensor(scene.materials, device),
+                               bytes_tensor(scene.material_textures, device), len(scene.materials), texs, table,
+                               plane_tensor(scene.depth, device))
+
+
+GBUFFER_TARGET_SHAPES = (("albedo", 4, "u8"), ("normal", 4, "f16"), ("orm", 4, "u8"), ("emissive", 4, "f16"),
+                         ("lightmap_uv", 2, "f16"), ("sss", 4, "f16"), ("extra", 4, "f16"), ("velocity", 2, "f16"))
+
+
+def gbuffer_targets(width: int, height: int, optional: bool = True, fill: int = 0xAB, device="cuda"):
+    """The eight G-buffer targets as device tensors (the optional four None unless
+    ``optional``), every byte set to ``fill``; and the hl_gbuffer_targets struct."""
+    torch = _torch()
+    planes = []
+    for i, (_, ch, kind) in enumerate(GBUFFER_TARGET_SHAPES):
+        if i >= 4 and not optional:
+            planes.append(None)
+            continue
+        nbytes = ch * (1 if kind == "u8" else 2)
+        raw = torch.full((height, width * nbytes), fill, dtype=torch.uint8, device=device)
+        planes.append(raw.view(torch.uint8 if kind == "u8" else torch.float16).view(height, width, ch))
+    return planes, N.gbuffer_targets_struct(width, height, planes)
+
+
+def reference_gbuffer(planes, depth) -> N.GBuffer:
+    """The HL_GBUF_REFERENCE G-buffer formed by the written albedo, normal, orm and
+    emissive targets and the rasteriser's depth."""
+    H, W = int(depth.shape[0]), int(depth.shape[1])
+    return N.gbuffer_struct(N.GBUF_REFERENCE, W, H, [planes[0], planes[1], planes[2], planes[3], depth])
+
+
+# ----------------------------------------------------------------------------------
 # Frames from host memory, pipelined
 # ----------------------------------------------------------------------------------
 

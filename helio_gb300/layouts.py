@@ -157,6 +157,100 @@ FRAGMENT_PARAMS = np.dtype(
 )
 FRAGMENTS_FORWARD, FRAGMENTS_TRANSPARENT = 0, 1
 
+# GBufferGlobals (helio-pass-gbuffer/src/lib.rs:43-56), the uniform of the G-buffer pass
+GBUFFER_GLOBALS = np.dtype(
+    [
+        ("frame", "<u4"),
+        ("delta_time", "<f4"),
+        ("light_count", "<u4"),
+        ("ambient_intensity", "<f4"),
+        ("ambient_color", "<f4", (4,)),
+        ("rc_world_min", "<f4", (4,)),
+        ("rc_world_max", "<f4", (4,)),
+        ("csm_splits", "<f4", (4,)),
+        ("debug_mode", "<u4"),
+        ("screen_width", "<f4"),
+        ("screen_height", "<f4"),
+        ("_pad0", "<u4"),
+    ]
+)
+
+# One texture slot of GpuMaterialTextures (helio/src/material.rs:154-162)
+MATERIAL_TEXTURE_SLOT = np.dtype(
+    [
+        ("texture_index", "<u4"),
+        ("uv_channel", "<u4"),
+        ("_pad", "<u4", (2,)),
+        ("offset_scale", "<f4", (4,)),  # offset.xy, scale.xy
+        ("rotation", "<f4", (4,)),      # sin, cos, 0, 0
+    ]
+)
+
+# GpuMaterialTextures (helio/src/material.rs:176-187); params = (normal_scale,
+# occlusion_strength, alpha_cutoff, 0)
+MATERIAL_TEXTURES = np.dtype(
+    [
+        ("base_color", MATERIAL_TEXTURE_SLOT),
+        ("normal", MATERIAL_TEXTURE_SLOT),
+        ("roughness_metallic", MATERIAL_TEXTURE_SLOT),
+        ("emissive", MATERIAL_TEXTURE_SLOT),
+        ("occlusion", MATERIAL_TEXTURE_SLOT),
+        ("specular_color", MATERIAL_TEXTURE_SLOT),
+        ("specular_weight", MATERIAL_TEXTURE_SLOT),
+        ("params", "<f4", (4,)),
+    ]
+)
+MATERIAL_SLOTS = ("base_color", "normal", "roughness_metallic", "emissive", "occlusion", "specular_color",
+                  "specular_weight")
+NO_TEXTURE = 0xFFFFFFFF
+NO_FRAGMENT = 0xFFFFFFFF
+FLAG_HAS_NORMAL_MAP = 1 << 3  # libhelio/src/material.rs:189
+WORKFLOW_METALLIC, WORKFLOW_SPECULAR = 0, 1
+
+# hl_surface: the interpolated vertex outputs gbuffer.wgsl's fs_main reads (:147-157)
+SURFACE = np.dtype(
+    [
+        ("world_normal", "<f4", (3,)),
+        ("bitangent_sign", "<f4"),
+        ("world_tangent", "<f4", (3,)),
+        ("material_id", "<u4"),
+        ("tex_coords", "<f4", (2,)),
+        ("lightmap_uv", "<f4", (2,)),
+        ("prev_clip", "<f4", (4,)),
+    ]
+)
+
+# hl_texture (include/helio_gb300.h): a texture level 0 and its sampler
+TEXTURE = np.dtype(
+    [
+        ("texels", "<u8"),
+        ("pitch", "<u8"),
+        ("width", "<u4"),
+        ("height", "<u4"),
+        ("format", "<u4"),
+        ("address_u", "<u4"),
+        ("address_v", "<u4"),
+        ("filter", "<u4"),
+    ]
+)
+TEX_RGBA8_UNORM, TEX_RGBA8_SRGB, TEX_RGBA16F, TEX_RGBA32F = 0, 1, 2, 3
+ADDRESS_REPEAT, ADDRESS_CLAMP_TO_EDGE, ADDRESS_MIRROR_REPEAT = 0, 1, 2
+FILTER_NEAREST, FILTER_LINEAR = 0, 1
+
+
+def missing_material_textures(n: int = 1) -> np.ndarray:
+    """``n`` GpuMaterialTextures as GpuMaterialTextures::missing() makes them
+    (helio/src/material.rs:164-200): no textures, identity transforms, params
+    (1, 1, 0.5, 0)."""
+    m = np.zeros(n, MATERIAL_TEXTURES)
+    for slot in MATERIAL_SLOTS:
+        m[slot]["texture_index"] = NO_TEXTURE
+        m[slot]["offset_scale"] = (0.0, 0.0, 1.0, 1.0)
+        m[slot]["rotation"] = (0.0, 1.0, 0.0, 0.0)
+    m["params"] = (1.0, 1.0, 0.5, 0.0)
+    return m
+
+
 # CSM split distances written into DeferredGlobals (libhelio/src/shadow.rs:13)
 CSM_SPLITS = (16.0, 80.0, 300.0, 1400.0)
 
@@ -170,6 +264,11 @@ EXPECTED_SIZES = {
     "FRAGMENT": 80,
     "TRANSFORM": 36,
     "FRAGMENT_PARAMS": 24,
+    "GBUFFER_GLOBALS": 96,
+    "MATERIAL_TEXTURE_SLOT": 48,
+    "MATERIAL_TEXTURES": 352,
+    "SURFACE": 64,
+    "TEXTURE": 40,
 }
 
 for _name, _size in EXPECTED_SIZES.items():

@@ -85,11 +85,30 @@ class FragmentParams(C.Structure):
 
 FRAGMENTS_FORWARD, FRAGMENTS_TRANSPARENT = 0, 1
 
+GBUFFER_TARGETS = 8
+MAX_MATERIAL_TEXTURES = 256
+
+
+class Texture(C.Structure):
+    """hl_texture: a texture's level 0 (device texels) and its sampler."""
+    _fields_ = [("texels", C.c_void_p), ("pitch", C.c_uint64), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("format", C.c_uint32), ("address_u", C.c_uint32), ("address_v", C.c_uint32),
+                ("filter", C.c_uint32)]
+
+
+class GBufferTargets(C.Structure):
+    """hl_gbuffer_targets: albedo, normal, orm, emissive (required), lightmap_uv, sss,
+    extra, velocity (optional)."""
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("reserved", C.c_uint32 * 2),
+                ("planes", C.c_void_p * GBUFFER_TARGETS), ("pitch", C.c_uint64 * GBUFFER_TARGETS)]
+
+
 EXPORTS = [
     "hl_abi_version", "hl_status_string", "hl_create", "hl_destroy", "hl_last_error_message", "hl_sync_status",
     "hl_tile_count", "hl_bin_tiles_ref", "hl_froxel_slice_table", "hl_bin_froxels", "hl_shade", "hl_shade_stats",
     "hl_shade_adjoint", "hl_batch_plan_create", "hl_batch_execute", "hl_batch_plan_view_grid",
     "hl_batch_plan_destroy", "hl_probe_fp32_peak", "hl_bin_froxels_noalloc", "hl_shade_fragments",
+    "hl_write_gbuffer",
 ]
 
 _lock = threading.Lock()
@@ -158,6 +177,8 @@ def _bind(l):
     l.hl_bin_froxels_noalloc.restype = i32
     l.hl_shade_fragments.argtypes = [vp, vp, P(FragmentParams), vp, u32, vp, u32, vp, vp, u32, P(LightGrid), vp, vp]
     l.hl_shade_fragments.restype = i32
+    l.hl_write_gbuffer.argtypes = [vp, vp, vp, C.c_uint64, vp, vp, u32, P(Texture), u32, P(GBufferTargets), vp]
+    l.hl_write_gbuffer.restype = i32
 
 
 def status_string(status: int) -> str:
@@ -290,6 +311,14 @@ class Context:
                                                n_transforms, C.byref(grid), _ptr(out_rgba), _stream(stream)),
                     "hl_shade_fragments")
 
+    def write_gbuffer(self, globals_, surfaces, surfaces_pitch, materials, material_textures, n_materials,
+                      textures, targets: "GBufferTargets", stream=None):
+        """G-buffer pass fragment stage; ``textures`` is a list of ``Texture``."""
+        arr = (Texture * max(1, len(textures)))(*textures)
+        self._check(self._l.hl_write_gbuffer(self._h, _ptr(globals_), _ptr(surfaces), int(surfaces_pitch),
+                                             _ptr(materials), _ptr(material_textures), n_materials, arr,
+                                             len(textures), C.byref(targets), _stream(stream)), "hl_write_gbuffer")
+
     def batch_plan(self, views, lights, n_lights, globals_, grid=None, autotune=False, cache_path=None,
                    stream=None) -> "BatchPlan":
         """Plan lighting every view of ``views`` (a list of ``View``) with one light buffer:
@@ -366,6 +395,29 @@ def target_struct(data, fmt: int = TARGET_RGBA32F, pitch: int | None = None) -> 
     t.data = _ptr(data)
     t.pitch = int(pitch if pitch is not None else data.stride(0) * data.element_size())
     t.format = fmt
+    return t
+
+
+def texture_struct(texels, fmt: int, address_u: int = 0, address_v: int = 0, filt: int = 1) -> Texture:
+    """``texels``: a device tensor of shape (h, w, 4) (uint8, float16 or float32)."""
+    t = Texture()
+    t.texels = _ptr(texels)
+    t.pitch = int(texels.stride(0) * texels.element_size())
+    t.height, t.width = int(texels.shape[0]), int(texels.shape[1])
+    t.format, t.address_u, t.address_v, t.filter = fmt, address_u, address_v, filt
+    return t
+
+
+def gbuffer_targets_struct(width: int, height: int, planes) -> GBufferTargets:
+    """``planes``: 8 device tensors or None (albedo, normal, orm, emissive, lightmap_uv,
+    sss, extra, velocity); pitches are the tensors' row strides in bytes."""
+    t = GBufferTargets()
+    t.width, t.height = width, height
+    for i, pl in enumerate(planes):
+        if pl is None:
+            continue
+        t.planes[i] = _ptr(pl)
+        t.pitch[i] = int(pl.stride(0) * pl.element_size())
     return t
 
 

@@ -4,6 +4,7 @@
     python -m helio_gb300.profile_run --workload 4 --frames 3 --adjoint  # + adjoint
     python -m helio_gb300.profile_run --batched --frames 3              # 98-view plan
     python -m helio_gb300.profile_run --workload 1 --frames 3 --fragments  # + fragment loop
+    python -m helio_gb300.profile_run --gbuffer-write --frames 3        # G-buffer pass only
 
 Every frame launches the same kernels as one bench step (froxel binning: 4 launches,
 shading: 1, adjoint: 2), so ``ncu -k <kernel> -s <n> -c 1`` can pick one warm launch.
@@ -22,6 +23,8 @@ def main(argv=None):
     ap.add_argument("--batched", action="store_true")
     ap.add_argument("--fragments", action="store_true",
                     help="also light one raster-ordered fragment per pixel (transparent mode)")
+    ap.add_argument("--gbuffer-write", action="store_true",
+                    help="only the G-buffer pass: hl_write_gbuffer over the bench's 1080p material scene")
     ap.add_argument("--scale", type=float, default=1.0)
     args = ap.parse_args(argv)
 
@@ -34,6 +37,17 @@ def main(argv=None):
 
     ctx = N.Context(0)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if args.gbuffer_write:
+        cam = S.default_camera(max(16, int(1920 * args.scale)), max(16, int(1080 * args.scale)))
+        ds = FR.upload_material_scene(S.material_scene(cam, 1001))
+        _, tg = FR.gbuffer_targets(cam.width, cam.height, optional=True, fill=0)
+        for _ in range(args.frames):
+            ev0.record()
+            ds.write(ctx, tg)
+            ev1.record()
+        ctx.sync_status()
+        print(f"G-buffer write {cam.width}x{cam.height}: {ev0.elapsed_time(ev1) * 1e3:.1f} us per frame", flush=True)
+        return
     if args.batched:
         views, lights = S.batched_views(args.scale)
         glb = L.make_globals(1, len(lights), ambient_color=(0.4, 0.45, 0.5), ambient_intensity=0.3)

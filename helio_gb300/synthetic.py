@@ -451,3 +451,150 @@ def fragment_params(mode: int, num_tiles_x: int, ambient_intensity: float = 0.4,
     p["mode"], p["num_tiles_x"] = mode, num_tiles_x
     p["ambient_intensity"], p["ambient_color"] = ambient_intensity, ambient_color
     return p
+
+
+# ----------------------------------------------------------------------------------
+# Material scenes: the inputs of the G-buffer pass's fragment stage
+# ----------------------------------------------------------------------------------
+
+
+@dataclass
+class MaterialScene:
+    """Inputs of hl_write_gbuffer for one view: per-pixel SURFACE records (the
+    rasteriser's interpolated vertex outputs), GpuMaterial / GpuMaterialTextures tables,
+    textures as (texels[h, w, 4], format, address_u, address_v, filter), the pass's
+    GBufferGlobals and the depth the rasteriser wrote (1.0 where nothing is covered)."""
+    camera: Camera
+    surfaces: np.ndarray
+    materials: np.ndarray
+    material_textures: np.ndarray
+    textures: list
+    globals_: np.ndarray
+    depth: np.ndarray
+
+    @property
+    def covered(self) -> np.ndarray:
+        return self.surfaces["material_id"] != L.NO_FRAGMENT
+
+
+def _texture(seed: int, stream: int, kind: str, size: int, fmt: int):
+    n = size * size
+    u = lambda k, lo=0.0, hi=1.0: uniform(seed, stream * 16 + k, n, lo, hi).reshape(size, size)
+    yy, xx = np.meshgrid(np.arange(size) / size, np.arange(size) / size, indexing="ij")
+    if kind == "normal":  # tangent-space normal map, z dominant, encoded n*0.5+0.5
+        tx = 0.35 * np.sin(2 * math.pi * (3 * xx + u(0) * 0.1))
+        ty = 0.35 * np.cos(2 * math.pi * (2 * yy + u(1) * 0.1))
+        tz = np.sqrt(np.maximum(1.0 - tx * tx - ty * ty, 0.0))
+        v = np.stack([tx * 0.5 + 0.5, ty * 0.5 + 0.5, tz * 0.5 + 0.5, np.ones_like(tx)], -1)
+    else:  # smooth pattern plus noise, channels independent
+        ch = [0.5 + 0.35 * np.sin(2 * math.pi * ((k + 1) * xx + (3 - k) * yy)) + 0.15 * (u(k) - 0.5) for k in range(4)]
+        v = np.stack(ch, -1)
+        if kind == "base" and stream % 2 == 0:  # opaque colour texture; the others are cut-outs
+            v[..., 3] = 1.0
+        if kind == "emissive":
+            v = v * 2.0
+    if fmt in (L.TEX_RGBA8_UNORM, L.TEX_RGBA8_SRGB):
+        return np.clip(np.rint(np.clip(v, 0, 1) * 255.0), 0, 255).astype(np.uint8)
+    return v.astype(np.float16 if fmt == L.TEX_RGBA16F else np.float32)
+
+
+def material_scene(cam: Camera, seed: int, n_materials: int = 64, n_textures: int = 24, block: int = 48,
+                   uncovered: float = 0.03, debug_mode: int = 0) -> MaterialScene:
+    """A seeded scene for the G-buffer pass: pixels in ``block`` x ``block`` squares
+    share a material; UVs vary smoothly (1 to 3 repeats across the view, so textures
+    are magnified or 1:1); about ``uncovered`` of the pixels are not covered by any
+    fragment. Textures: base colours sRGB RGBA8, normal maps and ORM maps RGBA8 unorm,
+    emissive RGBA16F, some RGBA32F; sizes 128-512; mostly repeat and linear, some
+    clamp-to-edge, mirrored-repeat and nearest. Materials: 80 % metallic workflow,
+    60 % with a normal map, about a quarter with base alpha below 1 (some discarded by
+    the 0.5 cutoff), some emissive."""
+    W, H = cam.width, cam.height
+    n = W * H
+    depth, N, _, _, _ = _surface(cam, seed)
+    r = lambda k, lo=0.0, hi=1.0, m=n: uniform(seed, 100 + k, m, lo, hi)
+
+    # textures
+    kinds = ["base", "normal", "orm", "emissive", "orm"]
+    textures = []
+    for t in range(n_textures):
+        kind = kinds[t % len(kinds)]
+        fmt = {"base": L.TEX_RGBA8_SRGB, "normal": L.TEX_RGBA8_UNORM, "orm": L.TEX_RGBA8_UNORM,
+               "emissive": L.TEX_RGBA16F}[kind]
+        if kind == "orm" and t % 3 == 0:
+            fmt = L.TEX_RGBA32F
+        size = (128, 256, 512)[t % 3]
+        au = (L.ADDRESS_REPEAT, L.ADDRESS_REPEAT, L.ADDRESS_CLAMP_TO_EDGE, L.ADDRESS_MIRROR_REPEAT)[t % 4]
+        av = (L.ADDRESS_REPEAT, L.ADDRESS_MIRROR_REPEAT, L.ADDRESS_REPEAT)[t % 3]
+        filt = L.FILTER_NEAREST if t % 7 == 3 else L.FILTER_LINEAR
+        textures.append((_texture(seed, 20 + t, kind, size, fmt), fmt, au, av, filt))
+    by_kind = {k: [i for i in range(n_textures) if kinds[i % len(kinds)] == k] for k in set(kinds)}
+
+    # materials
+    M = n_materials
+    mats = np.zeros(M, L.GPU_MATERIAL)
+    alpha = np.where(r(1, m=M) < 0.25, r(2, 0.3, 1.0, M), 1.0)
+    mats["base_color"] = np.stack([r(3, 0.2, 1.0, M), r(4, 0.2, 1.0, M), r(5, 0.2, 1.0, M), alpha], 1)
+    emissive_w = np.where(r(6, m=M) < 0.2, r(7, 0.0, 4.0, M), 0.0)
+    mats["emissive"] = np.stack([r(8, m=M), r(9, m=M), r(10, m=M), emissive_w], 1)
+    mats["roughness_metallic"] = np.stack([r(11, 0.05, 1.0, M), (r(12, m=M) < 0.3) * r(13, 0.5, 1.0, M),
+                                           r(14, 1.3, 1.8, M), r(15, m=M)], 1)
+    for f in ("tex_base_color", "tex_normal", "tex_roughness", "tex_emissive", "tex_occlusion"):
+        mats[f] = L.NO_TEXTURE
+    mats["workflow"] = np.where(r(16, m=M) < 0.2, L.WORKFLOW_SPECULAR, L.WORKFLOW_METALLIC)
+    mats["flags"] = np.where(r(17, m=M) < 0.6, L.FLAG_HAS_NORMAL_MAP, 0)
+    mtex = L.missing_material_textures(M)
+    pick = lambda k, pool, i: pool[int(r(30 + k, m=M)[i] * len(pool)) % len(pool)]
+    for i in range(M):
+        want = {"base_color": (0.8, "base"), "normal": (0.9 if mats["flags"][i] else 0.2, "normal"),
+                "roughness_metallic": (0.7, "orm"), "emissive": (0.3, "emissive"), "occlusion": (0.5, "orm"),
+                "specular_color": (0.6, "base"), "specular_weight": (0.6, "orm")}
+        for k, (slot, (p, kind)) in enumerate(want.items()):
+            if r(40 + k, m=M)[i] >= p or not by_kind.get(kind):
+                continue
+            s = mtex[slot][i]
+            s["texture_index"] = pick(k, by_kind[kind], i)
+            s["offset_scale"] = (r(50 + k, -1, 1, M)[i], r(60 + k, -1, 1, M)[i], r(70 + k, 0.5, 2, M)[i],
+                                 r(80 + k, 0.5, 2, M)[i])
+            ang = r(90 + k, 0, 2 * math.pi, M)[i] if r(97, m=M)[i] < 0.3 else 0.0
+            s["rotation"] = (math.sin(ang), math.cos(ang), 0.0, 0.0)
+            mtex[slot][i] = s
+    mtex["params"] = np.stack([r(18, 0.5, 1.5, M), r(19, m=M), np.where(r(20, m=M) < 0.8, 0.5, 0.0), np.zeros(M)], 1)
+
+    # per-pixel surfaces
+    ys, xs = np.divmod(np.arange(n), W)
+    bw = (W + block - 1) // block
+    blk = (ys // block) * bw + xs // block
+    nb = int(blk.max()) + 1
+    mid = (uniform(seed, 200, nb) * M).astype(np.uint32)[blk]
+    hole = r(21) < uncovered
+    mid[hole] = L.NO_FRAGMENT
+    srf = np.zeros(n, L.SURFACE)
+    Nf = N.reshape(n, 3) * r(22, 0.8, 1.2)[:, None]  # interpolated normals are not unit length
+    T0 = np.stack([r(23, -1, 1), r(24, -1, 1), r(25, -1, 1)], 1)
+    srf["world_normal"] = Nf
+    srf["bitangent_sign"] = np.where(r(26) < 0.5, -1.0, 1.0)
+    srf["world_tangent"] = T0
+    srf["material_id"] = mid
+    rep = uniform(seed, 201, nb, 1.0, 3.0)[blk]
+    off_u, off_v = uniform(seed, 202, nb, -1, 1)[blk], uniform(seed, 203, nb, -1, 1)[blk]
+    srf["tex_coords"] = np.stack([(xs + 0.5) / W * rep + off_u, (ys + 0.5) / H * rep + off_v], 1)
+    lm = np.where((mid % 2 == 0)[:, None], np.stack([r(27), r(28)], 1), -1.0)
+    srf["lightmap_uv"] = lm
+    d = depth.reshape(n).astype(np.float64)
+    ndc_x = (xs + 0.5) / W * 2 - 1
+    ndc_y = 1 - (ys + 0.5) / H * 2
+    near, far = cam.near, cam.far
+    w_clip = near * far / (far - d * (far - near))  # view depth of the stored NDC depth
+    px, py = ndc_x + r(29, -0.01, 0.01), ndc_y + r(30, -0.01, 0.01)
+    srf["prev_clip"] = np.stack([px * w_clip, py * w_clip, d * w_clip, w_clip], 1)
+    depth = np.where(hole.reshape(H, W), np.float32(1.0), depth).astype(np.float32)
+
+    glb = np.zeros(1, L.GBUFFER_GLOBALS)
+    glb["ambient_color"] = (0.1, 0.1, 0.15, 1.0)
+    glb["ambient_intensity"] = 0.1
+    glb["rc_world_min"] = (-100.0,) * 4
+    glb["rc_world_max"] = (100.0,) * 4
+    glb["csm_splits"] = L.CSM_SPLITS
+    glb["debug_mode"] = debug_mode
+    glb["screen_width"], glb["screen_height"] = float(W), float(H)
+    return MaterialScene(cam, srf.reshape(H, W), mats, mtex, textures, glb, depth)

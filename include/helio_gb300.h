@@ -330,6 +330,95 @@ hl_status hl_shade_fragments(hl_ctx* ctx, const void* camera, const hl_fragment_
                              const hl_light_grid* grid, float* out_rgba, void* stream);
 
 /* ---------------------------------------------------------------------------------
+ * G-buffer write — the fragment stage of the reference's GBufferPass
+ * -------------------------------------------------------------------------------*/
+
+#define HL_SIZEOF_GBUFFER_GLOBALS 96u    /* GBufferGlobals, helio-pass-gbuffer/src/lib.rs:43-56 */
+#define HL_SIZEOF_MATERIAL_TEXTURES 352u /* GpuMaterialTextures, helio/src/material.rs:178-187  */
+#define HL_MAX_MATERIAL_TEXTURES 256u    /* libhelio/src/material.rs:12                         */
+#define HL_NO_TEXTURE 0xFFFFFFFFu        /* GpuMaterial::NO_TEXTURE                             */
+#define HL_NO_FRAGMENT 0xFFFFFFFFu       /* hl_surface.material_id of a pixel nothing covers    */
+
+/* The interpolated vertex outputs gbuffer.wgsl's fs_main reads for one pixel
+ * (VertexOutput, gbuffer.wgsl:147-157), 64 bytes, records 16-byte aligned, one per
+ * pixel in row-major order (row pitch = `surfaces_pitch` bytes). */
+typedef struct hl_surface {
+    float world_normal[3];   /* interpolated, not normalised                          */
+    float bitangent_sign;
+    float world_tangent[3];  /* interpolated, not normalised                          */
+    uint32_t material_id;    /* index into materials; HL_NO_FRAGMENT: pixel untouched */
+    float tex_coords[2];     /* UV0                                                   */
+    float lightmap_uv[2];    /* already mapped into the atlas, or (-1,-1)             */
+    float prev_clip[4];      /* previous frame's clip position (velocity)             */
+} hl_surface;
+
+#define HL_TEX_RGBA8_UNORM 0u
+#define HL_TEX_RGBA8_SRGB 1u /* decoded to linear per texel before filtering */
+#define HL_TEX_RGBA16F 2u
+#define HL_TEX_RGBA32F 3u
+#define HL_ADDRESS_REPEAT 0u
+#define HL_ADDRESS_CLAMP_TO_EDGE 1u
+#define HL_ADDRESS_MIRROR_REPEAT 2u
+#define HL_FILTER_NEAREST 0u
+#define HL_FILTER_LINEAR 1u
+
+/* One entry of the material texture table: a texture's level 0 and its sampler
+ * (helio/src/material.rs:11-31 TextureSamplerDesc, :34-41 TextureUpload). */
+typedef struct hl_texture {
+    const void* texels;     /* device, row-major, aligned to the texel size        */
+    uint64_t pitch;         /* row pitch in bytes                                  */
+    uint32_t width, height; /* 1..16384                                            */
+    uint32_t format;        /* HL_TEX_*                                            */
+    uint32_t address_u;     /* HL_ADDRESS_*                                        */
+    uint32_t address_v;
+    uint32_t filter;        /* HL_FILTER_*: magnification and minification filter  */
+} hl_texture;
+
+/* The G-buffer targets the pass writes (helio-pass-gbuffer/src/lib.rs:236-282).
+ * planes 0-3 are required, 4-7 optional (NULL: not written):
+ *   0 albedo RGBA8 unorm   1 normal RGBA16F   2 orm RGBA8 unorm   3 emissive RGBA16F
+ *   4 lightmap_uv RG16F    5 sss RGBA16F      6 extra RGBA16F     7 velocity RG16F
+ * Planes 0-3 with the caller's depth plane form an HL_GBUF_REFERENCE G-buffer. */
+#define HL_GBUFFER_TARGETS 8
+typedef struct hl_gbuffer_targets {
+    uint32_t width, height;
+    uint32_t reserved[2];
+    void* planes[HL_GBUFFER_TARGETS];     /* device */
+    uint64_t pitch[HL_GBUFFER_TARGETS];   /* row pitch in bytes */
+} hl_gbuffer_targets;
+
+/* Writes the G-buffer of every covered pixel as fs_main of gbuffer.wgsl:425-497 does
+ * under the default PBR template (default_pbr_surface, :333-364; resolve_specular_f0,
+ * :308-329; select_uv / sample_texture, :287-306; compute_velocity, :417-423):
+ *   albedo   = (material.base_color * base_colour sample).rgb, alpha
+ *   normal   = (N, F0.r)   N = normalize(world_normal), normal-mapped when the
+ *                          material has FLAG_HAS_NORMAL_MAP (1<<3) and a normal texture
+ *   orm      = (ao, roughness, metallic, F0.g)    emissive = (emissive, F0.b)
+ *   lightmap_uv passed through; sss = 0; extra = 0 (the default template's values);
+ *   velocity = (x+0.5, y+0.5) - previous pixel position from prev_clip.
+ * Pixels whose alpha <= 0.001 or below the material's alpha cutoff are discarded (all
+ * targets untouched), as are pixels with material_id == HL_NO_FRAGMENT. globals'
+ * debug_mode 1 (UVs), 2 (base texture) and 3 (geometry normals) write the debug
+ * outputs of :443-489. Textures are sampled at level 0 (the level a magnified or 1:1
+ * texel footprint selects); bilinear weights are exact in f32. Colour targets clamp to
+ * [0,1] and round to nearest (RGBA8), or round to nearest even (RGBA16F).
+ *   globals           : device GBufferGlobals (96 B; debug_mode at byte 80)
+ *   surfaces          : device hl_surface[height rows of surfaces_pitch bytes]
+ *   materials         : device GpuMaterial[n_materials] (96 B each)
+ *   material_textures : device GpuMaterialTextures[n_materials] (352 B each)
+ *   textures          : HOST array of n_textures <= HL_MAX_MATERIAL_TEXTURES entries;
+ *                       slots index it by texture_index
+ * A material_id >= n_materials (pixel untouched) or a texture_index >= n_textures (the
+ * slot's fallback value used) is reported through hl_sync_status as
+ * HL_ERR_DEVICE_BOUNDS. Replaces: GBufferPass's fragment stage (gbuffer.wgsl:425-497;
+ * the rasteriser that produces the surfaces and the depth stays the caller's). */
+hl_status hl_write_gbuffer(hl_ctx* ctx, const void* globals, const hl_surface* surfaces,
+                           uint64_t surfaces_pitch, const void* materials,
+                           const void* material_textures, uint32_t n_materials,
+                           const hl_texture* textures, uint32_t n_textures,
+                           const hl_gbuffer_targets* targets, void* stream);
+
+/* ---------------------------------------------------------------------------------
  * Batched views (no reference counterpart)
  * -------------------------------------------------------------------------------*/
 

@@ -22,7 +22,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 BUILD_DIR = HERE / "_build"
 LIB_PATH = BUILD_DIR / "liboracle.so"
-SOURCES = [HERE / "oracle.cpp"]
+SOURCES = [HERE / "oracle.cpp", HERE / "gbuffer_write.cpp"]
 
 _lock = threading.Lock()
 _lib = None
@@ -68,6 +68,7 @@ def _bind(l):
     l.oracle_shade_fragments_f64.argtypes = frag_args
     l.oracle_shade_fragments_f32.argtypes = frag_args
     l.oracle_light_dir_from_rotation.argtypes = [f32p, f64p]
+    l.oracle_write_gbuffer.argtypes = [vp, vp, C.c_uint64, vp, vp, u32, vp, u32, u32, u32, f64p, vp, vp]
     l.oracle_set_threads.argtypes = [C.c_int]
     l.oracle_num_threads.restype = C.c_int
     return l
@@ -212,3 +213,33 @@ def shade_adjoint(camera_rec, globals_rec, gb, lights, grid, weights):
                                    _ptr(lists), _ptr(counts), _ptr(params) if params is not None else None, _ptr(w),
                                    _ptr(dl), _ptr(dp))
     return dl, dp
+
+
+# ----------------------------------------------------------------------------------
+# G-buffer write (gbuffer.wgsl fs_main, default PBR template)
+# ----------------------------------------------------------------------------------
+
+
+def write_gbuffer(globals_rec, surfaces, materials, material_textures, textures):
+    """f64 G-buffer values before quantisation, per pixel: (values[H,W,20], written[H,W],
+    bounds). values: albedo 0-3, normal 4-7, orm 8-11, emissive 12-15, lightmap_uv
+    16-17, velocity 18-19. ``surfaces``: (H, W) array of SURFACE records;
+    ``textures``: list of (texels ndarray [h, w, 4], format, address_u, address_v,
+    filter)."""
+    from helio_gb300 import layouts as L
+
+    srf = np.ascontiguousarray(surfaces)
+    H, W = srf.shape
+    keep = [np.ascontiguousarray(t[0]) for t in textures]
+    desc = np.zeros(max(1, len(textures)), L.TEXTURE)
+    for i, (t, (_, fmt, au, av, flt)) in enumerate(zip(keep, textures)):
+        desc[i] = (t.ctypes.data, t.strides[0], t.shape[1], t.shape[0], fmt, au, av, flt)
+    mats = np.ascontiguousarray(materials)
+    mtex = np.ascontiguousarray(material_textures)
+    out = np.zeros((H, W, 20), np.float64)
+    written = np.zeros((H, W), np.uint8)
+    bounds = np.zeros(1, np.int32)
+    lib().oracle_write_gbuffer(_ptr(np.ascontiguousarray(globals_rec)), _ptr(srf), srf.strides[0],
+                               _ptr(mats) if len(mats) else None, _ptr(mtex) if len(mtex) else None, len(mats),
+                               _ptr(desc), len(textures), W, H, _ptr(out), _ptr(written), _ptr(bounds))
+    return out, written.astype(bool), bool(bounds[0])

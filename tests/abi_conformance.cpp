@@ -355,8 +355,66 @@ void gpu_checks() {
     check(same, "batched view = single-view radiance");
     check(hl_batch_plan_destroy(plan) == HL_OK, "hl_batch_plan_destroy");
 
+    // ---- G-buffer write: one untextured metallic material over a 32x32 target ----
+    // GpuMaterial (96 B): base_color, emissive, roughness_metallic, 5 texture ids, workflow,
+    // flags, class; GpuMaterialTextures (352 B): 7 slots of 48 B (texture_index first),
+    // then params (normal_scale, occlusion_strength, alpha_cutoff, -).
+    unsigned char mat[96] = {}, mtex[352] = {}, gglb[HL_SIZEOF_GBUFFER_GLOBALS] = {};
+    const float mf[12] = {0.6f, 0.4f, 0.2f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.5f, 1.0f, 1.5f, 0.5f};
+    std::memcpy(mat, mf, sizeof mf);
+    const uint32_t no_tex = HL_NO_TEXTURE;
+    for (int s = 0; s < 7; ++s) std::memcpy(mtex + 48 * s, &no_tex, 4);
+    const float prm[4] = {1.0f, 1.0f, 0.5f, 0.0f};
+    std::memcpy(mtex + 336, prm, sizeof prm);
+    std::vector<hl_surface> srf(W * H);
+    for (auto& s : srf) {
+        s = hl_surface{{0.0f, 0.0f, 3.0f}, 1.0f, {1.0f, 0.0f, 0.0f}, 0u, {0.5f, 0.5f}, {-1.0f, -1.0f},
+                       {0.0f, 0.0f, 0.5f, 1.0f}};
+    }
+    srf[5].material_id = HL_NO_FRAGMENT;
+    void *d_mat, *d_mtex, *d_gglb, *d_srf, *d_t[4];
+    check_cuda(cudaMalloc(&d_mat, sizeof mat), "cudaMalloc material");
+    check_cuda(cudaMalloc(&d_mtex, sizeof mtex), "cudaMalloc material textures");
+    check_cuda(cudaMalloc(&d_gglb, sizeof gglb), "cudaMalloc G-buffer globals");
+    check_cuda(cudaMalloc(&d_srf, W * H * sizeof(hl_surface)), "cudaMalloc surfaces");
+    check_cuda(cudaMemcpy(d_mat, mat, sizeof mat, cudaMemcpyHostToDevice), "copy material");
+    check_cuda(cudaMemcpy(d_mtex, mtex, sizeof mtex, cudaMemcpyHostToDevice), "copy material textures");
+    check_cuda(cudaMemcpy(d_gglb, gglb, sizeof gglb, cudaMemcpyHostToDevice), "copy G-buffer globals");
+    check_cuda(cudaMemcpy(d_srf, srf.data(), W * H * sizeof(hl_surface), cudaMemcpyHostToDevice), "copy surfaces");
+    const uint32_t bpp[4] = {4, 8, 4, 8};
+    hl_gbuffer_targets tg;
+    std::memset(&tg, 0, sizeof tg);
+    tg.width = W;
+    tg.height = H;
+    for (int i = 0; i < 4; ++i) {
+        check_cuda(cudaMalloc(&d_t[i], W * H * bpp[i]), "cudaMalloc G-buffer target");
+        check_cuda(cudaMemset(d_t[i], 0xAB, W * H * bpp[i]), "fill G-buffer target");
+        tg.planes[i] = d_t[i];
+        tg.pitch[i] = uint64_t(W) * bpp[i];
+    }
+    hl_gbuffer_targets bad_tg = tg;
+    bad_tg.planes[1] = nullptr;
+    check(hl_write_gbuffer(ctx, d_gglb, static_cast<const hl_surface*>(d_srf), W * sizeof(hl_surface), d_mat,
+                           d_mtex, 1, nullptr, 0, &bad_tg, nullptr) == HL_ERR_INVALID_ARGUMENT,
+          "hl_write_gbuffer rejects a missing normal target");
+    check(hl_write_gbuffer(ctx, d_gglb, static_cast<const hl_surface*>(d_srf), W * sizeof(hl_surface), d_mat,
+                           d_mtex, 1, nullptr, 0, &tg, nullptr) == HL_OK,
+          "hl_write_gbuffer");
+    check(hl_sync_status(ctx, nullptr) == HL_OK, "sync after hl_write_gbuffer");
+    std::vector<uint32_t> alb(W * H);
+    check_cuda(cudaMemcpy(alb.data(), d_t[0], W * H * 4, cudaMemcpyDeviceToHost), "read albedo");
+    // round(255 * (0.6, 0.4, 0.2, 1.0)) = (153, 102, 51, 255)
+    check(alb[0] == (153u | 102u << 8 | 51u << 16 | 255u << 24), "albedo = RGBA8 of the base colour");
+    check(alb[5] == 0xABABABABu, "an uncovered pixel is left untouched");
+    std::vector<uint16_t> nrm(W * H * 4);
+    check_cuda(cudaMemcpy(nrm.data(), d_t[1], W * H * 8, cudaMemcpyDeviceToHost), "read normal");
+    // normal (0, 0, 1) in f16 and F0.r = 0.6 (metallic 1): 0x0000 0x0000 0x3C00, 0x38CD
+    check(nrm[0] == 0 && nrm[1] == 0 && nrm[2] == 0x3C00 && nrm[3] == 0x38CD,
+          "normal = normalize(world_normal), F0.r = albedo at metallic 1");
+
     for (void* p : {d_cam, d_light, d_glb, static_cast<void*>(d_lists), static_cast<void*>(d_counts), g0, g1, g2,
-                    d_out, static_cast<void*>(d_off), static_cast<void*>(d_idx), d_out2, d_w, d_dl, d_dp, d_out3})
+                    d_out, static_cast<void*>(d_off), static_cast<void*>(d_idx), d_out2, d_w, d_dl, d_dp, d_out3,
+                    d_mat, d_mtex, d_gglb, d_srf, d_t[0], d_t[1], d_t[2], d_t[3]})
         cudaFree(p);
     check(hl_destroy(ctx) == HL_OK, "hl_destroy");
 }
