@@ -174,11 +174,9 @@ __device__ __forceinline__ float4 sample_tex(const TexDev& t, float u, float v, 
     }
 }
 
-// sample_texture (gbuffer.wgsl:300-306) with select_uv (:287-297). Out of line: one
-// copy of the sampler serves every slot, which keeps the kernel within the instruction
-// cache.
-__device__ __noinline__ float4 sample_slot(const TexDev* tex, uint32_t n_tex, int* status, const float* srgb255,
-                                           const unsigned char* slot, float u, float v, float4 fallback) {
+// sample_texture (gbuffer.wgsl:300-306) with select_uv (:287-297).
+__device__ __forceinline__ float4 sample_slot(const TexDev* tex, uint32_t n_tex, int* status, const float* srgb255,
+                                              const unsigned char* slot, float u, float v, float4 fallback) {
     const uint32_t idx = ldgu(slot);
     if (idx == HL_NO_TEXTURE) return fallback;
     if (idx >= n_tex) {
@@ -230,6 +228,7 @@ __device__ __forceinline__ void store_targets(const GbwParams& p, uint32_t x, ui
 __global__ void __launch_bounds__(kGbwThreadsX * kGbwThreadsY, 4)
 gbuffer_write_kernel(const __grid_constant__ GbwParams p) {
     __shared__ float srgb[256];
+    __shared__ float4 samp[7][kGbwThreadsX * kGbwThreadsY];  // each thread's texture samples
     const uint32_t t = threadIdx.y * kGbwThreadsX + threadIdx.x;
     srgb[t] = p.srgb[t];
     __syncthreads();
@@ -256,12 +255,39 @@ gbuffer_write_kernel(const __grid_constant__ GbwParams p) {
     const unsigned char* mt = p.mtex + uint64_t(HL_SIZEOF_MATERIAL_TEXTURES) * mid;
     const uint32_t debug = ldgu(p.globals + 80);
     const float4 one = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-    GbOut o;
+    const float4 base_color = ldg4(mat), emis = ldg4(mat + 16), rm = ldg4(mat + 32);
+    const float4 prm = ldg4(mt + kParamsOffset);
+    const uint32_t flags = ldgu(mat + 72);
+    const bool specular = ldgu(mat + 68) == kWorkflowSpecular;
+    const bool normal_mapped = (flags & kFlagHasNormalMap) != 0u && ldgu(mt + S_NORMAL * kSlotBytes) != HL_NO_TEXTURE;
 
+    // The slots this pixel samples, base colour first (its alpha decides the discard
+    // before anything else is sampled). One loop body holds the only copy of the
+    // sampler; each result goes to this thread's column of samp.
+    uint32_t need = 1u << S_BASE;
+    if (debug == 1u) need = 0u;
+    else if (debug == 3u) need |= 1u << S_RM;
+    else if (debug != 2u) {
+        need |= (1u << S_RM) | (1u << S_OCCLUSION) | (1u << S_EMISSIVE);
+        if (normal_mapped) need |= 1u << S_NORMAL;
+        if (specular) need |= (1u << S_SPEC_COLOR) | (1u << S_SPEC_WEIGHT);
+    }
+    for (uint32_t m = need; m != 0u; m &= m - 1u) {
+        const uint32_t k = __ffs(m) - 1u;
+        const float4 fb = k == S_NORMAL ? make_float4(0.5f, 0.5f, 1.0f, 1.0f) : one;
+        const float4 r = sample_slot(p.tex, p.n_tex, p.status, srgb, mt + k * kSlotBytes, u, v, fb);
+        samp[k][t] = r;
+        // default_pbr_surface's alpha, and the discard of gbuffer.wgsl:484-485
+        if (k == S_BASE && debug == 0u) {
+            const float alpha = base_color.w * r.w;
+            if (alpha <= 0.001f || alpha < prm.z) return;
+        }
+    }
+    GbOut o;
     if (debug == 1u || debug == 2u) {  // gbuffer.wgsl:431-459
         float4 a = make_float4(u, v, 0.0f, 1.0f);
         if (debug == 2u) {
-            const float4 b = sample_slot(p.tex, p.n_tex, p.status, srgb, mt + S_BASE * kSlotBytes, u, v, one);
+            const float4 b = samp[S_BASE][t];
             a = make_float4(b.x, b.y, b.z, 1.0f);
         }
         o = GbOut{{a.x, a.y, a.z, a.w}, {0.0f, 0.0f, 1.0f, 0.0f}, {0, 0, 0, 0}, {0, 0, 0, 0}};
@@ -269,12 +295,11 @@ gbuffer_write_kernel(const __grid_constant__ GbwParams p) {
         return;
     }
 
-    const float4 base_color = ldg4(mat), emis = ldg4(mat + 16), rm = ldg4(mat + 32);
-    const float4 base = sample_slot(p.tex, p.n_tex, p.status, srgb, mt + S_BASE * kSlotBytes, u, v, one);
+    const float4 base = samp[S_BASE][t];
     const float4 albedo = make_float4(base_color.x * base.x, base_color.y * base.y, base_color.z * base.z,
                                       base_color.w * base.w);
     const float3 ng = normalize3(s0.x, s0.y, s0.z);
-    const float4 orm_s = sample_slot(p.tex, p.n_tex, p.status, srgb, mt + S_RM * kSlotBytes, u, v, one);
+    const float4 orm_s = samp[S_RM][t];
     const float rough = fminf(fmaxf(rm.x * orm_s.y, 0.045f), 1.0f);
     const float metal = fminf(fmaxf(rm.y * orm_s.z, 0.0f), 1.0f);
 
@@ -286,32 +311,28 @@ gbuffer_write_kernel(const __grid_constant__ GbwParams p) {
     }
 
     // default_pbr_surface (gbuffer.wgsl:333-364)
-    const float4 prm = ldg4(mt + kParamsOffset);
     const float alpha = albedo.w;
-    if (alpha <= 0.001f || alpha < prm.z) return;  // :484-485, discard
-
     float3 n = ng;
-    const uint32_t flags = ldgu(mat + 72);
-    if ((flags & kFlagHasNormalMap) != 0u && ldgu(mt + S_NORMAL * kSlotBytes) != HL_NO_TEXTURE) {
+    if (normal_mapped) {
         const float tdn = s1.x * ng.x + s1.y * ng.y + s1.z * ng.z;
         const float3 tt = normalize3(s1.x - tdn * ng.x, s1.y - tdn * ng.y, s1.z - tdn * ng.z);
         const float bs = s0.w;
         const float3 bb = make_float3((ng.y * tt.z - ng.z * tt.y) * bs, (ng.z * tt.x - ng.x * tt.z) * bs,
                                       (ng.x * tt.y - ng.y * tt.x) * bs);
-        const float4 ns = sample_slot(p.tex, p.n_tex, p.status, srgb, mt + S_NORMAL * kSlotBytes, u, v, make_float4(0.5f, 0.5f, 1.0f, 1.0f));
+        const float4 ns = samp[S_NORMAL][t];
         const float tx = (ns.x * 2.0f - 1.0f) * prm.x, ty = (ns.y * 2.0f - 1.0f) * prm.x, tz = ns.z * 2.0f - 1.0f;
         n = normalize3(tt.x * tx + bb.x * ty + ng.x * tz, tt.y * tx + bb.y * ty + ng.y * tz,
                        tt.z * tx + bb.z * ty + ng.z * tz);
     }
-    const float4 occ = sample_slot(p.tex, p.n_tex, p.status, srgb, mt + S_OCCLUSION * kSlotBytes, u, v, one);
-    const float4 em_s = sample_slot(p.tex, p.n_tex, p.status, srgb, mt + S_EMISSIVE * kSlotBytes, u, v, one);
+    const float4 occ = samp[S_OCCLUSION][t];
+    const float4 em_s = samp[S_EMISSIVE][t];
     const float ao = 1.0f + (occ.x - 1.0f) * prm.y;
 
     // resolve_specular_f0 (gbuffer.wgsl:308-329)
     float f0r, f0g, f0b;
-    if (ldgu(mat + 68) == kWorkflowSpecular) {
-        const float4 sc = sample_slot(p.tex, p.n_tex, p.status, srgb, mt + S_SPEC_COLOR * kSlotBytes, u, v, one);
-        const float4 sw = sample_slot(p.tex, p.n_tex, p.status, srgb, mt + S_SPEC_WEIGHT * kSlotBytes, u, v, one);
+    if (specular) {
+        const float4 sc = samp[S_SPEC_COLOR][t];
+        const float4 sw = samp[S_SPEC_WEIGHT][t];
         const float ior = fmaxf(rm.z, 1.0f);
         const float q = (ior - 1.0f) / (ior + 1.0f);
         const float k = rm.w * sw.w;
