@@ -483,6 +483,20 @@ def run_forms(ctx, dev, stream, flush, with_oracle=True):
             "pixel_grad_p9999": float(f"{np.quantile(rel_p, 0.9999):.3e}"),
             "pixel_grad_max": float(f"{rel_p.max():.3e}"),
         }
+        # the forward radiance of this FP32 G-buffer against the FP64 oracle
+        from helio_gb300 import metrics
+
+        fwd()
+        st = torch.zeros((H, W, 3), dtype=torch.int32, device=dev)
+        ctx.shade_stats(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, st, sh)
+        ctx.sync_status(sh)
+        ref, pc = oracle.shade(w.camera.record, w.globals_, w.gbuffer, w.lights, ("froxels", idx_h, off_h, p_np),
+                               pair_counts=True)
+        e = metrics.radiance_error(rad.double().cpu().numpy(), ref, st.cpu().numpy().view(np.uint32)[..., 2],
+                                   pc[..., 2])
+        forms["adjoint"]["forward_error_vs_fp64_oracle"] = {
+            "max": float(f"{e['max']:.3e}"), "p9999": float(f"{e['p9999']:.3e}"), "n": e["n"], "flips": e["flips"],
+            "n_over_1e5": e["n_over_1e5"]}
     del df, off, idx, rad, d_rad, d_l, d_p
 
     # ---- batched: w3, 96 cube faces + 1080p + 720p, 2048 lights ----

@@ -124,7 +124,8 @@ __global__ void __launch_bounds__(256, 4) shade_fragments_kernel(
     p.f0r = f3.x;  // the material's F0 as given, not clamped
     p.f0g = f3.y;
     p.f0b = f3.z;
-    const PixelBrdf b = pixel_brdf(p);
+    PixelBrdf b = pixel_brdf(p);
+    df_view(p, b, camx, camy, camz);  // V as a double-float unit vector
     uint32_t base = 0, count = 0;
     if (GRID == HL_GRID_TILES) {
         const uint32_t tile = (y / kTile) * prm.num_tiles_x + x / kTile;

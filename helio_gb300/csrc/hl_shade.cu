@@ -151,6 +151,7 @@ __device__ __forceinline__ void load_pixel(const Smem<NPX, NF>& s, int i, Pixel&
         p.f0b = fmin_(fmax_(metallic_f0(ab, p.metal), 0.0f), 0.999f);
     }
     b = pixel_brdf(p);
+    if (PRECISE) df_view(p, b, camx, camy, camz);  // V as a double-float unit vector
 }
 
 }  // namespace sk
@@ -172,7 +173,7 @@ __device__ __noinline__ int precise_pair(const GpuCamera* cam, uint32_t x, uint3
     // V = -(true P): the camera sits at minus the residual
     finish_pixel<true>(p, p.nrx, p.nry, p.nrz, ar, ag, ab, p.rough, p.metal, p.f0r, p.f0g, p.f0b, -rx, -ry, -rz);
     const PixelBrdf pb = pixel_brdf(p);
-    return eval<true>(p, pb, l, cr, cg, cb);
+    return eval<true, false>(p, pb, l, cr, cg, cb);
 }
 
 // Evaluates nb queued pairs (ring positions head..head+nb-1), one per lane, and adds

@@ -6,9 +6,9 @@
 // Accuracy measures (each keeps the result within ~1e-6 relative of the float64
 // evaluation where the reference's own f32 formulation loses digits):
 //  * world position: inv_view_proj * (ndc, depth, 1) as a compensated dot product
-//    (Ogita-Rump-Oishi Dot2) with the pixel-centre NDC carried as a double-float, then
-//    P = h.xyz / h.w kept as hi + lo. At depth ~100 the plain f32 product loses ~1e-4
-//    relative to cancellation in h.w.
+//    (Ogita-Rump-Oishi Dot2) with the pixel-centre NDC carried as a double-float,
+//    renormalised, then P = h.xyz / h.w kept as hi + lo. At depth ~100 the plain f32
+//    product loses ~1e-4 relative to cancellation in h.w.
 //  * to_light = (light.pos - P.hi) - P.lo, and the range falloff
 //    1 - (d/r)^4 = (r^2 - d^2)(r^2 + d^2)/r^4 with r^2 - d^2 from double-float
 //    squares, so lights near the edge of their range keep their relative accuracy.
@@ -108,6 +108,29 @@ HL_HD DF two_prod(float a, float b) {
     return DF{p, fma_(a, b, -p)};
 }
 
+// Unit vector of the double-float vector (x + xl, y + yl, z + zl), as double-floats
+// accurate to ~2^-44: |v|^2 as a double-float, an f32 rsqrt refined by one Newton step
+// whose residual 1 - |v|^2 r^2 is formed in double-float arithmetic.
+HL_HD void df_unit(float x, float xl, float y, float yl, float z, float zl, float& ux, float& uxl, float& uy,
+                   float& uyl, float& uz, float& uzl) {
+    const DF qx = two_prod(x, x), qy = two_prod(y, y), qz = two_prod(z, z);
+    const DF a = two_sum(qx.hi, qy.hi), b = two_sum(a.hi, qz.hi);
+    const float lo = (a.lo + b.lo) + (qx.lo + qy.lo + qz.lo) + 2.0f * fma_(x, xl, fma_(y, yl, z * zl));
+    const DF s = two_sum(b.hi, lo);
+    const float r = rsqrt_(s.hi);
+    const DF r2 = two_prod(r, r);
+    const DF p1 = two_prod(s.hi, r2.hi);
+    const float e = ((1.0f - p1.hi) - p1.lo) - fma_(s.hi, r2.lo, s.lo * r2.hi);  // 1 - |v|^2 r^2
+    const float rl = r * e * 0.5f;                                                // r (1 + e/2) = r + rl
+    const DF px = two_prod(x, r), py = two_prod(y, r), pz = two_prod(z, r);
+    ux = px.hi;
+    uy = py.hi;
+    uz = pz.hi;
+    uxl = px.lo + fma_(x, rl, xl * r);
+    uyl = py.lo + fma_(y, rl, yl * r);
+    uzl = pz.lo + fma_(z, rl, zl * r);
+}
+
 // ---- per-pixel surface ------------------------------------------------------------
 struct Pixel {
     float Px, Py, Pz;      // world position (hi)
@@ -129,6 +152,7 @@ struct PixelBrdf {
     float gv;          // Schlick-GGX for the view
     float one_m_metal;
     float nv4;         // 4*NdV
+    float vlx, vly, vlz;  // low words of V as a double-float unit vector (df_view), else 0
 };
 
 HL_HD PixelBrdf pixel_brdf(const Pixel& p) {
@@ -141,7 +165,17 @@ HL_HD PixelBrdf pixel_brdf(const Pixel& p) {
     b.gv = divn_(p.NdV, fma_(p.NdV, b.omk, b.k + 0.0001f));
     b.one_m_metal = 1.0f - p.metal;
     b.nv4 = 4.0f * p.NdV;
+    b.vlx = b.vly = b.vlz = 0.0f;
     return b;
+}
+
+// V = normalize(camera - P) as a double-float unit vector from the pixel's double-float
+// position: p.V* its high words, b.vl* its low words (read by eval<true> for lights
+// nearly opposite the view).
+HL_HD void df_view(Pixel& p, PixelBrdf& b, float cx, float cy, float cz) {
+    const DF ux = two_sum(cx, -p.Px), uy = two_sum(cy, -p.Py), uz = two_sum(cz, -p.Pz);
+    const DF vx = two_sum(ux.hi, ux.lo - p.Plx), vy = two_sum(uy.hi, uy.lo - p.Ply), vz = two_sum(uz.hi, uz.lo - p.Plz);
+    df_unit(vx.hi, vx.lo, vy.hi, vy.lo, vz.hi, vz.lo, p.Vx, b.vlx, p.Vy, b.vly, p.Vz, b.vlz);
 }
 
 // Camera-relative reconstruction rows: with M = inv_view_proj and c the camera
@@ -214,8 +248,11 @@ HL_HD void reconstruct(const float* m, uint32_t x, uint32_t y, float W, float H,
         s = s + (u.lo + t.lo);
         s = fma_(m[r], ndx.lo, s);
         s = fma_(m[4 + r], ndy.lo, s);
-        hh[r] = p;
-        hl[r] = s;
+        // renormalise: after cancellation (the w row at far depth) s can be ~1e-5 of p,
+        // and the quotient's correction below assumes |lo| <= ulp(hi)
+        const DF n = two_sum(p, s);
+        hh[r] = n.hi;
+        hl[r] = n.lo;
     }
     const float w = hh[3], wl = hl[3];
     float* outs[3] = {&Px, &Py, &Pz};
@@ -346,11 +383,15 @@ constexpr float kFastMinNdV = 1.0f / 8192.0f;
 // surface, sf = 1. Returns kCut (out* untouched) when a cut applies, kLit with the
 // contribution in out*, or — on the fast path with guard > 0 — kNeedsPrecise. `cut` is
 // the radiance cut (0.002, :781); 0 disables it, as the Forward+ shader has none.
-template <bool PRECISE>
+// DF_HALF (precise evaluations): H from double-float unit vectors when V and L are
+// nearly opposite, with V's low words from df_view (b.vl*, 0 without it); the FP16
+// path's precise re-evaluation (tolerance 2e-3) passes false.
+template <bool PRECISE, bool DF_HALF = PRECISE>
 HL_HD int eval(const Pixel& p, const PixelBrdf& b, const ShadeLight& l, float& outr, float& outg, float& outb,
                float guard = 0.0f, float cut = kRadianceCut) {
     float Lx, Ly, Lz, rr, rg, rb;
     float NdL, d2_near = 0.0f, fall_near = 1.0f;
+    float tx = -l.dx, ty = -l.dy, tz = -l.dz, ex = 0.0f, ey = 0.0f, ez = 0.0f;  // to_light as hi + lo
     if (l.type == 0u) {
         const float il = rsqrt_(fma_(l.dz, l.dz, fma_(l.dy, l.dy, l.dx * l.dx)));
         Lx = -l.dx * il;
@@ -361,14 +402,16 @@ HL_HD int eval(const Pixel& p, const PixelBrdf& b, const ShadeLight& l, float& o
         rb = l.cb * l.intensity;
         NdL = fma_(p.Nz, Lz, fma_(p.Ny, Ly, p.Nx * Lx));
     } else {
-        float tx, ty, tz, d2, fall, ntl = 0.0f;
+        float d2, fall, ntl = 0.0f;
         const float r2 = l.range * l.range;
         if (PRECISE) {
             // to_light = (light - P.hi) - P.lo as normalised double-floats
             const DF ux = two_sum(l.px, -p.Px), uy = two_sum(l.py, -p.Py), uz = two_sum(l.pz, -p.Pz);
             const DF sx = two_sum(ux.hi, ux.lo - p.Plx), sy = two_sum(uy.hi, uy.lo - p.Ply),
                      sz = two_sum(uz.hi, uz.lo - p.Plz);
-            const float ex = sx.lo, ey = sy.lo, ez = sz.lo;
+            ex = sx.lo;
+            ey = sy.lo;
+            ez = sz.lo;
             tx = sx.hi;
             ty = sy.hi;
             tz = sz.hi;
@@ -430,7 +473,18 @@ HL_HD int eval(const Pixel& p, const PixelBrdf& b, const ShadeLight& l, float& o
     if (!(NdL > 0.0f)) return kCut;
     if (rr < cut && rg < cut && rb < cut) return kCut;
     // H = normalize(V + L)
-    const float hx = p.Vx + Lx, hy = p.Vy + Ly, hz = p.Vz + Lz;
+    float hx = p.Vx + Lx, hy = p.Vy + Ly, hz = p.Vz + Lz;
+    if (PRECISE && DF_HALF && fma_(hz, hz, fma_(hy, hy, hx * hx)) < 0.25f) {
+        // V and L nearly opposite (H.V < 1/4): the sum cancels and would turn the f32
+        // rounding of V and L into an error of H's direction; form it from
+        // double-float unit vectors instead
+        float lx, lxl, ly, lyl, lz, lzl;
+        df_unit(tx, ex, ty, ey, tz, ez, lx, lxl, ly, lyl, lz, lzl);
+        const DF sx = two_sum(p.Vx, lx), sy = two_sum(p.Vy, ly), sz = two_sum(p.Vz, lz);
+        hx = sx.hi + (sx.lo + (b.vlx + lxl));
+        hy = sy.hi + (sy.lo + (b.vly + lyl));
+        hz = sz.hi + (sz.lo + (b.vlz + lzl));
+    }
     const float ih = rsqrt_(fma_(hz, hz, fma_(hy, hy, hx * hx)));
     const float Hx = hx * ih, Hy = hy * ih, Hz = hz * ih;
     // Fresnel-Schlick
