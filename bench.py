@@ -655,7 +655,72 @@ def run_forms(ctx, dev, stream, flush, with_oracle=True):
 
     # ---- the G-buffer pass's fragment stage, and a reference-layout frame it feeds ----
     forms["gbuffer_write"] = gbuffer_write_form(ctx, dev, stream, flush, w, df, fp, off, idx, cap, grid, with_oracle)
+    # ---- the w1 frame with the shadow term of the light loop ----
+    forms["shadows"] = shadows_form(ctx, dev, stream, flush, w, fp, off, idx, cap, grid, with_oracle)
     return forms
+
+
+def shadows_form(ctx, dev, stream, flush, w, fp, off, idx, cap, grid, with_oracle=True):
+    """The w1 frame (froxel binning + shading into RGBA32F) with shadow_factor: the first
+    42 lights (the shader's MAX_SHADOW_LIGHTS; all point lights in w1) cast shadows from
+    six 1024^2 cube faces each, dynamic and static Depth32Float atlases of 252 layers
+    (2.1 GB), the default (Medium) ShadowConfig: 12-tap Vogel PCF over both atlases."""
+    import torch
+
+    from helio_gb300 import frame as FR
+    from helio_gb300 import layouts as L
+    from helio_gb300 import metrics
+    from helio_gb300 import native as N
+    from helio_gb300 import synthetic as S
+
+    sh = stream.cuda_stream
+    W, H = w.gbuffer.width, w.gbuffer.height
+    sc = S.shadow_scene(w.camera, w.lights, L.MAX_SHADOW_LIGHTS, quality="medium")
+    dyn, sta = S.shadow_atlases(sc.kinds, L.SHADOW_ATLAS_SIZE, seed=1, xp=torch, device=dev)
+    mats = torch.from_numpy(sc.matrices).to(dev)
+    cfg = FR.bytes_tensor(sc.config, dev)
+    maps = N.shadow_maps_struct(dyn, sta, mats, cfg, sc.max_lights)
+    d_lights = FR.bytes_tensor(sc.lights, dev)
+    dfs = FR.upload(w.camera.record, w.globals_, sc.lights, w.gbuffer, dev)
+    rad = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
+    tgt = N.target_struct(rad)
+
+    def frame():
+        ctx.bin_froxels(dfs.camera, d_lights, dfs.n_lights, fp, off, idx, cap, sh)
+        ctx.shade_shadowed(dfs.camera, dfs.globals_, dfs.gbuffer, d_lights, dfs.n_lights, grid, maps, tgt, sh)
+
+    t_s = _median_ms(frame, stream, flush, 50)
+    ctx.sync_status(sh)
+    casters = [int(v) for v in np.bincount(sc.lights["light_type"][: L.MAX_SHADOW_LIGHTS], minlength=3)]
+    entry = {"workload": WORKLOAD + ", lights 0-41 cast shadows (1024^2 cube faces, dynamic + static atlases of "
+                                    "252 layers), Medium ShadowConfig (12-tap PCF)",
+             "casters_by_type": {"directional": casters[0], "point": casters[1], "spot": casters[2]},
+             "frame_ms": round(t_s, 4), "mpix_s": round(W * H / t_s / 1e3, 1),
+             "atlas_bytes": int(2 * dyn.numel() * 4)}
+    if with_oracle:
+        import oracle
+
+        off_h = off.cpu().numpy().view(np.uint32)
+        idx_h = idx.cpu().numpy().view(np.uint32)[: int(off_h[-1])]
+        p_np = L.froxel_params(*w.froxel_grid, W, H, w.camera.far)
+        shadows = dict(dynamic=dyn.cpu().numpy(), static=sta.cpu().numpy(), matrices=sc.matrices, config=sc.config,
+                       max_lights=sc.max_lights)
+        ref, pc, _ = oracle.shade_shadowed(w.camera.record, w.globals_, w.gbuffer, sc.lights,
+                                           ("froxels", idx_h, off_h, p_np), shadows, pair_counts=True)
+        st = torch.zeros((H, W, 3), dtype=torch.int32, device=dev)
+        ctx.shade_stats(dfs.camera, dfs.globals_, dfs.gbuffer, d_lights, dfs.n_lights, grid, st, sh)
+        ctx.sync_status(sh)
+        e = metrics.radiance_error(rad.double().cpu().numpy(), ref, st.cpu().numpy().view(np.uint32)[..., 2],
+                                   pc[..., 2])
+        plain = oracle.shade(w.camera.record, w.globals_, w.gbuffer, sc.lights, ("froxels", idx_h, off_h, p_np))
+        sky = np.isnan(ref[..., 0])
+        darker = float((ref[~sky][:, :3] < plain[~sky][:, :3] * (1 - 1e-6)).any(-1).mean())
+        entry["pixels_darkened_by_shadows"] = round(darker, 4)
+        entry["error_vs_fp64_oracle"] = {"max": float(f"{e['max']:.3e}"), "p9999": float(f"{e['p9999']:.3e}"),
+                                         "n_over_2e3": e["n_over_2e3"], "flips": e["flips"], "n": e["n"]}
+    del dyn, sta
+    torch.cuda.empty_cache()
+    return entry
 
 
 def gbuffer_write_form(ctx, dev, stream, flush, w, df, fp, off, idx, cap, grid, with_oracle=True):

@@ -18,7 +18,7 @@ using namespace hl_host;
 
 hl_status shade_common(hl_ctx* ctx, const void* camera, const void* globals, const hl_gbuffer* gbuffer,
                        const void* lights, uint32_t n_lights, const hl_light_grid* grid, const hl_target* radiance,
-                       uint32_t* stats, void* stream) {
+                       uint32_t* stats, void* stream, const hl_shadow_maps* shadows = nullptr) {
     hl_status s = check_common(ctx, camera, lights, n_lights);
     if (s != HL_OK) return s;
     if (!globals || !aligned(globals, 16)) return fail(ctx, HL_ERR_INVALID_ARGUMENT, "globals is NULL or misaligned");
@@ -34,6 +34,22 @@ hl_status shade_common(hl_ctx* ctx, const void* camera, const void* globals, con
     } else if (!aligned(stats, 4)) {
         return fail(ctx, HL_ERR_LAYOUT, "stats pointer not 4-byte aligned");
     }
+    hl::ShadowView sv{};
+    if (shadows) {
+        const hl_shadow_maps& m = *shadows;
+        if (!m.dynamic_atlas || !m.static_atlas || !m.matrices || !m.config)
+            return fail(ctx, HL_ERR_INVALID_ARGUMENT, "shadow maps: an atlas, the matrices or the config is NULL");
+        if (!aligned(m.dynamic_atlas, 4) || !aligned(m.static_atlas, 4) || !aligned(m.matrices, 16) ||
+            !aligned(m.config, 16))
+            return fail(ctx, HL_ERR_LAYOUT, "shadow maps: atlases need 4-byte, matrices and config 16-byte alignment");
+        if (m.size == 0 || m.size > 16384 || m.layers == 0 || m.layers > 65536)
+            return fail(ctx, HL_ERR_SIZE, "shadow maps: %u layers of %u texels (1..65536 layers, 1..16384 texels)",
+                        m.layers, m.size);
+        if (m.reserved != 0) return fail(ctx, HL_ERR_INVALID_ARGUMENT, "shadow maps: reserved field must be 0");
+        sv = hl::ShadowView{m.dynamic_atlas, m.static_atlas, static_cast<const float*>(m.matrices),
+                            static_cast<const unsigned char*>(m.config), ctx->d_status, m.size, m.layers,
+                            m.max_shadow_lights, float(m.size)};
+    }
     DeviceGuard dg(ctx->device);
     if (!dg.ok) return fail(ctx, HL_ERR_CUDA, "cudaSetDevice(%d) failed", ctx->device);
     if ((s = ensure(ctx, ctx->shade_cand, ctx->shade_cand_cap, n_lights > 0 ? n_lights : 1, "shade light table")) !=
@@ -41,7 +57,7 @@ hl_status shade_common(hl_ctx* ctx, const void* camera, const void* globals, con
         return s;
     cudaError_t e = hl::launch_shade(gbuffer->layout, grid->kind, stats ? HL_TARGET_RGBA32F : radiance->format, camera,
                                      globals, gv, lights, n_lights, grv, tab, tv, stats, ctx->d_status,
-                                     ctx->shade_cand, as_stream(stream));
+                                     ctx->shade_cand, as_stream(stream), shadows ? &sv : nullptr);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "shade launch");
     return HL_OK;
 }
@@ -194,6 +210,12 @@ hl_status hl_bin_froxels(hl_ctx* ctx, const void* camera, const void* lights, ui
 hl_status hl_shade(hl_ctx* ctx, const void* camera, const void* globals, const hl_gbuffer* gbuffer, const void* lights,
                    uint32_t n_lights, const hl_light_grid* grid, const hl_target* radiance, void* stream) {
     return shade_common(ctx, camera, globals, gbuffer, lights, n_lights, grid, radiance, nullptr, stream);
+}
+
+hl_status hl_shade_shadowed(hl_ctx* ctx, const void* camera, const void* globals, const hl_gbuffer* gbuffer,
+                            const void* lights, uint32_t n_lights, const hl_light_grid* grid,
+                            const hl_shadow_maps* shadows, const hl_target* radiance, void* stream) {
+    return shade_common(ctx, camera, globals, gbuffer, lights, n_lights, grid, radiance, nullptr, stream, shadows);
 }
 
 hl_status hl_shade_stats(hl_ctx* ctx, const void* camera, const void* globals, const hl_gbuffer* gbuffer,

@@ -18,6 +18,7 @@
 #include "hl_common.cuh"
 #include "hl_internal.h"
 #include "hl_shade_math.cuh"
+#include "hl_shadow.cuh"
 #include "hl_texel.cuh"
 
 namespace hl {
@@ -179,10 +180,11 @@ __device__ __noinline__ int precise_pair(const GpuCamera* cam, uint32_t x, uint3
 // Evaluates nb queued pairs (ring positions head..head+nb-1), one per lane, and adds
 // them into the per-pixel Kahan accumulators in queue order. Out of line so that the
 // BRDF code exists once in the kernel.
-template <uint32_t LAYOUT, bool STATS, int TW, int NPX>
+template <uint32_t LAYOUT, bool STATS, int TW, int NPX, bool SHADOW>
 __device__ __noinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>()>& s, const uint32_t* queue, uint32_t head, uint32_t nb,
                                          uint32_t lane, const GpuCamera* cam, const GpuLight* lights, uint32_t x0,
-                                         uint32_t y0, float W, float H) {
+                                         uint32_t y0, float W, float H, const DeferredGlobals* glb,
+                                         const ShadowView* sv) {
     using namespace sk;
     constexpr bool PRECISE = (LAYOUT != HL_GBUF_F16);
     uint32_t (*cnt)[NPX] = reinterpret_cast<uint32_t (*)[NPX]>(s.acc);
@@ -218,6 +220,20 @@ __device__ __noinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>
         if (!PRECISE && st == kNeedsPrecise)
             st = precise_pair(cam, x0 + q % TW, y0 + q / TW, W, H, dq, p, s.px[F_AR][q], s.px[F_AG][q],
                               s.px[F_AB][q], l, ux.lo, uy.lo, uz.lo, cr, cg, cb);
+        if (SHADOW && st == kLit && li < sv->max_lights && d.x != HL_NO_SHADOW) {
+            // the pair's shadow factor (deferred_lighting.wgsl:1136-1141) at the pixel's f32
+            // world position (camera-relative on the fast path)
+            const float camx = cam->position_near[0], camy = cam->position_near[1], camz = cam->position_near[2];
+            const float wx = PRECISE ? p.Px + p.Plx : camx + (p.Px + p.Plx);
+            const float wy = PRECISE ? p.Py + p.Ply : camy + (p.Py + p.Ply);
+            const float wz = PRECISE ? p.Pz + p.Plz : camz + (p.Pz + p.Plz);
+            const float4 csm = *reinterpret_cast<const float4*>(glb->csm_splits);
+            const float sf = shadow_factor(*sv, li, a, b, d.x, d.y, wx, wy, wz, p.Nx, p.Ny, p.Nz,
+                                           float(x0 + q % TW) + 0.5f, float(y0 + q / TW) + 0.5f, camx, camy, camz, csm);
+            cr *= sf;
+            cg *= sf;
+            cb *= sf;
+        }
     }
     const bool lit = act && st == kLit;
     if (STATS) {
@@ -246,12 +262,13 @@ __device__ __noinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>
 // PREFETCH: the kernel's grid is this view's tiles (bx, by); before the walk the CTA asks
 // L2 for the G-buffer of the tile three CTAs per SM further on, the one likely to start
 // on an SM as the current wave drains, so its set-up loads hit L2.
-template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, int TW, int TH, bool PREFETCH = false>
+template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, int TW, int TH, bool PREFETCH = false,
+          bool SHADOW = false>
 __device__ __forceinline__ void shade_tile(
     const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const GBufView& gb,
     const GpuLight* __restrict__ lights, const float4* __restrict__ cand, uint32_t n_lights, const GridView& grid,
     const float* __restrict__ tabz, const TargetView& out, uint32_t* __restrict__ stats, int* __restrict__ status,
-    uint32_t bx, uint32_t by) {
+    uint32_t bx, uint32_t by, const ShadowView* sv = nullptr) {
     using namespace sk;
     constexpr bool FROXELS = (GRID == HL_GRID_FROXELS);
     constexpr int NPX = TW * TH;
@@ -516,7 +533,7 @@ __device__ __forceinline__ void shade_tile(
                     qlen += __popc(pm);
                     __syncwarp();
                     if (qlen >= 32) {
-                        flush_batch<LAYOUT, STATS, TW, NPX>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H);
+                        flush_batch<LAYOUT, STATS, TW, NPX, SHADOW>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H, glb, sv);
                         head += 32;
                         qlen -= 32;
                     }
@@ -551,13 +568,13 @@ __device__ __forceinline__ void shade_tile(
             }
             __syncwarp();
             while (qlen >= 32) {
-                flush_batch<LAYOUT, STATS, TW, NPX>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H);
+                flush_batch<LAYOUT, STATS, TW, NPX, SHADOW>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H, glb, sv);
                 head += 32;
                 qlen -= 32;
             }
         }
     }
-    if (qlen > 0) flush_batch<LAYOUT, STATS, TW, NPX>(s, queue, head, qlen, lane, cam, lights, x0, y0, W, H);
+    if (qlen > 0) flush_batch<LAYOUT, STATS, TW, NPX, SHADOW>(s, queue, head, qlen, lane, cam, lights, x0, y0, W, H, glb, sv);
 
     // ---- 5. output -----------------------------------------------------------------
     __syncthreads();
@@ -628,13 +645,14 @@ __device__ __forceinline__ void shade_tile(
     }
 }
 
-template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, int TW, int TH>
+template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, int TW, int TH, bool SHADOW>
 __global__ void __launch_bounds__(sk::kThreads, 3) shade_kernel(
     const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const GBufView gb,
     const GpuLight* __restrict__ lights, uint32_t n_lights, const GridView grid, const __grid_constant__ SliceTable tab,
-    const TargetView out, uint32_t* __restrict__ stats, int* __restrict__ status, const float4* __restrict__ cand) {
-    shade_tile<LAYOUT, GRID, TARGET, STATS, TW, TH, true>(cam, glb, gb, lights, cand, n_lights, grid, tab.z, out,
-                                                          stats, status, blockIdx.x, blockIdx.y);
+    const TargetView out, uint32_t* __restrict__ stats, int* __restrict__ status, const float4* __restrict__ cand,
+    const __grid_constant__ ShadowView sv) {
+    shade_tile<LAYOUT, GRID, TARGET, STATS, TW, TH, true, SHADOW>(cam, glb, gb, lights, cand, n_lights, grid, tab.z,
+                                                                  out, stats, status, blockIdx.x, blockIdx.y, &sv);
 }
 
 // Every tile of every view of a batch (froxel grids, 32x16 tiles): CTA b lights tile
@@ -709,13 +727,13 @@ cudaError_t launch_batched(const ShadeViewDesc* descs, uint32_t n_views, uint32_
     return cudaGetLastError();
 }
 
-template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS>
+template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, bool SHADOW = false>
 cudaError_t launch_one(const void* camera, const void* globals, const GBufView& gb, const void* lights, uint32_t n,
                        const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats, int* status, float4* cand,
-                       cudaStream_t stream) {
+                       cudaStream_t stream, const ShadowView* sv = nullptr) {
     constexpr bool FROXELS = (GRID == HL_GRID_FROXELS);
     constexpr int TW = FROXELS ? 32 : 16, TH = 16;
-    auto kern = shade_kernel<LAYOUT, GRID, TARGET, STATS, TW, TH>;
+    auto kern = shade_kernel<LAYOUT, GRID, TARGET, STATS, TW, TH, SHADOW>;
     const int smem = int(sizeof(sk::Smem<TW * TH, sk::record_fields<LAYOUT>()>));
     static unsigned long long attr_devices = 0;  // devices on which the smem limit is raised
     int dev = 0;
@@ -732,15 +750,25 @@ cudaError_t launch_one(const void* camera, const void* globals, const GBufView& 
         if (e != cudaSuccess) return e;
     }
     const dim3 g((gb.width + TW - 1) / TW, (gb.height + TH - 1) / TH);
+    ShadowView svv{};
+    if (sv) svv = *sv;
     return launch_pdl(kern, g, dim3(sk::kThreads), smem, stream, static_cast<const GpuCamera*>(camera),
                       static_cast<const DeferredGlobals*>(globals), gb, static_cast<const GpuLight*>(lights), n, grid,
-                      tab, out, stats, status, static_cast<const float4*>(cand));
+                      tab, out, stats, status, static_cast<const float4*>(cand), svv);
 }
 
 template <uint32_t LAYOUT, uint32_t GRID>
 cudaError_t dispatch_target(uint32_t target, const void* camera, const void* globals, const GBufView& gb,
                             const void* lights, uint32_t n, const GridView& grid, const SliceTable& tab,
-                            const TargetView& out, uint32_t* stats, int* status, float4* cand, cudaStream_t stream) {
+                            const TargetView& out, uint32_t* stats, int* status, float4* cand, cudaStream_t stream,
+                            const ShadowView* sv) {
+    if (sv && !stats) {
+        if (target == HL_TARGET_RGBA16F)
+            return launch_one<LAYOUT, GRID, HL_TARGET_RGBA16F, false, true>(camera, globals, gb, lights, n, grid, tab,
+                                                                            out, stats, status, cand, stream, sv);
+        return launch_one<LAYOUT, GRID, HL_TARGET_RGBA32F, false, true>(camera, globals, gb, lights, n, grid, tab, out,
+                                                                        stats, status, cand, stream, sv);
+    }
     if (stats)
         return launch_one<LAYOUT, GRID, HL_TARGET_RGBA32F, true>(camera, globals, gb, lights, n, grid, tab, out, stats,
                                                                  status, cand, stream);
@@ -755,12 +783,12 @@ template <uint32_t LAYOUT>
 cudaError_t dispatch_grid(uint32_t grid_kind, uint32_t target, const void* camera, const void* globals,
                           const GBufView& gb, const void* lights, uint32_t n, const GridView& grid,
                           const SliceTable& tab, const TargetView& out, uint32_t* stats, int* status, float4* cand,
-                          cudaStream_t stream) {
+                          cudaStream_t stream, const ShadowView* sv) {
     if (grid_kind == HL_GRID_FROXELS)
         return dispatch_target<LAYOUT, HL_GRID_FROXELS>(target, camera, globals, gb, lights, n, grid, tab, out, stats,
-                                                        status, cand, stream);
+                                                        status, cand, stream, sv);
     return dispatch_target<LAYOUT, HL_GRID_TILES>(target, camera, globals, gb, lights, n, grid, tab, out, stats,
-                                                  status, cand, stream);
+                                                  status, cand, stream, sv);
 }
 
 }  // namespace
@@ -768,17 +796,17 @@ cudaError_t dispatch_grid(uint32_t grid_kind, uint32_t target, const void* camer
 cudaError_t launch_shade(uint32_t layout, uint32_t grid_kind, uint32_t target_format, const void* camera,
                          const void* globals, const GBufView& gb, const void* lights, uint32_t n_lights,
                          const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats,
-                         int* status, float4* cand, cudaStream_t stream) {
+                         int* status, float4* cand, cudaStream_t stream, const ShadowView* shadows) {
     switch (layout) {
         case HL_GBUF_REFERENCE:
             return dispatch_grid<HL_GBUF_REFERENCE>(grid_kind, target_format, camera, globals, gb, lights, n_lights,
-                                                    grid, tab, out, stats, status, cand, stream);
+                                                    grid, tab, out, stats, status, cand, stream, shadows);
         case HL_GBUF_F32:
             return dispatch_grid<HL_GBUF_F32>(grid_kind, target_format, camera, globals, gb, lights, n_lights, grid,
-                                              tab, out, stats, status, cand, stream);
+                                              tab, out, stats, status, cand, stream, shadows);
         default:
             return dispatch_grid<HL_GBUF_F16>(grid_kind, target_format, camera, globals, gb, lights, n_lights, grid,
-                                              tab, out, stats, status, cand, stream);
+                                              tab, out, stats, status, cand, stream, shadows);
     }
 }
 

@@ -251,6 +251,60 @@ def missing_material_textures(n: int = 1) -> np.ndarray:
     return m
 
 
+# ShadowConfig (libhelio/src/shadow.rs:33-64): four cascades of (split_distance,
+# depth_bias, filter_radius, pcss_light_size), then the PCSS toggle and sample counts.
+# 80 bytes (the struct's doc comment says 96).
+SHADOW_CONFIG = np.dtype(
+    [
+        ("cascades", "<f4", (4, 4)),
+        ("enable_pcss", "<u4"),
+        ("pcss_blocker_samples", "<u4"),
+        ("pcss_filter_samples", "<u4"),
+        ("pcf_sample_count", "<u4"),
+    ]
+)
+
+# hl_shadow_maps (include/helio_gb300.h)
+SHADOW_MAPS = np.dtype(
+    [
+        ("dynamic_atlas", "<u8"),
+        ("static_atlas", "<u8"),
+        ("matrices", "<u8"),
+        ("config", "<u8"),
+        ("size", "<u4"),
+        ("layers", "<u4"),
+        ("max_shadow_lights", "<u4"),
+        ("reserved", "<u4"),
+    ]
+)
+SHADOW_ATLAS_SIZE = 1024  # the shader's ATLAS_SIZE (deferred_lighting.wgsl:235)
+MAX_SHADOW_LIGHTS = 42    # MAX_SHADOW_LIGHTS (deferred_lighting.wgsl:20)
+
+# The quality presets of ShadowConfig::from_quality (libhelio/src/shadow.rs:74-205):
+# per cascade (split, bias, filter radius, PCSS light size), then (enable_pcss,
+# blocker samples, filter samples, PCF samples).
+SHADOW_PRESETS = {
+    "low": ([(16.0, 0.00010, 1.0, 0.0), (80.0, 0.00015, 1.5, 0.0), (300.0, 0.00020, 2.0, 0.0),
+             (1400.0, 0.00030, 3.0, 0.0)], (0, 4, 4, 8)),
+    "medium": ([(16.0, 0.00010, 1.5, 0.0), (80.0, 0.00015, 2.0, 0.0), (300.0, 0.00020, 2.5, 0.0),
+                (1400.0, 0.00030, 3.5, 0.0)], (0, 8, 8, 12)),
+    "high": ([(16.0, 0.00008, 2.0, 2.0), (80.0, 0.00012, 2.5, 4.0), (300.0, 0.00018, 3.0, 8.0),
+              (1400.0, 0.00025, 4.0, 16.0)], (1, 8, 16, 12)),
+    "ultra": ([(16.0, 0.00008, 2.5, 2.0), (80.0, 0.00012, 3.0, 4.0), (300.0, 0.00018, 3.5, 8.0),
+               (1400.0, 0.00025, 4.5, 16.0)], (1, 16, 32, 16)),
+}
+
+
+def shadow_config(quality: str = "medium") -> np.ndarray:
+    """A ShadowConfig of one of the reference's presets (default: Medium, the
+    reference's Default)."""
+    cascades, (pcss, nb, nf, npcf) = SHADOW_PRESETS[quality]
+    c = np.zeros(1, SHADOW_CONFIG)
+    c["cascades"] = np.array(cascades, np.float32)
+    c["enable_pcss"], c["pcss_blocker_samples"], c["pcss_filter_samples"], c["pcf_sample_count"] = pcss, nb, nf, npcf
+    return c
+
+
 # CSM split distances written into DeferredGlobals (libhelio/src/shadow.rs:13)
 CSM_SPLITS = (16.0, 80.0, 300.0, 1400.0)
 
@@ -269,6 +323,8 @@ EXPECTED_SIZES = {
     "MATERIAL_TEXTURES": 352,
     "SURFACE": 64,
     "TEXTURE": 40,
+    "SHADOW_CONFIG": 80,
+    "SHADOW_MAPS": 48,
 }
 
 for _name, _size in EXPECTED_SIZES.items():

@@ -96,6 +96,13 @@ class Texture(C.Structure):
                 ("filter", C.c_uint32)]
 
 
+class ShadowMaps(C.Structure):
+    """hl_shadow_maps: two Depth32Float atlases, the light matrices and ShadowConfig."""
+    _fields_ = [("dynamic_atlas", C.c_void_p), ("static_atlas", C.c_void_p), ("matrices", C.c_void_p),
+                ("config", C.c_void_p), ("size", C.c_uint32), ("layers", C.c_uint32),
+                ("max_shadow_lights", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 class GBufferTargets(C.Structure):
     """hl_gbuffer_targets: albedo, normal, orm, emissive (required), lightmap_uv, sss,
     extra, velocity (optional)."""
@@ -108,7 +115,7 @@ EXPORTS = [
     "hl_tile_count", "hl_bin_tiles_ref", "hl_froxel_slice_table", "hl_bin_froxels", "hl_shade", "hl_shade_stats",
     "hl_shade_adjoint", "hl_batch_plan_create", "hl_batch_execute", "hl_batch_plan_view_grid",
     "hl_batch_plan_destroy", "hl_probe_fp32_peak", "hl_bin_froxels_noalloc", "hl_shade_fragments",
-    "hl_write_gbuffer",
+    "hl_write_gbuffer", "hl_shade_shadowed",
 ]
 
 _lock = threading.Lock()
@@ -179,6 +186,8 @@ def _bind(l):
     l.hl_shade_fragments.restype = i32
     l.hl_write_gbuffer.argtypes = [vp, vp, vp, C.c_uint64, vp, vp, u32, P(Texture), u32, P(GBufferTargets), vp]
     l.hl_write_gbuffer.restype = i32
+    l.hl_shade_shadowed.argtypes = [vp, vp, vp, P(GBuffer), vp, u32, P(LightGrid), P(ShadowMaps), P(Target), vp]
+    l.hl_shade_shadowed.restype = i32
 
 
 def status_string(status: int) -> str:
@@ -293,6 +302,13 @@ class Context:
         self._check(self._l.hl_shade(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer), _ptr(lights), n_lights,
                                      C.byref(grid), C.byref(target), _stream(stream)), "hl_shade")
 
+    def shade_shadowed(self, camera, globals_, gbuffer: GBuffer, lights, n_lights, grid: LightGrid,
+                       shadows: "ShadowMaps", target: Target, stream=None):
+        """hl_shade with the shadow term (shadows=None: plain hl_shade)."""
+        self._check(self._l.hl_shade_shadowed(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer), _ptr(lights),
+                                              n_lights, C.byref(grid), C.byref(shadows) if shadows else None,
+                                              C.byref(target), _stream(stream)), "hl_shade_shadowed")
+
     def shade_stats(self, camera, globals_, gbuffer: GBuffer, lights, n_lights, grid: LightGrid, counts, stream=None):
         self._check(self._l.hl_shade_stats(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer), _ptr(lights),
                                            n_lights, C.byref(grid), _ptr(counts), _stream(stream)), "hl_shade_stats")
@@ -406,6 +422,17 @@ def texture_struct(texels, fmt: int, address_u: int = 0, address_v: int = 0, fil
     t.height, t.width = int(texels.shape[0]), int(texels.shape[1])
     t.format, t.address_u, t.address_v, t.filter = fmt, address_u, address_v, filt
     return t
+
+
+def shadow_maps_struct(dynamic, static, matrices, config, max_shadow_lights: int = 42) -> ShadowMaps:
+    """``dynamic``/``static``: device tensors (layers, size, size) float32; ``matrices``:
+    device tensor of GpuShadowMatrix records; ``config``: device ShadowConfig bytes."""
+    m = ShadowMaps()
+    m.dynamic_atlas, m.static_atlas = _ptr(dynamic), _ptr(static)
+    m.matrices, m.config = _ptr(matrices), _ptr(config)
+    m.layers, m.size = int(dynamic.shape[0]), int(dynamic.shape[1])
+    m.max_shadow_lights = max_shadow_lights
+    return m
 
 
 def gbuffer_targets_struct(width: int, height: int, planes) -> GBufferTargets:

@@ -598,3 +598,108 @@ def material_scene(cam: Camera, seed: int, n_materials: int = 64, n_textures: in
     glb["debug_mode"] = debug_mode
     glb["screen_width"], glb["screen_height"] = float(W), float(H)
     return MaterialScene(cam, srf.reshape(H, W), mats, mtex, textures, glb, depth)
+
+
+# ----------------------------------------------------------------------------------
+# Shadow maps: light-space matrices and depth atlases
+# ----------------------------------------------------------------------------------
+
+
+def orthographic_rh_dx(half_w: float, half_h: float, near: float, far: float) -> np.ndarray:
+    """glam ``orthographic_rh`` (DirectX depth range [0, 1]) of a box centred on the axis."""
+    m = np.eye(4)
+    m[0, 0], m[1, 1] = 1.0 / half_w, 1.0 / half_h
+    m[2, 2], m[2, 3] = 1.0 / (near - far), near / (near - far)
+    return m
+
+
+def _look(eye, d):
+    d = np.asarray(d, np.float64)
+    up = (1.0, 0.0, 0.0) if abs(d[1]) > 0.99 * np.linalg.norm(d) else (0.0, 1.0, 0.0)
+    return look_at_rh(eye, np.asarray(eye, np.float64) + d, up)
+
+
+CUBE_FACES = ((1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1))  # point_light_face order
+
+
+@dataclass
+class ShadowScene:
+    """Shadow inputs for hl_shade_shadowed: ``lights`` with shadow_index set for the
+    first ``n_shadowed`` lights (6 layers each, as GpuShadowMatrix lays them out),
+    matrices (layers, 16) float32 column major, the config, and ``kinds[layer]`` =
+    "persp" or "ortho" for the atlas generator."""
+    lights: np.ndarray
+    matrices: np.ndarray
+    config: np.ndarray
+    kinds: list
+    max_lights: int
+
+
+def shadow_scene(cam: Camera, lights: np.ndarray, n_shadowed: int, quality: str = "medium",
+                 max_lights: int = L.MAX_SHADOW_LIGHTS) -> ShadowScene:
+    """Light-space matrices for the first ``n_shadowed`` lights: six 90-degree cube faces
+    for a point light, one perspective of the outer cone for a spot light, four
+    orthographic cascades (half extents = the CSM splits) around the camera for a
+    directional light; DirectX depth, near 0.05, far = the light's range (500 for
+    cascades)."""
+    lt = lights.copy()
+    n_shadowed = min(n_shadowed, len(lt))
+    mats = np.tile(np.eye(4).T.reshape(16).astype(np.float32), (6 * max(n_shadowed, 1), 1))
+    kinds = ["persp"] * (6 * max(n_shadowed, 1))
+    lt["shadow_index"] = L.NO_SHADOW
+    for i in range(n_shadowed):
+        base = 6 * i
+        lt["shadow_index"][i] = base
+        pos = lt["position_range"][i, :3].astype(np.float64)
+        rng = float(lt["position_range"][i, 3])
+        typ = int(lt["light_type"][i])
+        d = lt["direction_outer"][i, :3].astype(np.float64)
+        if typ == L.LIGHT_POINT:
+            proj = perspective_rh_dx(math.radians(90.0), 1.0, 0.05, max(rng, 0.1))
+            for f, ax in enumerate(CUBE_FACES):
+                mats[base + f] = _cols(proj @ _look(pos, ax))
+        elif typ == L.LIGHT_SPOT:
+            half = math.acos(min(max(float(lt["direction_outer"][i, 3]), -1.0), 1.0))
+            fov = min(max(2.0 * half, math.radians(2.0)), math.radians(170.0))
+            mats[base] = _cols(perspective_rh_dx(fov, 1.0, 0.05, max(rng, 0.1)) @ _look(pos, d))
+        else:  # directional: cascades around the camera
+            dn = d / np.linalg.norm(d)
+            for c, split in enumerate(L.CSM_SPLITS):
+                view = _look(cam.eye - dn * 500.0, dn)
+                mats[base + c] = _cols(orthographic_rh_dx(split, split, 0.1, 1000.0) @ view)
+                kinds[base + c] = "ortho"
+    return ShadowScene(lt, mats, L.shadow_config(quality), kinds, max_lights)
+
+
+def shadow_atlases(kinds, size: int, seed: int, xp=np, device=None):
+    """Dynamic and static Depth32Float atlases (layers, size, size): smooth depth fields
+    per layer (sums of sinusoids with layer-dependent phases), in [0.99, 1] for
+    perspective layers and [0.2, 1] for orthographic cascades, so that part of every
+    layer's receivers is occluded; the static atlas is empty (1.0) outside blobs.
+    ``xp`` is numpy or torch (with ``device``) for large atlases."""
+    n = len(kinds)
+    ph = uniform(seed, 300, 6 * n, 0.0, 2 * math.pi).reshape(n, 6)
+    lo = np.array([0.99 if k == "persp" else 0.2 for k in kinds])
+    if xp is np:
+        t = np.arange(size, dtype=np.float64) / size
+        Y, X = np.meshgrid(t, t, indexing="ij")
+        dyn = np.empty((n, size, size), np.float32)
+        sta = np.empty((n, size, size), np.float32)
+        for i in range(n):
+            a = 0.5 + 0.25 * np.sin(2 * math.pi * (3 * X + ph[i, 0])) + 0.25 * np.sin(2 * math.pi * (5 * Y + ph[i, 1]))
+            b = np.sin(2 * math.pi * (2 * X + ph[i, 2])) * np.sin(2 * math.pi * (3 * Y + ph[i, 3]))
+            dyn[i] = lo[i] + (1 - lo[i]) * np.clip(a, 0, 1)
+            sta[i] = np.where(b > 0.5, lo[i] + (1 - lo[i]) * (1.5 - b), 1.0)
+        return dyn, sta
+    torch = xp
+    t = torch.arange(size, dtype=torch.float32, device=device) / size
+    Y, X = torch.meshgrid(t, t, indexing="ij")
+    dyn = torch.empty((n, size, size), dtype=torch.float32, device=device)
+    sta = torch.empty((n, size, size), dtype=torch.float32, device=device)
+    for i in range(n):
+        p = [float(v) for v in ph[i]]
+        a = 0.5 + 0.25 * torch.sin(2 * math.pi * (3 * X + p[0])) + 0.25 * torch.sin(2 * math.pi * (5 * Y + p[1]))
+        b = torch.sin(2 * math.pi * (2 * X + p[2])) * torch.sin(2 * math.pi * (3 * Y + p[3]))
+        dyn[i] = float(lo[i]) + (1 - float(lo[i])) * a.clamp(0, 1)
+        sta[i] = torch.where(b > 0.5, float(lo[i]) + (1 - float(lo[i])) * (1.5 - b), torch.ones_like(b))
+    return dyn, sta

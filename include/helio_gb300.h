@@ -238,6 +238,52 @@ hl_status hl_shade(hl_ctx* ctx, const void* camera, const void* globals, const h
                    const void* lights, uint32_t n_lights, const hl_light_grid* grid,
                    const hl_target* radiance, void* stream);
 
+/* Shadow maps of the lights: the deferred pass's shadow bindings
+ * (deferred_lighting.wgsl:129-167; libhelio/src/shadow.rs:33-64, light.rs:150-164).
+ *   dynamic_atlas, static_atlas : device, Depth32Float layers, `layers` x size x size texels,
+ *                                 layer-major, rows of `size` texels (the shader's
+ *                                 shadow_atlas and static_shadow_atlas)
+ *   matrices                    : device, GpuShadowMatrix[layers] (64 B: column-major light
+ *                                 view-projection); a light's layers start at its
+ *                                 shadow_index: 6 cube faces (point), cascades 0-3
+ *                                 (directional), one (spot)
+ *   config                      : device, ShadowConfig (80 B: four cascades of
+ *                                 {split_distance, depth_bias, filter_radius,
+ *                                 pcss_light_size}, then enable_pcss, pcss_blocker_samples,
+ *                                 pcss_filter_samples, pcf_sample_count)
+ *   size                        : texels per side; the shader's ATLAS_SIZE (1024)
+ *   max_shadow_lights           : lights with an index >= this cast no shadow (the shader's
+ *                                 MAX_SHADOW_LIGHTS, 42) */
+#define HL_SIZEOF_SHADOW_CONFIG 80u
+#define HL_SIZEOF_SHADOW_MATRIX 64u
+#define HL_NO_SHADOW 0xFFFFFFFFu
+typedef struct hl_shadow_maps {
+    const float* dynamic_atlas;
+    const float* static_atlas;
+    const void* matrices;
+    const void* config;
+    uint32_t size;
+    uint32_t layers;
+    uint32_t max_shadow_lights;
+    uint32_t reserved; /* must be 0 */
+} hl_shadow_maps;
+
+/* hl_shade with the shadow term of fs_main's light loop (deferred_lighting.wgsl:452-565,
+ * 1136-1141): each lit (pixel, light) pair is scaled by shadow_factor, for lights with
+ * index < max_shadow_lights and shadow_index != HL_NO_SHADOW: the world position offset
+ * along N by 0.01 (1 - N.L), projected by the light's matrix (point lights: the cube
+ * face of the largest axis of the offset from the light; directional lights: the CSM
+ * cascade of the distance to the camera against globals.csm_splits, blended over 10 %
+ * zones), then Vogel-disk PCF (sample_cascade_shadow, :283-329) or, for directional
+ * cascades with PCSS enabled and a light size, PCSS (:331-450) over both atlases with
+ * a LessEqual, bilinear, clamp-to-edge comparison, lit = min(dynamic, static). Points
+ * outside a layer's [0,1] uv or depth range are lit. A layer index >= layers is
+ * skipped (lit) and reported through hl_sync_status (HL_ERR_DEVICE_BOUNDS). With
+ * shadows == NULL this is hl_shade. */
+hl_status hl_shade_shadowed(hl_ctx* ctx, const void* camera, const void* globals, const hl_gbuffer* gbuffer,
+                            const void* lights, uint32_t n_lights, const hl_light_grid* grid,
+                            const hl_shadow_maps* shadows, const hl_target* radiance, void* stream);
+
 /* Per-pixel pair statistics of the same shading pass, for FLOP accounting: for every
  * pixel (x,y), counts[(y*W+x)*3 + {0,1,2}] = lights listed for the pixel, lights in
  * range (the reference's light-loop test, deferred_lighting.wgsl:1128-1131), and full

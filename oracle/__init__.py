@@ -22,7 +22,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 BUILD_DIR = HERE / "_build"
 LIB_PATH = BUILD_DIR / "liboracle.so"
-SOURCES = [HERE / "oracle.cpp", HERE / "gbuffer_write.cpp"]
+SOURCES = [HERE / "oracle.cpp", HERE / "gbuffer_write.cpp", HERE / "shadow_factor.h"]
 
 _lock = threading.Lock()
 _lib = None
@@ -38,7 +38,7 @@ def build(force: bool = False) -> Path:
     cmd = [
         "g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
         "-ffp-contract=off", "-fno-fast-math", "-fno-strict-aliasing",
-        *map(str, SOURCES), "-o", str(tmp),
+        *[str(p) for p in SOURCES if p.suffix == ".cpp"], "-o", str(tmp),
     ]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB_PATH)
@@ -63,6 +63,8 @@ def _bind(l):
     shade_args = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, f64p, u32p, u32, u32]
     l.oracle_shade_f64.argtypes = shade_args
     l.oracle_shade_f32.argtypes = shade_args
+    l.oracle_shade_shadowed_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, vp, f64p,
+                                            u32p, u32, u32, vp]
     l.oracle_shade_adjoint_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, f64p, f64p, f64p]
     frag_args = [vp, vp, vp, u32, vp, u32, u32p, vp, u32, u32, u32p, u32p, vp, f64p]
     l.oracle_shade_fragments_f64.argtypes = frag_args
@@ -168,6 +170,38 @@ def shade(camera_rec, globals_rec, gb, lights, grid, precision="f64", rows=None,
        _ptr(lts) if len(lts) else None, len(lts), kind, _ptr(lists), _ptr(counts),
        _ptr(params) if params is not None else None, _ptr(out), _ptr(pc) if pc is not None else None, r0, r1)
     return (out, pc) if pair_counts else out
+
+
+def shade_shadowed(camera_rec, globals_rec, gb, lights, grid, shadows, rows=None, pair_counts=False):
+    """``shade`` (f64) with the shadow term. ``shadows``: dict with numpy arrays
+    ``dynamic`` and ``static`` (layers, size, size) float32, ``matrices`` (layers, 16)
+    float32 column-major, ``config`` (a SHADOW_CONFIG record) and ``max_lights``.
+    Returns (radiance, pair_counts or None, bounds_flag)."""
+    from helio_gb300 import layouts as L
+
+    W, H = gb.width, gb.height
+    r0, r1 = (0, H) if rows is None else rows
+    out = np.full((H, W, 4), np.nan, np.float64)
+    pc = np.zeros((H, W, 3), np.uint32) if pair_counts else None
+    arrs, ptrs, pitch = _planes(gb)
+    kind, lists, counts, params = _grid_args(grid)
+    lts = np.ascontiguousarray(lights)
+    dyn = np.ascontiguousarray(shadows["dynamic"], np.float32)
+    sta = np.ascontiguousarray(shadows["static"], np.float32)
+    mats = np.ascontiguousarray(shadows["matrices"], np.float32)
+    cfg = np.ascontiguousarray(shadows["config"])
+    desc = np.zeros(1, L.SHADOW_MAPS)
+    desc["dynamic_atlas"], desc["static_atlas"] = dyn.ctypes.data, sta.ctypes.data
+    desc["matrices"], desc["config"] = mats.ctypes.data, cfg.ctypes.data
+    desc["size"], desc["layers"] = dyn.shape[1], dyn.shape[0]
+    desc["max_shadow_lights"] = shadows["max_lights"]
+    bounds = np.zeros(1, np.int32)
+    lib().oracle_shade_shadowed_f64(_ptr(np.ascontiguousarray(camera_rec)), _ptr(np.ascontiguousarray(globals_rec)),
+                                    gb.layout, W, H, ptrs, pitch, _ptr(lts) if len(lts) else None, len(lts), kind,
+                                    _ptr(lists), _ptr(counts), _ptr(params) if params is not None else None,
+                                    _ptr(desc), _ptr(out), _ptr(pc) if pc is not None else None, r0, r1,
+                                    _ptr(bounds))
+    return out, pc, bool(bounds[0])
 
 
 def shade_fragments(camera_rec, params, fragments, lights, grid, entity_indices=None, transforms=None,

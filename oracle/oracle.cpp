@@ -36,6 +36,8 @@
 #include <omp.h>
 #endif
 
+#include "shadow_factor.h"
+
 namespace {
 
 // ----------------------------------------------------------------------------------
@@ -586,7 +588,8 @@ uint32_t froxel_of_pixel(const FroxelParams& p, const float* tab, uint32_t x, ui
 template <class T>
 void shade_impl(const void* camera, const void* globals, const GBufferDesc& g, const void* lights,
                 uint32_t n_lights, const GridDesc& grid, double* out_rgba /* W*H*4 */,
-                uint32_t* pair_counts /* W*H*3 or null */, uint32_t row0, uint32_t row1) {
+                uint32_t* pair_counts /* W*H*3 or null */, uint32_t row0, uint32_t row1,
+                const shadow_oracle::ShadowDesc* shadows = nullptr, int* shadow_bounds = nullptr) {
     Cam<T> c = load_camera<T>(camera);
     RawGlobals gl;
     std::memcpy(&gl, globals, sizeof gl);
@@ -648,7 +651,16 @@ void shade_impl(const void* camera, const void* globals, const GBufferDesc& g, c
                 }
                 ++n_range;
                 V3<T> contrib;
-                if (pbr_direct_light(l, P, N, V, F0, s.albedo, s.rough, s.metal, contrib)) ++n_full;
+                if (pbr_direct_light(l, P, N, V, F0, s.albedo, s.rough, s.metal, contrib)) {
+                    ++n_full;
+                    // the pair's shadow factor sf (deferred_lighting.wgsl:1136-1141, 819)
+                    if (shadows && idx < shadows->max_lights && l.shadow_index != shadow_oracle::kNoShadow) {
+                        const double sf = shadow_oracle::shadow_factor<T>(
+                            *shadows, idx, l.pos, l.dir, l.shadow_index, l.type, P.x, P.y, P.z, N.x, N.y, N.z,
+                            float(x) + 0.5f, float(y) + 0.5f, c.pos.x, c.pos.y, c.pos.z, gl.csm_splits, shadow_bounds);
+                        contrib = contrib * T(sf);
+                    }
+                }
                 Lo = Lo + contrib;
             }
             // Hemisphere ambient (deferred_lighting.wgsl:1196-1199) with ao * ssao(=1)
@@ -1058,6 +1070,20 @@ void oracle_shade_f64(const void* cam, const void* globals, uint32_t layout, uin
     GBufferDesc g = make_gbuf(layout, W, H, planes, pitch);
     GridDesc gr = make_grid(grid_kind, lists, counts, froxel);
     shade_impl<double>(cam, globals, g, lights, n, gr, out_rgba, pair_counts, row0, row1);
+}
+
+// oracle_shade_f64 with the shadow term; shadows: an hl_shadow_maps whose pointers are
+// host memory. *bounds is set when a shadow layer index is beyond the atlas.
+void oracle_shade_shadowed_f64(const void* cam, const void* globals, uint32_t layout, uint32_t W, uint32_t H,
+                               const void* const* planes, const uint64_t* pitch, const void* lights, uint32_t n,
+                               uint32_t grid_kind, const uint32_t* lists, const uint32_t* counts, const void* froxel,
+                               const void* shadows, double* out_rgba, uint32_t* pair_counts, uint32_t row0,
+                               uint32_t row1, int* bounds) {
+    GBufferDesc g = make_gbuf(layout, W, H, planes, pitch);
+    GridDesc gr = make_grid(grid_kind, lists, counts, froxel);
+    *bounds = 0;
+    shade_impl<double>(cam, globals, g, lights, n, gr, out_rgba, pair_counts, row0, row1,
+                       static_cast<const shadow_oracle::ShadowDesc*>(shadows), bounds);
 }
 
 void oracle_shade_f32(const void* cam, const void* globals, uint32_t layout, uint32_t W, uint32_t H, const void* const* planes,

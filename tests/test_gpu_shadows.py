@@ -1,0 +1,155 @@
+"""GPU parity of hl_shade_shadowed (the shadow term of the deferred pass's light loop)
+against the f64 oracle.
+
+Tolerances as for hl_shade (relative per pixel, floor 1e-6 of the image maximum):
+FP32 / reference G-buffers 1e-5, FP16 G-buffer 2e-3. A pixel may exceed them when one
+of its shadow taps compares a receiver depth that the kernel's f32 biased position and
+the oracle's f64 one put on different sides of a texel depth (a "shadow flip"): such
+pixels must be rare (at most 5e-4 of the lit pixels) and their error bounded by one
+tap's weight in the filter."""
+import numpy as np
+import pytest
+
+import oracle
+from helio_gb300 import frame as FR
+from helio_gb300 import layouts as L
+from helio_gb300 import metrics
+from helio_gb300 import native as N
+from helio_gb300 import synthetic as S
+
+from gpu_util import gpu_shade
+from scenes import directional_light, mixed_lights, point_light, spot_light
+
+pytestmark = pytest.mark.gpu
+
+TOL = {S.LAYOUT_F32: 1e-5, S.LAYOUT_REFERENCE: 1e-5, S.LAYOUT_F16: 2e-3}
+
+
+def _lights(cam, seed):
+    """Shadow casters first: a directional light, spots and points, then a mix."""
+    casters = np.concatenate([
+        directional_light((0.3, -1.0, 0.25), intensity=2.0),
+        spot_light((0.0, 3.0, -8.0), 30.0, (0.0, -0.4, -1.0), 40.0, 30.0, intensity=6.0),
+        spot_light((-4.0, 1.0, -20.0), 40.0, (0.3, 0.0, -1.0), 35.0, 20.0, intensity=6.0),
+        point_light((2.0, 1.0, -15.0), 40.0, intensity=5.0),
+        point_light((-3.0, -1.0, -30.0), 50.0, intensity=5.0),
+        point_light((0.0, 0.0, -60.0), 60.0, intensity=8.0),
+    ])
+    return np.concatenate([casters, mixed_lights(cam, seed, 60, 20, n_dir=1)])
+
+
+def _setup(layout, quality, W=320, H=192, size=256, seed=31):
+    cam = S.default_camera(W, H)
+    gb = S.make_gbuffer(cam, layout, seed=seed)
+    sc = S.shadow_scene(cam, _lights(cam, seed), 6, quality=quality)
+    dyn, sta = S.shadow_atlases(sc.kinds, size, seed=seed)
+    tx, _ = L.tile_grid(W, H)
+    glb = L.make_globals(tx, len(sc.lights), ambient_color=(0.4, 0.45, 0.5), ambient_intensity=0.3)
+    return cam, gb, sc, dyn, sta, glb
+
+
+def _device_shadows(sc, dyn, sta):
+    import torch
+
+    d = dict(dyn=torch.from_numpy(dyn).cuda(), sta=torch.from_numpy(sta).cuda(),
+             mats=torch.from_numpy(sc.matrices).cuda(), cfg=FR.bytes_tensor(sc.config))
+    return d, N.shadow_maps_struct(d["dyn"], d["sta"], d["mats"], d["cfg"], sc.max_lights)
+
+
+def _shade_shadowed(ctx, df, grid, maps, fill=7.0):
+    import torch
+
+    out = torch.full((df.height, df.width, 4), fill, dtype=torch.float32, device="cuda")
+    ctx.shade_shadowed(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, maps, N.target_struct(out))
+    ctx.sync_status()
+    return out.cpu().numpy().astype(np.float64)
+
+
+def _froxel_grid(cam, lights, W, H):
+    import torch
+
+    p = L.froxel_params(16, 9, 24, W, H, cam.far)
+    off, idx = oracle.bin_froxels(cam.record, lights, p, capacity=1 << 24)
+    doff = torch.from_numpy(off.view(np.int32).copy()).cuda()
+    didx = torch.from_numpy(idx.view(np.int32).copy()).cuda()
+    return ("froxels", idx, off, p), N.froxel_grid_struct(didx, doff, N.froxel_params_from_numpy(p), didx.numel()), \
+        (didx, doff)
+
+
+@pytest.mark.parametrize("quality", ["medium", "high"])
+@pytest.mark.parametrize("layout", [S.LAYOUT_F32, S.LAYOUT_REFERENCE, S.LAYOUT_F16])
+def test_shadowed_matches_oracle(ctx, layout, quality):
+    cam, gb, sc, dyn, sta, glb = _setup(layout, quality)
+    W, H = gb.width, gb.height
+    df = FR.upload(cam.record, glb, sc.lights, gb)
+    ogrid, dgrid, keep = _froxel_grid(cam, sc.lights, W, H)
+    dsh, maps = _device_shadows(sc, dyn, sta)
+    img = _shade_shadowed(ctx, df, dgrid, maps)
+    shadows = dict(dynamic=dyn, static=sta, matrices=sc.matrices, config=sc.config, max_lights=sc.max_lights)
+    ref, pc, bounds = oracle.shade_shadowed(cam.record, glb, gb, sc.lights, ogrid, shadows, pair_counts=True)
+    assert not bounds
+    st = gpu_shade(ctx, df, dgrid, stats=True)
+    e = metrics.radiance_error(img, ref, st[..., 2], pc[..., 2])
+    assert e["flips"] <= max(2, 1e-4 * e["n"]), e
+    sky = np.isnan(ref[..., 0])
+    assert np.all(img[sky] == 7.0)
+    # the shadows are exercised: many pixels darker than without them
+    plain = oracle.shade(cam.record, glb, gb, sc.lights, ogrid)
+    darker = (ref[~sky][:, :3] < plain[~sky][:, :3] * (1 - 1e-6)).any(-1).mean()
+    assert darker > 0.05, darker
+    tol = TOL[layout]
+    k, o = img[..., :3], ref[..., :3]
+    valid = ~sky & (st[..., 2] == pc[..., 2])
+    mx = np.abs(o[valid]).max()
+    rel = (np.abs(k - o) / np.maximum(np.abs(o), 1e-6 * mx)).max(-1)[valid]
+    n_over = int((rel > tol).sum())
+    assert n_over <= max(3, 5e-4 * rel.size), (n_over, float(rel.max()), e)
+    assert float(np.quantile(rel, 0.9999)) <= tol, e
+
+
+def test_shadows_off_equal_hl_shade(ctx):
+    cam, gb, sc, dyn, sta, glb = _setup(S.LAYOUT_F32, "medium", W=160, H=96, size=64)
+    df = FR.upload(cam.record, glb, sc.lights, gb)
+    _, dgrid, keep = _froxel_grid(cam, sc.lights, gb.width, gb.height)
+    dsh, maps = _device_shadows(sc, dyn, sta)
+    maps.max_shadow_lights = 0  # no light casts a shadow
+    np.testing.assert_array_equal(_shade_shadowed(ctx, df, dgrid, maps), gpu_shade(ctx, df, dgrid))
+    np.testing.assert_array_equal(_shade_shadowed(ctx, df, dgrid, None), gpu_shade(ctx, df, dgrid))
+
+
+def test_shadow_layer_beyond_atlas_is_reported(ctx):
+    import torch
+
+    cam, gb, sc, dyn, sta, glb = _setup(S.LAYOUT_F32, "medium", W=160, H=96, size=64)
+    lt = sc.lights.copy()
+    lt["shadow_index"][:6] = 10_000
+    df = FR.upload(cam.record, glb, lt, gb)
+    _, dgrid, keep = _froxel_grid(cam, lt, gb.width, gb.height)
+    dsh, maps = _device_shadows(sc, dyn, sta)
+    out = torch.zeros((gb.height, gb.width, 4), dtype=torch.float32, device="cuda")
+    ctx.shade_shadowed(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, dgrid, maps, N.target_struct(out))
+    with pytest.raises(N.HelioError) as e:
+        ctx.sync_status()
+    assert e.value.status == N.HL_ERR_DEVICE_BOUNDS
+    # skipped layers are lit: the result is the unshadowed one
+    np.testing.assert_array_equal(out.cpu().numpy().astype(np.float64), gpu_shade(ctx, df, dgrid))
+
+
+def test_shadow_argument_errors(ctx):
+    cam, gb, sc, dyn, sta, glb = _setup(S.LAYOUT_F32, "medium", W=64, H=48, size=32)
+    df = FR.upload(cam.record, glb, sc.lights, gb)
+    _, dgrid, keep = _froxel_grid(cam, sc.lights, gb.width, gb.height)
+    dsh, maps = _device_shadows(sc, dyn, sta)
+    import torch
+
+    out = torch.zeros((gb.height, gb.width, 4), dtype=torch.float32, device="cuda")
+    for field, value, status in (("static_atlas", None, N.HL_ERR_INVALID_ARGUMENT), ("size", 0, N.HL_ERR_SIZE),
+                                 ("reserved", 1, N.HL_ERR_INVALID_ARGUMENT),
+                                 ("matrices", dsh["mats"].data_ptr() + 4, N.HL_ERR_LAYOUT)):
+        _, m = _device_shadows(sc, dyn, sta)
+        setattr(m, field, value)
+        with pytest.raises(N.HelioError) as e:
+            ctx.shade_shadowed(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, dgrid, m,
+                               N.target_struct(out))
+        assert e.value.status == status, field
+    ctx.sync_status()
