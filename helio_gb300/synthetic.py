@@ -619,7 +619,7 @@ def _look(eye, d):
     return look_at_rh(eye, np.asarray(eye, np.float64) + d, up)
 
 
-CUBE_FACES = ((1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1))  # point_light_face order
+SHADOW_CUBE_AXES = ((1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1))  # point_light_face order
 
 
 @dataclass
@@ -656,7 +656,7 @@ def shadow_scene(cam: Camera, lights: np.ndarray, n_shadowed: int, quality: str 
         d = lt["direction_outer"][i, :3].astype(np.float64)
         if typ == L.LIGHT_POINT:
             proj = perspective_rh_dx(math.radians(90.0), 1.0, 0.05, max(rng, 0.1))
-            for f, ax in enumerate(CUBE_FACES):
+            for f, ax in enumerate(SHADOW_CUBE_AXES):
                 mats[base + f] = _cols(proj @ _look(pos, ax))
         elif typ == L.LIGHT_SPOT:
             half = math.acos(min(max(float(lt["direction_outer"][i, 3]), -1.0), 1.0))
