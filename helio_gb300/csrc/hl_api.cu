@@ -47,8 +47,9 @@ hl_status shade_common(hl_ctx* ctx, const void* camera, const void* globals, con
                         m.layers, m.size);
         if (m.reserved != 0) return fail(ctx, HL_ERR_INVALID_ARGUMENT, "shadow maps: reserved field must be 0");
         sv = hl::ShadowView{m.dynamic_atlas, m.static_atlas, static_cast<const float*>(m.matrices),
-                            static_cast<const unsigned char*>(m.config), ctx->d_status, m.size, m.layers,
-                            m.max_shadow_lights, float(m.size)};
+                            static_cast<const unsigned char*>(m.config), ctx->d_status,
+                            reinterpret_cast<const float*>(static_cast<const unsigned char*>(globals) + 64), m.size,
+                            m.layers, m.max_shadow_lights, float(m.size)};
     }
     DeviceGuard dg(ctx->device);
     if (!dg.ok) return fail(ctx, HL_ERR_CUDA, "cudaSetDevice(%d) failed", ctx->device);

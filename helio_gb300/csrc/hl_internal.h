@@ -75,6 +75,7 @@ struct ShadowView {
     const float* mats;           // GpuShadowMatrix[layers], 16 floats each, column major
     const unsigned char* cfg;    // ShadowConfig, 80 bytes
     int* status;
+    const float* csm;            // DeferredGlobals.csm_splits (device)
     uint32_t size, layers, max_lights;
     float fsize;                 // float(size): the shader's ATLAS_SIZE
 };

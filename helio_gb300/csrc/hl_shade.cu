@@ -183,8 +183,7 @@ __device__ __noinline__ int precise_pair(const GpuCamera* cam, uint32_t x, uint3
 template <uint32_t LAYOUT, bool STATS, int TW, int NPX, bool SHADOW>
 __device__ __noinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>()>& s, const uint32_t* queue, uint32_t head, uint32_t nb,
                                          uint32_t lane, const GpuCamera* cam, const GpuLight* lights, uint32_t x0,
-                                         uint32_t y0, float W, float H, const DeferredGlobals* glb,
-                                         const ShadowView* sv) {
+                                         uint32_t y0, float W, float H, const ShadowView* sv) {
     using namespace sk;
     constexpr bool PRECISE = (LAYOUT != HL_GBUF_F16);
     uint32_t (*cnt)[NPX] = reinterpret_cast<uint32_t (*)[NPX]>(s.acc);
@@ -221,13 +220,21 @@ __device__ __noinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>
             st = precise_pair(cam, x0 + q % TW, y0 + q / TW, W, H, dq, p, s.px[F_AR][q], s.px[F_AG][q],
                               s.px[F_AB][q], l, ux.lo, uy.lo, uz.lo, cr, cg, cb);
         if (SHADOW && st == kLit && li < sv->max_lights && d.x != HL_NO_SHADOW) {
-            // the pair's shadow factor (deferred_lighting.wgsl:1136-1141) at the pixel's f32
-            // world position (camera-relative on the fast path)
+            // the pair's shadow factor (deferred_lighting.wgsl:1136-1141) at the pixel's world
+            // position rounded to f32: on the fast path from a precise reconstruction, since
+            // the camera-relative f32 position can be ~1e-5 off, enough to move a receiver
+            // across a shadow texel's depth
             const float camx = cam->position_near[0], camy = cam->position_near[1], camz = cam->position_near[2];
-            const float wx = PRECISE ? p.Px + p.Plx : camx + (p.Px + p.Plx);
-            const float wy = PRECISE ? p.Py + p.Ply : camy + (p.Py + p.Ply);
-            const float wz = PRECISE ? p.Pz + p.Plz : camz + (p.Pz + p.Plz);
-            const float4 csm = *reinterpret_cast<const float4*>(glb->csm_splits);
+            float wx = p.Px + p.Plx, wy = p.Py + p.Ply, wz = p.Pz + p.Plz;
+            if (!PRECISE) {
+                float hx, hy, hz, lx, ly, lz;
+                reconstruct<true>(cam->inv_view_proj, x0 + q % TW, y0 + q / TW, W, H, fabsf(dq), hx, hy, hz, lx, ly,
+                                  lz);
+                wx = hx + lx;
+                wy = hy + ly;
+                wz = hz + lz;
+            }
+            const float4 csm = __ldg(reinterpret_cast<const float4*>(sv->csm));
             const float sf = shadow_factor(*sv, li, a, b, d.x, d.y, wx, wy, wz, p.Nx, p.Ny, p.Nz,
                                            float(x0 + q % TW) + 0.5f, float(y0 + q / TW) + 0.5f, camx, camy, camz, csm);
             cr *= sf;
@@ -533,7 +540,7 @@ __device__ __forceinline__ void shade_tile(
                     qlen += __popc(pm);
                     __syncwarp();
                     if (qlen >= 32) {
-                        flush_batch<LAYOUT, STATS, TW, NPX, SHADOW>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H, glb, sv);
+                        flush_batch<LAYOUT, STATS, TW, NPX, SHADOW>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H, sv);
                         head += 32;
                         qlen -= 32;
                     }
@@ -568,13 +575,13 @@ __device__ __forceinline__ void shade_tile(
             }
             __syncwarp();
             while (qlen >= 32) {
-                flush_batch<LAYOUT, STATS, TW, NPX, SHADOW>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H, glb, sv);
+                flush_batch<LAYOUT, STATS, TW, NPX, SHADOW>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H, sv);
                 head += 32;
                 qlen -= 32;
             }
         }
     }
-    if (qlen > 0) flush_batch<LAYOUT, STATS, TW, NPX, SHADOW>(s, queue, head, qlen, lane, cam, lights, x0, y0, W, H, glb, sv);
+    if (qlen > 0) flush_batch<LAYOUT, STATS, TW, NPX, SHADOW>(s, queue, head, qlen, lane, cam, lights, x0, y0, W, H, sv);
 
     // ---- 5. output -----------------------------------------------------------------
     __syncthreads();
