@@ -18,7 +18,8 @@ using namespace hl_host;
 
 hl_status shade_common(hl_ctx* ctx, const void* camera, const void* globals, const hl_gbuffer* gbuffer,
                        const void* lights, uint32_t n_lights, const hl_light_grid* grid, const hl_target* radiance,
-                       uint32_t* stats, void* stream, const hl_shadow_maps* shadows = nullptr) {
+                       uint32_t* stats, void* stream, const hl_shadow_maps* shadows = nullptr,
+                       const hl_rc_cascade* rc = nullptr) {
     hl_status s = check_common(ctx, camera, lights, n_lights);
     if (s != HL_OK) return s;
     if (!globals || !aligned(globals, 16)) return fail(ctx, HL_ERR_INVALID_ARGUMENT, "globals is NULL or misaligned");
@@ -34,7 +35,7 @@ hl_status shade_common(hl_ctx* ctx, const void* camera, const void* globals, con
     } else if (!aligned(stats, 4)) {
         return fail(ctx, HL_ERR_LAYOUT, "stats pointer not 4-byte aligned");
     }
-    hl::ShadowView sv{};
+    hl::ExtView sv{};
     if (shadows) {
         const hl_shadow_maps& m = *shadows;
         if (!m.dynamic_atlas || !m.static_atlas || !m.matrices || !m.config)
@@ -46,10 +47,22 @@ hl_status shade_common(hl_ctx* ctx, const void* camera, const void* globals, con
             return fail(ctx, HL_ERR_SIZE, "shadow maps: %u layers of %u texels (1..65536 layers, 1..16384 texels)",
                         m.layers, m.size);
         if (m.reserved != 0) return fail(ctx, HL_ERR_INVALID_ARGUMENT, "shadow maps: reserved field must be 0");
-        sv = hl::ShadowView{m.dynamic_atlas, m.static_atlas, static_cast<const float*>(m.matrices),
+        sv = hl::ExtView{m.dynamic_atlas, m.static_atlas, static_cast<const float*>(m.matrices),
                             static_cast<const unsigned char*>(m.config), ctx->d_status,
                             reinterpret_cast<const float*>(static_cast<const unsigned char*>(globals) + 64), m.size,
                             m.layers, m.max_shadow_lights, float(m.size)};
+    }
+    if (rc) {
+        const uint32_t need_w = HL_RC_PROBE_DIM * HL_RC_DIR_DIM, need_h = HL_RC_PROBE_DIM * HL_RC_PROBE_DIM * HL_RC_DIR_DIM;
+        if (!rc->texels) return fail(ctx, HL_ERR_INVALID_ARGUMENT, "rc cascade texels are NULL");
+        if (!aligned(rc->texels, 8) || rc->pitch % 8 != 0)
+            return fail(ctx, HL_ERR_LAYOUT, "rc cascade pointer/pitch not 8-byte aligned (RGBA16F)");
+        if (rc->width < need_w || rc->height < need_h || rc->pitch < uint64_t(rc->width) * 8)
+            return fail(ctx, HL_ERR_SIZE, "rc cascade is %ux%u (pitch %llu), needs at least %ux%u", rc->width,
+                        rc->height, (unsigned long long)rc->pitch, need_w, need_h);
+        sv.rc = static_cast<const unsigned char*>(rc->texels);
+        sv.rc_pitch = rc->pitch;
+        sv.status = ctx->d_status;
     }
     DeviceGuard dg(ctx->device);
     if (!dg.ok) return fail(ctx, HL_ERR_CUDA, "cudaSetDevice(%d) failed", ctx->device);
@@ -58,7 +71,7 @@ hl_status shade_common(hl_ctx* ctx, const void* camera, const void* globals, con
         return s;
     cudaError_t e = hl::launch_shade(gbuffer->layout, grid->kind, stats ? HL_TARGET_RGBA32F : radiance->format, camera,
                                      globals, gv, lights, n_lights, grv, tab, tv, stats, ctx->d_status,
-                                     ctx->shade_cand, as_stream(stream), shadows ? &sv : nullptr);
+                                     ctx->shade_cand, as_stream(stream), (shadows || rc) ? &sv : nullptr);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "shade launch");
     return HL_OK;
 }
@@ -217,6 +230,13 @@ hl_status hl_shade_shadowed(hl_ctx* ctx, const void* camera, const void* globals
                             const void* lights, uint32_t n_lights, const hl_light_grid* grid,
                             const hl_shadow_maps* shadows, const hl_target* radiance, void* stream) {
     return shade_common(ctx, camera, globals, gbuffer, lights, n_lights, grid, radiance, nullptr, stream, shadows);
+}
+
+hl_status hl_shade_ex(hl_ctx* ctx, const void* camera, const void* globals, const hl_gbuffer* gbuffer,
+                      const void* lights, uint32_t n_lights, const hl_light_grid* grid,
+                      const hl_shade_bindings* bindings, const hl_target* radiance, void* stream) {
+    return shade_common(ctx, camera, globals, gbuffer, lights, n_lights, grid, radiance, nullptr, stream,
+                        bindings ? bindings->shadows : nullptr, bindings ? bindings->rc : nullptr);
 }
 
 hl_status hl_shade_stats(hl_ctx* ctx, const void* camera, const void* globals, const hl_gbuffer* gbuffer,

@@ -68,8 +68,10 @@ cudaError_t launch_bin_froxels_batched(const BinViewDesc* descs, uint32_t n_view
 // Shading. layout: HL_GBUF_*, grid_kind: HL_GRID_*, target_format: HL_TARGET_*.
 // stats != nullptr selects the pair-statistics variant (no radiance written).
 // cand: n_lights float4 of scratch for the candidate-test light table.
-// The shadow bindings as the shading kernel reads them (validated by the API layer).
-struct ShadowView {
+// The pass's optional bindings as the extended shading kernel reads them (validated by
+// the API layer): shadow maps (dyn == nullptr: none) and radiance-cascade probes
+// (rc == nullptr: none).
+struct ExtView {
     const float* dyn;            // dynamic atlas, layers x size x size
     const float* sta;            // static atlas
     const float* mats;           // GpuShadowMatrix[layers], 16 floats each, column major
@@ -78,13 +80,15 @@ struct ShadowView {
     const float* csm;            // DeferredGlobals.csm_splits (device)
     uint32_t size, layers, max_lights;
     float fsize;                 // float(size): the shader's ATLAS_SIZE
+    const unsigned char* rc;     // rc_cascade0, RGBA16F
+    uint64_t rc_pitch;
 };
 
-// shadows != nullptr selects the shadowed variant (hl_shade_shadowed).
+// ext != nullptr selects the extended variant (hl_shade_ex, hl_shade_shadowed).
 cudaError_t launch_shade(uint32_t layout, uint32_t grid_kind, uint32_t target_format, const void* camera,
                          const void* globals, const GBufView& gb, const void* lights, uint32_t n_lights,
                          const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats,
-                         int* status, float4* cand, cudaStream_t stream, const ShadowView* shadows = nullptr);
+                         int* status, float4* cand, cudaStream_t stream, const ExtView* ext = nullptr);
 
 // Adjoint of shading. partials: grid_size * n_lights * 8 floats of scratch.
 uint32_t adjoint_grid_size(int device, uint32_t width, uint32_t height);

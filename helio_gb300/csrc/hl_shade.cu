@@ -18,6 +18,7 @@
 #include "hl_common.cuh"
 #include "hl_internal.h"
 #include "hl_shade_math.cuh"
+#include "hl_indirect.cuh"
 #include "hl_shadow.cuh"
 #include "hl_texel.cuh"
 
@@ -180,10 +181,10 @@ __device__ __noinline__ int precise_pair(const GpuCamera* cam, uint32_t x, uint3
 // Evaluates nb queued pairs (ring positions head..head+nb-1), one per lane, and adds
 // them into the per-pixel Kahan accumulators in queue order. Out of line so that the
 // BRDF code exists once in the kernel.
-template <uint32_t LAYOUT, bool STATS, int TW, int NPX, bool SHADOW>
+template <uint32_t LAYOUT, bool STATS, int TW, int NPX, bool EXT>
 __device__ __noinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>()>& s, const uint32_t* queue, uint32_t head, uint32_t nb,
                                          uint32_t lane, const GpuCamera* cam, const GpuLight* lights, uint32_t x0,
-                                         uint32_t y0, float W, float H, const ShadowView* sv) {
+                                         uint32_t y0, float W, float H, const ExtView* sv) {
     using namespace sk;
     constexpr bool PRECISE = (LAYOUT != HL_GBUF_F16);
     uint32_t (*cnt)[NPX] = reinterpret_cast<uint32_t (*)[NPX]>(s.acc);
@@ -219,7 +220,7 @@ __device__ __noinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>
         if (!PRECISE && st == kNeedsPrecise)
             st = precise_pair(cam, x0 + q % TW, y0 + q / TW, W, H, dq, p, s.px[F_AR][q], s.px[F_AG][q],
                               s.px[F_AB][q], l, ux.lo, uy.lo, uz.lo, cr, cg, cb);
-        if (SHADOW && st == kLit && li < sv->max_lights && d.x != HL_NO_SHADOW) {
+        if (EXT && sv->dyn && st == kLit && li < sv->max_lights && d.x != HL_NO_SHADOW) {
             // the pair's shadow factor (deferred_lighting.wgsl:1136-1141) at the pixel's world
             // position rounded to f32: on the fast path from a precise reconstruction, since
             // the camera-relative f32 position can be ~1e-5 off, enough to move a receiver
@@ -270,12 +271,12 @@ __device__ __noinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>
 // L2 for the G-buffer of the tile three CTAs per SM further on, the one likely to start
 // on an SM as the current wave drains, so its set-up loads hit L2.
 template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, int TW, int TH, bool PREFETCH = false,
-          bool SHADOW = false>
+          bool EXT = false>
 __device__ __forceinline__ void shade_tile(
     const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const GBufView& gb,
     const GpuLight* __restrict__ lights, const float4* __restrict__ cand, uint32_t n_lights, const GridView& grid,
     const float* __restrict__ tabz, const TargetView& out, uint32_t* __restrict__ stats, int* __restrict__ status,
-    uint32_t bx, uint32_t by, const ShadowView* sv = nullptr) {
+    uint32_t bx, uint32_t by, const ExtView* sv = nullptr) {
     using namespace sk;
     constexpr bool FROXELS = (GRID == HL_GRID_FROXELS);
     constexpr int NPX = TW * TH;
@@ -540,7 +541,7 @@ __device__ __forceinline__ void shade_tile(
                     qlen += __popc(pm);
                     __syncwarp();
                     if (qlen >= 32) {
-                        flush_batch<LAYOUT, STATS, TW, NPX, SHADOW>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H, sv);
+                        flush_batch<LAYOUT, STATS, TW, NPX, EXT>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H, sv);
                         head += 32;
                         qlen -= 32;
                     }
@@ -575,18 +576,20 @@ __device__ __forceinline__ void shade_tile(
             }
             __syncwarp();
             while (qlen >= 32) {
-                flush_batch<LAYOUT, STATS, TW, NPX, SHADOW>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H, sv);
+                flush_batch<LAYOUT, STATS, TW, NPX, EXT>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H, sv);
                 head += 32;
                 qlen -= 32;
             }
         }
     }
-    if (qlen > 0) flush_batch<LAYOUT, STATS, TW, NPX, SHADOW>(s, queue, head, qlen, lane, cam, lights, x0, y0, W, H, sv);
+    if (qlen > 0) flush_batch<LAYOUT, STATS, TW, NPX, EXT>(s, queue, head, qlen, lane, cam, lights, x0, y0, W, H, sv);
 
     // ---- 5. output -----------------------------------------------------------------
     __syncthreads();
     const uint32_t debug_mode = glb->debug_mode;
-    if (!STATS && t == 0 && (glb->has_rc_gi != 0u || debug_mode == 10u || debug_mode == 11u))
+    bool rc_ok = false;  // radiance-cascade GI bound and enabled
+    if (EXT) rc_ok = sv->rc != nullptr && glb->has_rc_gi != 0u;
+    if (!STATS && t == 0 && ((glb->has_rc_gi != 0u && !rc_ok) || debug_mode == 10u || debug_mode == 11u))
         raise_status(status, HL_ERR_NOT_SUPPORTED);
 #pragma unroll
     for (int k = 0; k < PPT; ++k) {
@@ -625,9 +628,27 @@ __device__ __forceinline__ void shade_tile(
                     skb = glb->ambient_color[2] * amb;
         const float ht = fma_(ny, 0.5f, 0.5f);
         // hemisphere ambient (deferred_lighting.wgsl:1196-1199) times ao (x white SSAO)
-        const float hr = fma_(skr, ht, skr * 0.15f * (1.0f - ht)) * tx.ar;
-        const float hg = fma_(skg, ht, skg * 0.15f * (1.0f - ht)) * tx.ag;
-        const float hb = fma_(skb, ht, skb * 0.15f * (1.0f - ht)) * tx.ab;
+        float hr = fma_(skr, ht, skr * 0.15f * (1.0f - ht)) * tx.ar;
+        float hg = fma_(skg, ht, skg * 0.15f * (1.0f - ht)) * tx.ag;
+        float hb = fma_(skb, ht, skb * 0.15f * (1.0f - ht)) * tx.ab;
+        if (EXT && rc_ok) {
+            // radiance-cascade indirect diffuse blended over the hemisphere ambient
+            // (deferred_lighting.wgsl:1159-1163, 1197-1209)
+            const float camx = cam->position_near[0], camy = cam->position_near[1], camz = cam->position_near[2];
+            const float wx = PRECISE ? s.px[F_PX][i] + s.px[F_PLX][i] : camx + (s.px[F_PX][i] + s.px[F_PLX][i]);
+            const float wy = PRECISE ? s.px[F_PY][i] + s.px[F_PLY][i] : camy + (s.px[F_PY][i] + s.px[F_PLY][i]);
+            const float wz = PRECISE ? s.px[F_PZ][i] + s.px[F_PLZ][i] : camz + (s.px[F_PZ][i] + s.px[F_PLZ][i]);
+            const float metal = s.px[F_METAL][i];
+            float f0r, f0g, f0b;
+            if (int(NF) > int(F_F0R)) {
+                f0r = s.px[F_F0R][i]; f0g = s.px[F_F0G][i]; f0b = s.px[F_F0B][i];
+            } else {
+                f0r = metallic_f0(tx.ar, metal); f0g = metallic_f0(tx.ag, metal); f0b = metallic_f0(tx.ab, metal);
+            }
+            rc::ambient(*sv, glb, wx, wy, wz, nxo, ny, nzo, s.px[F_NDV][i], s.px[F_ROUGH][i], metal,
+                        fmin_(fmax_(f0r, 0.0f), 0.999f), fmin_(fmax_(f0g, 0.0f), 0.999f), fmin_(fmax_(f0b, 0.0f), 0.999f),
+                        tx.ar, tx.ag, tx.ab, hr, hg, hb);
+        }
         float4 c;
         c.x = (s.acc[0][i] + fma_(hr, tx.ao, 0.0f)) + tx.er;
         c.y = (s.acc[1][i] + fma_(hg, tx.ao, 0.0f)) + tx.eg;
@@ -652,13 +673,13 @@ __device__ __forceinline__ void shade_tile(
     }
 }
 
-template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, int TW, int TH, bool SHADOW>
+template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, int TW, int TH, bool EXT>
 __global__ void __launch_bounds__(sk::kThreads, 3) shade_kernel(
     const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const GBufView gb,
     const GpuLight* __restrict__ lights, uint32_t n_lights, const GridView grid, const __grid_constant__ SliceTable tab,
     const TargetView out, uint32_t* __restrict__ stats, int* __restrict__ status, const float4* __restrict__ cand,
-    const __grid_constant__ ShadowView sv) {
-    shade_tile<LAYOUT, GRID, TARGET, STATS, TW, TH, true, SHADOW>(cam, glb, gb, lights, cand, n_lights, grid, tab.z,
+    const __grid_constant__ ExtView sv) {
+    shade_tile<LAYOUT, GRID, TARGET, STATS, TW, TH, true, EXT>(cam, glb, gb, lights, cand, n_lights, grid, tab.z,
                                                                   out, stats, status, blockIdx.x, blockIdx.y, &sv);
 }
 
@@ -734,13 +755,13 @@ cudaError_t launch_batched(const ShadeViewDesc* descs, uint32_t n_views, uint32_
     return cudaGetLastError();
 }
 
-template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, bool SHADOW = false>
+template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, bool EXT = false>
 cudaError_t launch_one(const void* camera, const void* globals, const GBufView& gb, const void* lights, uint32_t n,
                        const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats, int* status, float4* cand,
-                       cudaStream_t stream, const ShadowView* sv = nullptr) {
+                       cudaStream_t stream, const ExtView* sv = nullptr) {
     constexpr bool FROXELS = (GRID == HL_GRID_FROXELS);
     constexpr int TW = FROXELS ? 32 : 16, TH = 16;
-    auto kern = shade_kernel<LAYOUT, GRID, TARGET, STATS, TW, TH, SHADOW>;
+    auto kern = shade_kernel<LAYOUT, GRID, TARGET, STATS, TW, TH, EXT>;
     const int smem = int(sizeof(sk::Smem<TW * TH, sk::record_fields<LAYOUT>()>));
     static unsigned long long attr_devices = 0;  // devices on which the smem limit is raised
     int dev = 0;
@@ -757,7 +778,7 @@ cudaError_t launch_one(const void* camera, const void* globals, const GBufView& 
         if (e != cudaSuccess) return e;
     }
     const dim3 g((gb.width + TW - 1) / TW, (gb.height + TH - 1) / TH);
-    ShadowView svv{};
+    ExtView svv{};
     if (sv) svv = *sv;
     return launch_pdl(kern, g, dim3(sk::kThreads), smem, stream, static_cast<const GpuCamera*>(camera),
                       static_cast<const DeferredGlobals*>(globals), gb, static_cast<const GpuLight*>(lights), n, grid,
@@ -768,7 +789,7 @@ template <uint32_t LAYOUT, uint32_t GRID>
 cudaError_t dispatch_target(uint32_t target, const void* camera, const void* globals, const GBufView& gb,
                             const void* lights, uint32_t n, const GridView& grid, const SliceTable& tab,
                             const TargetView& out, uint32_t* stats, int* status, float4* cand, cudaStream_t stream,
-                            const ShadowView* sv) {
+                            const ExtView* sv) {
     if (sv && !stats) {
         if (target == HL_TARGET_RGBA16F)
             return launch_one<LAYOUT, GRID, HL_TARGET_RGBA16F, false, true>(camera, globals, gb, lights, n, grid, tab,
@@ -790,7 +811,7 @@ template <uint32_t LAYOUT>
 cudaError_t dispatch_grid(uint32_t grid_kind, uint32_t target, const void* camera, const void* globals,
                           const GBufView& gb, const void* lights, uint32_t n, const GridView& grid,
                           const SliceTable& tab, const TargetView& out, uint32_t* stats, int* status, float4* cand,
-                          cudaStream_t stream, const ShadowView* sv) {
+                          cudaStream_t stream, const ExtView* sv) {
     if (grid_kind == HL_GRID_FROXELS)
         return dispatch_target<LAYOUT, HL_GRID_FROXELS>(target, camera, globals, gb, lights, n, grid, tab, out, stats,
                                                         status, cand, stream, sv);
@@ -803,7 +824,7 @@ cudaError_t dispatch_grid(uint32_t grid_kind, uint32_t target, const void* camer
 cudaError_t launch_shade(uint32_t layout, uint32_t grid_kind, uint32_t target_format, const void* camera,
                          const void* globals, const GBufView& gb, const void* lights, uint32_t n_lights,
                          const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats,
-                         int* status, float4* cand, cudaStream_t stream, const ShadowView* shadows) {
+                         int* status, float4* cand, cudaStream_t stream, const ExtView* shadows) {
     switch (layout) {
         case HL_GBUF_REFERENCE:
             return dispatch_grid<HL_GBUF_REFERENCE>(grid_kind, target_format, camera, globals, gb, lights, n_lights,

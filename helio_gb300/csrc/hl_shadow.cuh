@@ -77,7 +77,7 @@ __device__ __forceinline__ bool project(const float* m, float px, float py, floa
     return u >= 0.0f && v >= 0.0f && u <= 1.0f && v <= 1.0f && z >= 0.0f && z <= 1.0f;
 }
 
-__device__ __forceinline__ bool layer_ok(const ShadowView& sv, uint32_t layer) {
+__device__ __forceinline__ bool layer_ok(const ExtView& sv, uint32_t layer) {
     if (layer < sv.layers) return true;
     raise_status(sv.status, HL_ERR_DEVICE_BOUNDS);
     return false;
@@ -87,7 +87,7 @@ __device__ __forceinline__ bool layer_ok(const ShadowView& sv, uint32_t layer) {
 // counts above kMaxSamples are rejected (lit, HL_ERR_SIZE) so that no launch loops for
 // long on a corrupt configuration.
 constexpr uint32_t kMaxSamples = 1024;
-__device__ __forceinline__ float pcf(const ShadowView& sv, uint32_t layer, float u, float v, float ref, float radius,
+__device__ __forceinline__ float pcf(const ExtView& sv, uint32_t layer, float u, float v, float ref, float radius,
                                      uint32_t count, float theta) {
     if (count > kMaxSamples) {
         raise_status(sv.status, HL_ERR_SIZE);
@@ -106,15 +106,15 @@ __device__ __forceinline__ float pcf(const ShadowView& sv, uint32_t layer, float
     return lit / float(count);
 }
 
-__device__ __forceinline__ uint32_t cfg_u32(const ShadowView& sv, int word) {
+__device__ __forceinline__ uint32_t cfg_u32(const ExtView& sv, int word) {
     return __ldg(reinterpret_cast<const uint32_t*>(sv.cfg) + word);
 }
-__device__ __forceinline__ float cfg_f32(const ShadowView& sv, int word) {
+__device__ __forceinline__ float cfg_f32(const ExtView& sv, int word) {
     return __ldg(reinterpret_cast<const float*>(sv.cfg) + word);
 }
 
 // sample_cascade_shadow (:264-329).
-static __device__ float sample_cascade(const ShadowView& sv, uint32_t layer, uint32_t cascade, float scale, float px,
+static __device__ float sample_cascade(const ExtView& sv, uint32_t layer, uint32_t cascade, float scale, float px,
                                 float py, float pz, float fx, float fy) {
     if (!layer_ok(sv, layer)) return 1.0f;
     float u, v, z;
@@ -130,7 +130,7 @@ static __device__ float sample_cascade(const ShadowView& sv, uint32_t layer, uin
 }
 
 // sample_cascade_shadow_pcss (:393-450) with pcss_blocker_search (:334-377).
-static __device__ float sample_cascade_pcss(const ShadowView& sv, uint32_t layer, uint32_t cascade, float px, float py,
+static __device__ float sample_cascade_pcss(const ExtView& sv, uint32_t layer, uint32_t cascade, float px, float py,
                                      float pz, float fx, float fy) {
     if (!layer_ok(sv, layer)) return 1.0f;
     float u, v, z;
@@ -180,7 +180,7 @@ __device__ __forceinline__ float smoothstep_(float lo, float hi, float x) {
 }
 
 // One directional cascade: PCSS when enabled for it, else PCF with its scale.
-static __device__ float directional_cascade(const ShadowView& sv, uint32_t shadow_index, uint32_t c, float bx, float by,
+static __device__ float directional_cascade(const ExtView& sv, uint32_t shadow_index, uint32_t c, float bx, float by,
                                      float bz, float fx, float fy) {
     const bool pcss = cfg_u32(sv, 16) != 0u && cfg_f32(sv, 4 * int(c) + 3) > 0.0f;
     if (pcss) return sample_cascade_pcss(sv, shadow_index + c, c, bx, by, bz, fx, fy);
@@ -192,7 +192,7 @@ static __device__ float directional_cascade(const ShadowView& sv, uint32_t shado
 // shadow_factor (:452-565) of light `li` at world position w with unit normal n, for the
 // fragment at pixel centre (fx, fy). Out of line: the shading kernels call it for lit
 // pairs of shadow-casting lights only.
-static __device__ __noinline__ float shadow_factor(const ShadowView& sv, uint32_t li, float4 pos_range, float4 dir_outer,
+static __device__ __noinline__ float shadow_factor(const ExtView& sv, uint32_t li, float4 pos_range, float4 dir_outer,
                                             uint32_t shadow_index, uint32_t type, float wx, float wy, float wz,
                                             float nx, float ny, float nz, float fx, float fy, float camx, float camy,
                                             float camz, float4 csm) {

@@ -277,6 +277,10 @@ SHADOW_MAPS = np.dtype(
         ("reserved", "<u4"),
     ]
 )
+# hl_rc_cascade (include/helio_gb300.h): the radiance-cascade probe texture rc_cascade0
+RC_CASCADE = np.dtype([("texels", "<u8"), ("pitch", "<u8"), ("width", "<u4"), ("height", "<u4")])
+RC_PROBE_DIM, RC_DIR_DIM = 16, 4  # deferred_lighting.wgsl:824-825
+
 SHADOW_ATLAS_SIZE = 1024  # the shader's ATLAS_SIZE (deferred_lighting.wgsl:235)
 MAX_SHADOW_LIGHTS = 42    # MAX_SHADOW_LIGHTS (deferred_lighting.wgsl:20)
 
@@ -325,6 +329,7 @@ EXPECTED_SIZES = {
     "TEXTURE": 40,
     "SHADOW_CONFIG": 80,
     "SHADOW_MAPS": 48,
+    "RC_CASCADE": 24,
 }
 
 for _name, _size in EXPECTED_SIZES.items():

@@ -103,6 +103,16 @@ class ShadowMaps(C.Structure):
                 ("max_shadow_lights", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class RcCascade(C.Structure):
+    """hl_rc_cascade: the radiance-cascade probe texture (RGBA16F)."""
+    _fields_ = [("texels", C.c_void_p), ("pitch", C.c_uint64), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class ShadeBindings(C.Structure):
+    """hl_shade_bindings: optional shadow maps and radiance-cascade probes."""
+    _fields_ = [("shadows", C.POINTER(ShadowMaps)), ("rc", C.POINTER(RcCascade))]
+
+
 class GBufferTargets(C.Structure):
     """hl_gbuffer_targets: albedo, normal, orm, emissive (required), lightmap_uv, sss,
     extra, velocity (optional)."""
@@ -115,7 +125,7 @@ EXPORTS = [
     "hl_tile_count", "hl_bin_tiles_ref", "hl_froxel_slice_table", "hl_bin_froxels", "hl_shade", "hl_shade_stats",
     "hl_shade_adjoint", "hl_batch_plan_create", "hl_batch_execute", "hl_batch_plan_view_grid",
     "hl_batch_plan_destroy", "hl_probe_fp32_peak", "hl_bin_froxels_noalloc", "hl_shade_fragments",
-    "hl_write_gbuffer", "hl_shade_shadowed",
+    "hl_write_gbuffer", "hl_shade_shadowed", "hl_shade_ex",
 ]
 
 _lock = threading.Lock()
@@ -188,6 +198,8 @@ def _bind(l):
     l.hl_write_gbuffer.restype = i32
     l.hl_shade_shadowed.argtypes = [vp, vp, vp, P(GBuffer), vp, u32, P(LightGrid), P(ShadowMaps), P(Target), vp]
     l.hl_shade_shadowed.restype = i32
+    l.hl_shade_ex.argtypes = [vp, vp, vp, P(GBuffer), vp, u32, P(LightGrid), P(ShadeBindings), P(Target), vp]
+    l.hl_shade_ex.restype = i32
 
 
 def status_string(status: int) -> str:
@@ -308,6 +320,16 @@ class Context:
         self._check(self._l.hl_shade_shadowed(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer), _ptr(lights),
                                               n_lights, C.byref(grid), C.byref(shadows) if shadows else None,
                                               C.byref(target), _stream(stream)), "hl_shade_shadowed")
+
+    def shade_ex(self, camera, globals_, gbuffer: GBuffer, lights, n_lights, grid: LightGrid, target: Target,
+                 shadows: "ShadowMaps" = None, rc: "RcCascade" = None, stream=None):
+        """hl_shade with the optional bindings (shadow maps, radiance-cascade probes)."""
+        b = ShadeBindings()
+        b.shadows = C.pointer(shadows) if shadows is not None else None
+        b.rc = C.pointer(rc) if rc is not None else None
+        self._check(self._l.hl_shade_ex(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer), _ptr(lights),
+                                        n_lights, C.byref(grid), C.byref(b), C.byref(target), _stream(stream)),
+                    "hl_shade_ex")
 
     def shade_stats(self, camera, globals_, gbuffer: GBuffer, lights, n_lights, grid: LightGrid, counts, stream=None):
         self._check(self._l.hl_shade_stats(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer), _ptr(lights),
@@ -433,6 +455,15 @@ def shadow_maps_struct(dynamic, static, matrices, config, max_shadow_lights: int
     m.layers, m.size = int(dynamic.shape[0]), int(dynamic.shape[1])
     m.max_shadow_lights = max_shadow_lights
     return m
+
+
+def rc_cascade_struct(texels) -> RcCascade:
+    """``texels``: a device float16 tensor (height, width, 4)."""
+    r = RcCascade()
+    r.texels = _ptr(texels)
+    r.pitch = int(texels.stride(0) * texels.element_size())
+    r.height, r.width = int(texels.shape[0]), int(texels.shape[1])
+    return r
 
 
 def gbuffer_targets_struct(width: int, height: int, planes) -> GBufferTargets:

@@ -703,3 +703,33 @@ def shadow_atlases(kinds, size: int, seed: int, xp=np, device=None):
         dyn[i] = float(lo[i]) + (1 - float(lo[i])) * a.clamp(0, 1)
         sta[i] = torch.where(b > 0.5, float(lo[i]) + (1 - float(lo[i])) * (1.5 - b), torch.ones_like(b))
     return dyn, sta
+
+
+# ----------------------------------------------------------------------------------
+# Radiance-cascade probes
+# ----------------------------------------------------------------------------------
+
+
+def rc_probes(seed: int, scale: float = 0.5) -> np.ndarray:
+    """A synthetic rc_cascade0 texture, (1024, 64, 4) float16: every probe (x, y, z) of the
+    16^3 grid and direction (dx, dy) holds a smooth irradiance in [0, scale) per channel,
+    so the RC weight clamp(4 |irradiance|, 0, 1) takes partial and full values."""
+    P, D = L.RC_PROBE_DIM, L.RC_DIR_DIM
+    x = np.arange(P * D)[None, :] / (P * D)
+    y = np.arange(P * P * D)[:, None] / (P * P * D)
+    ph = uniform(seed, 400, 6, 0.0, 2 * math.pi)
+    out = np.empty((P * P * D, P * D, 4), np.float16)
+    for ch in range(3):
+        v = 0.5 + 0.25 * np.sin(2 * math.pi * (3 * x + ph[ch])) + 0.25 * np.sin(2 * math.pi * (7 * y + ph[ch + 3]))
+        out[..., ch] = (scale * v).astype(np.float16)
+    out[..., 3] = np.float16(1.0)
+    return out
+
+
+def rc_globals(globals_rec: np.ndarray, world_min, world_max) -> np.ndarray:
+    """A copy of a DeferredGlobals with radiance-cascade GI on over the given volume."""
+    g = globals_rec.copy()
+    g["has_rc_gi"] = 1
+    g["rc_world_min"] = (*world_min, 0.0)
+    g["rc_world_max"] = (*world_max, 0.0)
+    return g

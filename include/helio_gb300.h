@@ -284,6 +284,37 @@ hl_status hl_shade_shadowed(hl_ctx* ctx, const void* camera, const void* globals
                             const void* lights, uint32_t n_lights, const hl_light_grid* grid,
                             const hl_shadow_maps* shadows, const hl_target* radiance, void* stream);
 
+/* Radiance-cascade irradiance probes the pass reads for indirect diffuse light
+ * (rc_cascade0, deferred_lighting.wgsl:168, 822-917): Rgba16Float texels, probe (x, y, z)
+ * of a 16^3 grid over [globals.rc_world_min, rc_world_max] holds 4x4 octahedral
+ * directions at column x*4 + dx, row (y*16 + z)*4 + dy. */
+#define HL_RC_PROBE_DIM 16u
+#define HL_RC_DIR_DIM 4u
+typedef struct hl_rc_cascade {
+    const void* texels;     /* device, RGBA16F, rows of `pitch` bytes                  */
+    uint64_t pitch;
+    uint32_t width, height; /* at least 64 x 1024 (probe_dim*dir_dim x probe_dim^2*dir_dim) */
+} hl_rc_cascade;
+
+/* The optional bindings of the deferred pass that hl_shade_ex reads. */
+typedef struct hl_shade_bindings {
+    const hl_shadow_maps* shadows; /* NULL: shadow factor 1                                  */
+    const hl_rc_cascade* rc;       /* NULL: no radiance-cascade GI (globals.has_rc_gi must be
+                                      0, else hl_sync_status reports HL_ERR_NOT_SUPPORTED)   */
+} hl_shade_bindings;
+
+/* hl_shade with the pass's optional bindings: the shadow term (as hl_shade_shadowed) and
+ * radiance-cascade indirect diffuse light. With rc given and globals.has_rc_gi != 0, each
+ * pixel's ambient term becomes mix(hemisphere, kD_ibl * rc_irradiance * albedo, w),
+ * w = clamp(4 |rc_irradiance|, 0, 1), kD_ibl from fresnel_schlick_roughness(NdV, F0,
+ * roughness) (pbr_eval.wgsl:63-66), rc_irradiance = sample_rc_irradiance (trilinear over
+ * the 8 probes around the pixel, cosine-weighted over their 16 directions, faded out
+ * over the volume's outer 5 %) times ao, as fs_main composes it
+ * (deferred_lighting.wgsl:1159-1228). bindings == NULL, or both NULL, is hl_shade. */
+hl_status hl_shade_ex(hl_ctx* ctx, const void* camera, const void* globals, const hl_gbuffer* gbuffer,
+                      const void* lights, uint32_t n_lights, const hl_light_grid* grid,
+                      const hl_shade_bindings* bindings, const hl_target* radiance, void* stream);
+
 /* Per-pixel pair statistics of the same shading pass, for FLOP accounting: for every
  * pixel (x,y), counts[(y*W+x)*3 + {0,1,2}] = lights listed for the pixel, lights in
  * range (the reference's light-loop test, deferred_lighting.wgsl:1128-1131), and full

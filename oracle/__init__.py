@@ -22,7 +22,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 BUILD_DIR = HERE / "_build"
 LIB_PATH = BUILD_DIR / "liboracle.so"
-SOURCES = [HERE / "oracle.cpp", HERE / "gbuffer_write.cpp", HERE / "shadow_factor.h"]
+SOURCES = [HERE / "oracle.cpp", HERE / "gbuffer_write.cpp", HERE / "shadow_factor.h", HERE / "rc_gi.h"]
 
 _lock = threading.Lock()
 _lib = None
@@ -63,8 +63,8 @@ def _bind(l):
     shade_args = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, f64p, u32p, u32, u32]
     l.oracle_shade_f64.argtypes = shade_args
     l.oracle_shade_f32.argtypes = shade_args
-    l.oracle_shade_shadowed_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, vp, f64p,
-                                            u32p, u32, u32, vp]
+    l.oracle_shade_ex_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, vp, vp, f64p,
+                                      u32p, u32, u32, vp]
     l.oracle_shade_adjoint_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, f64p, f64p, f64p]
     frag_args = [vp, vp, vp, u32, vp, u32, u32p, vp, u32, u32, u32p, u32p, vp, f64p]
     l.oracle_shade_fragments_f64.argtypes = frag_args
@@ -177,6 +177,14 @@ def shade_shadowed(camera_rec, globals_rec, gb, lights, grid, shadows, rows=None
     ``dynamic`` and ``static`` (layers, size, size) float32, ``matrices`` (layers, 16)
     float32 column-major, ``config`` (a SHADOW_CONFIG record) and ``max_lights``.
     Returns (radiance, pair_counts or None, bounds_flag)."""
+    return shade_ex(camera_rec, globals_rec, gb, lights, grid, shadows=shadows, rows=rows, pair_counts=pair_counts)
+
+
+def shade_ex(camera_rec, globals_rec, gb, lights, grid, shadows=None, rc=None, rows=None, pair_counts=False):
+    """``shade`` (f64) with the pass's optional bindings: ``shadows`` as for
+    ``shade_shadowed`` (or None) and ``rc``, the radiance-cascade probe texture as a
+    (height, width, 4) float16 array (or None). Returns (radiance, pair_counts or None,
+    bounds_flag)."""
     from helio_gb300 import layouts as L
 
     W, H = gb.width, gb.height
@@ -186,21 +194,29 @@ def shade_shadowed(camera_rec, globals_rec, gb, lights, grid, shadows, rows=None
     arrs, ptrs, pitch = _planes(gb)
     kind, lists, counts, params = _grid_args(grid)
     lts = np.ascontiguousarray(lights)
-    dyn = np.ascontiguousarray(shadows["dynamic"], np.float32)
-    sta = np.ascontiguousarray(shadows["static"], np.float32)
-    mats = np.ascontiguousarray(shadows["matrices"], np.float32)
-    cfg = np.ascontiguousarray(shadows["config"])
-    desc = np.zeros(1, L.SHADOW_MAPS)
-    desc["dynamic_atlas"], desc["static_atlas"] = dyn.ctypes.data, sta.ctypes.data
-    desc["matrices"], desc["config"] = mats.ctypes.data, cfg.ctypes.data
-    desc["size"], desc["layers"] = dyn.shape[1], dyn.shape[0]
-    desc["max_shadow_lights"] = shadows["max_lights"]
+    desc = None
+    if shadows is not None:
+        dyn = np.ascontiguousarray(shadows["dynamic"], np.float32)
+        sta = np.ascontiguousarray(shadows["static"], np.float32)
+        mats = np.ascontiguousarray(shadows["matrices"], np.float32)
+        cfg = np.ascontiguousarray(shadows["config"])
+        desc = np.zeros(1, L.SHADOW_MAPS)
+        desc["dynamic_atlas"], desc["static_atlas"] = dyn.ctypes.data, sta.ctypes.data
+        desc["matrices"], desc["config"] = mats.ctypes.data, cfg.ctypes.data
+        desc["size"], desc["layers"] = dyn.shape[1], dyn.shape[0]
+        desc["max_shadow_lights"] = shadows["max_lights"]
+    rcd = None
+    if rc is not None:
+        rct = np.ascontiguousarray(rc, np.float16)
+        rcd = np.zeros(1, L.RC_CASCADE)
+        rcd["texels"], rcd["pitch"] = rct.ctypes.data, rct.strides[0]
+        rcd["height"], rcd["width"] = rct.shape[0], rct.shape[1]
     bounds = np.zeros(1, np.int32)
-    lib().oracle_shade_shadowed_f64(_ptr(np.ascontiguousarray(camera_rec)), _ptr(np.ascontiguousarray(globals_rec)),
-                                    gb.layout, W, H, ptrs, pitch, _ptr(lts) if len(lts) else None, len(lts), kind,
-                                    _ptr(lists), _ptr(counts), _ptr(params) if params is not None else None,
-                                    _ptr(desc), _ptr(out), _ptr(pc) if pc is not None else None, r0, r1,
-                                    _ptr(bounds))
+    lib().oracle_shade_ex_f64(_ptr(np.ascontiguousarray(camera_rec)), _ptr(np.ascontiguousarray(globals_rec)),
+                              gb.layout, W, H, ptrs, pitch, _ptr(lts) if len(lts) else None, len(lts), kind,
+                              _ptr(lists), _ptr(counts), _ptr(params) if params is not None else None,
+                              _ptr(desc) if desc is not None else None, _ptr(rcd) if rcd is not None else None,
+                              _ptr(out), _ptr(pc) if pc is not None else None, r0, r1, _ptr(bounds))
     return out, pc, bool(bounds[0])
 
 

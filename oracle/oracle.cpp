@@ -36,6 +36,7 @@
 #include <omp.h>
 #endif
 
+#include "rc_gi.h"
 #include "shadow_factor.h"
 
 namespace {
@@ -589,7 +590,8 @@ template <class T>
 void shade_impl(const void* camera, const void* globals, const GBufferDesc& g, const void* lights,
                 uint32_t n_lights, const GridDesc& grid, double* out_rgba /* W*H*4 */,
                 uint32_t* pair_counts /* W*H*3 or null */, uint32_t row0, uint32_t row1,
-                const shadow_oracle::ShadowDesc* shadows = nullptr, int* shadow_bounds = nullptr) {
+                const shadow_oracle::ShadowDesc* shadows = nullptr, int* shadow_bounds = nullptr,
+                const rc_oracle::RcDesc* rc = nullptr) {
     Cam<T> c = load_camera<T>(camera);
     RawGlobals gl;
     std::memcpy(&gl, globals, sizeof gl);
@@ -666,6 +668,23 @@ void shade_impl(const void* camera, const void* globals, const GBufferDesc& g, c
             // Hemisphere ambient (deferred_lighting.wgsl:1196-1199) with ao * ssao(=1)
             T hemi_t = N.y * T(0.5) + T(0.5);
             V3<T> hemi = v3<T>(mixt(ground.x, sky.x, hemi_t), mixt(ground.y, sky.y, hemi_t), mixt(ground.z, sky.z, hemi_t)) * s.albedo;
+            if (rc && gl.has_rc_gi != 0u) {
+                // RC indirect diffuse over the hemisphere (deferred_lighting.wgsl:1159-1163, 1197-1209)
+                T irr[3];
+                rc_oracle::irradiance<T>(*rc, gl.rc_world_min, gl.rc_world_max, P.x, P.y, P.z, N.x, N.y, N.z, irr);
+                const T NdV = tmax(dot(N, V), T(0));
+                const T x = clampt(T(1) - NdV, T(0), T(1));
+                const T p5 = x * x * x * x * x;
+                const T f0[3] = {F0.x, F0.y, F0.z}, alb[3] = {s.albedo.x, s.albedo.y, s.albedo.z};
+                const T w = clampt(tsqrt(irr[0] * irr[0] + irr[1] * irr[1] + irr[2] * irr[2]) * T(4), T(0), T(1));
+                T amb[3] = {hemi.x, hemi.y, hemi.z};
+                for (int ch = 0; ch < 3; ++ch) {
+                    const T F = f0[ch] + (tmax(T(1) - s.rough, f0[ch]) - f0[ch]) * p5;
+                    const T diff = (T(1) - F) * (T(1) - s.metal) * irr[ch] * alb[ch];
+                    amb[ch] = mixt(amb[ch], diff, w);
+                }
+                hemi = v3<T>(amb[0], amb[1], amb[2]);
+            }
             T ao = s.ao * T(1);
             V3<T> color = Lo + hemi * ao;
             color = color + s.emissive;
@@ -1072,18 +1091,20 @@ void oracle_shade_f64(const void* cam, const void* globals, uint32_t layout, uin
     shade_impl<double>(cam, globals, g, lights, n, gr, out_rgba, pair_counts, row0, row1);
 }
 
-// oracle_shade_f64 with the shadow term; shadows: an hl_shadow_maps whose pointers are
-// host memory. *bounds is set when a shadow layer index is beyond the atlas.
-void oracle_shade_shadowed_f64(const void* cam, const void* globals, uint32_t layout, uint32_t W, uint32_t H,
-                               const void* const* planes, const uint64_t* pitch, const void* lights, uint32_t n,
-                               uint32_t grid_kind, const uint32_t* lists, const uint32_t* counts, const void* froxel,
-                               const void* shadows, double* out_rgba, uint32_t* pair_counts, uint32_t row0,
-                               uint32_t row1, int* bounds) {
+// oracle_shade_f64 with the pass's optional bindings: shadows (an hl_shadow_maps whose
+// pointers are host memory, or NULL) and radiance-cascade probes (an hl_rc_cascade with
+// host texels, or NULL). *bounds is set when a shadow layer index is beyond the atlas.
+void oracle_shade_ex_f64(const void* cam, const void* globals, uint32_t layout, uint32_t W, uint32_t H,
+                         const void* const* planes, const uint64_t* pitch, const void* lights, uint32_t n,
+                         uint32_t grid_kind, const uint32_t* lists, const uint32_t* counts, const void* froxel,
+                         const void* shadows, const void* rc, double* out_rgba, uint32_t* pair_counts, uint32_t row0,
+                         uint32_t row1, int* bounds) {
     GBufferDesc g = make_gbuf(layout, W, H, planes, pitch);
     GridDesc gr = make_grid(grid_kind, lists, counts, froxel);
     *bounds = 0;
     shade_impl<double>(cam, globals, g, lights, n, gr, out_rgba, pair_counts, row0, row1,
-                       static_cast<const shadow_oracle::ShadowDesc*>(shadows), bounds);
+                       static_cast<const shadow_oracle::ShadowDesc*>(shadows), bounds,
+                       static_cast<const rc_oracle::RcDesc*>(rc));
 }
 
 void oracle_shade_f32(const void* cam, const void* globals, uint32_t layout, uint32_t W, uint32_t H, const void* const* planes,

@@ -1,5 +1,6 @@
-"""GPU parity of hl_shade_shadowed (the shadow term of the deferred pass's light loop)
-against the f64 oracle.
+"""GPU parity of the deferred pass's optional bindings against the f64 oracle:
+hl_shade_shadowed / hl_shade_ex with shadow maps (the shadow term of the light loop) and
+with radiance-cascade probes (indirect diffuse light).
 
 Tolerances as for hl_shade (relative per pixel, floor 1e-6 of the image maximum):
 FP32 / reference G-buffers 1e-5, FP16 G-buffer 2e-3. A pixel may exceed them when one
@@ -153,3 +154,94 @@ def test_shadow_argument_errors(ctx):
                                N.target_struct(out))
         assert e.value.status == status, field
     ctx.sync_status()
+
+
+# ---- radiance-cascade GI (hl_shade_ex) ----
+
+RC_MIN, RC_MAX = (-60.0, -40.0, -110.0), (60.0, 40.0, 0.0)
+
+
+def _rc_device(probes):
+    import torch
+
+    t = torch.from_numpy(probes).cuda()
+    return t, N.rc_cascade_struct(t)
+
+
+def _shade_ex(ctx, df, grid, shadows=None, rc=None, fill=7.0):
+    import torch
+
+    out = torch.full((df.height, df.width, 4), fill, dtype=torch.float32, device="cuda")
+    ctx.shade_ex(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, N.target_struct(out),
+                 shadows=shadows, rc=rc)
+    ctx.sync_status()
+    return out.cpu().numpy().astype(np.float64)
+
+
+# Radiance-cascade GI blends the hemisphere ambient h towards kD_ibl * irradiance * albedo
+# by w = clamp(4 |irradiance|, 0, 1) (deferred_lighting.wgsl:1202-1209): where the blend
+# nearly replaces a much larger h, the f32 error of w (~1e-6 relative, from the
+# irradiance's sums) shows up as h * dw relative to a small result (measured up to
+# 3.3e-4), so FP32 layouts are held to 5e-4 for these cases.
+TOL_RC = {S.LAYOUT_F32: 5e-4, S.LAYOUT_REFERENCE: 5e-4, S.LAYOUT_F16: 2e-3}
+
+
+def _check_tol(img, ref, st, pc, layout, tols=TOL_RC):
+    e = metrics.radiance_error(img, ref, st[..., 2], pc[..., 2])
+    assert e["flips"] <= max(2, 1e-4 * e["n"]), e
+    sky = np.isnan(ref[..., 0])
+    k, o = img[..., :3], ref[..., :3]
+    valid = ~sky & (st[..., 2] == pc[..., 2])
+    mx = np.abs(o[valid]).max()
+    rel = (np.abs(k - o) / np.maximum(np.abs(o), 1e-6 * mx)).max(-1)[valid]
+    tol = tols[layout]
+    assert int((rel > tol).sum()) <= max(3, 5e-4 * rel.size), (int((rel > tol).sum()), float(rel.max()), e)
+    assert float(np.quantile(rel, 0.9999)) <= tol, e
+    return e
+
+
+@pytest.mark.parametrize("with_shadows", [False, True])
+@pytest.mark.parametrize("layout", [S.LAYOUT_F32, S.LAYOUT_REFERENCE, S.LAYOUT_F16])
+def test_rc_gi_matches_oracle(ctx, layout, with_shadows):
+    cam, gb, sc, dyn, sta, glb = _setup(layout, "high")
+    glb = S.rc_globals(glb, RC_MIN, RC_MAX)
+    probes = S.rc_probes(7)
+    df = FR.upload(cam.record, glb, sc.lights, gb)
+    ogrid, dgrid, keep = _froxel_grid(cam, sc.lights, gb.width, gb.height)
+    dsh, maps = _device_shadows(sc, dyn, sta)
+    drc, rcs = _rc_device(probes)
+    img = _shade_ex(ctx, df, dgrid, shadows=maps if with_shadows else None, rc=rcs)
+    shadows = dict(dynamic=dyn, static=sta, matrices=sc.matrices, config=sc.config, max_lights=sc.max_lights)
+    ref, pc, _ = oracle.shade_ex(cam.record, glb, gb, sc.lights, ogrid, shadows=shadows if with_shadows else None,
+                                 rc=probes, pair_counts=True)
+    st = gpu_shade(ctx, df, dgrid, stats=True)
+    _check_tol(img, ref, st, pc, layout)
+    # the GI term is exercised: the radiance differs from the hemisphere-only one
+    plain = oracle.shade_ex(cam.record, glb, gb, sc.lights, ogrid, shadows=shadows if with_shadows else None)[0]
+    sky = np.isnan(ref[..., 0])
+    changed = (np.abs(ref[~sky][:, :3] - plain[~sky][:, :3]) > 1e-6 * np.abs(plain[~sky][:, :3])).any(-1).mean()
+    assert changed > 0.3, changed
+
+
+def test_rc_gi_off_or_unbound(ctx):
+    cam, gb, sc, dyn, sta, glb = _setup(S.LAYOUT_F32, "medium", W=160, H=96, size=64)
+    df = FR.upload(cam.record, glb, sc.lights, gb)
+    _, dgrid, keep = _froxel_grid(cam, sc.lights, gb.width, gb.height)
+    drc, rcs = _rc_device(S.rc_probes(3))
+    # probes bound, has_rc_gi == 0: the hemisphere ambient, as hl_shade
+    np.testing.assert_array_equal(_shade_ex(ctx, df, dgrid, rc=rcs), gpu_shade(ctx, df, dgrid))
+    # has_rc_gi != 0 without probes: reported as not supported
+    dfo = FR.upload(cam.record, S.rc_globals(glb, RC_MIN, RC_MAX), sc.lights, gb)
+    import torch
+
+    out = torch.zeros((gb.height, gb.width, 4), dtype=torch.float32, device="cuda")
+    ctx.shade_ex(dfo.camera, dfo.globals_, dfo.gbuffer, dfo.lights, dfo.n_lights, dgrid, N.target_struct(out))
+    with pytest.raises(N.HelioError) as e:
+        ctx.sync_status()
+    assert e.value.status == N.HL_ERR_NOT_SUPPORTED
+    # a probe texture smaller than 64 x 1024 is rejected
+    small = N.rc_cascade_struct(drc[:512])
+    with pytest.raises(N.HelioError) as e:
+        ctx.shade_ex(dfo.camera, dfo.globals_, dfo.gbuffer, dfo.lights, dfo.n_lights, dgrid, N.target_struct(out),
+                     rc=small)
+    assert e.value.status == N.HL_ERR_SIZE
