@@ -718,6 +718,31 @@ def shadows_form(ctx, dev, stream, flush, w, fp, off, idx, cap, grid, with_oracl
         entry["pixels_darkened_by_shadows"] = round(darker, 4)
         entry["error_vs_fp64_oracle"] = {"max": float(f"{e['max']:.3e}"), "p9999": float(f"{e['p9999']:.3e}"),
                                          "n_over_2e3": e["n_over_2e3"], "flips": e["flips"], "n": e["n"]}
+
+    # the same frame with radiance-cascade GI as well (hl_shade_ex: shadows + RC probes)
+    probes = S.rc_probes(7)
+    d_rc = torch.from_numpy(probes).to(dev)
+    rcs = N.rc_cascade_struct(d_rc)
+    glb_rc = S.rc_globals(w.globals_, (-60.0, -40.0, -110.0), (60.0, 40.0, 0.0))
+    d_glb_rc = FR.bytes_tensor(glb_rc, dev)
+
+    def frame_rc():
+        ctx.bin_froxels(dfs.camera, d_lights, dfs.n_lights, fp, off, idx, cap, sh)
+        ctx.shade_ex(dfs.camera, d_glb_rc, dfs.gbuffer, d_lights, dfs.n_lights, grid, tgt, shadows=maps, rc=rcs,
+                     stream=sh)
+
+    t_rc = _median_ms(frame_rc, stream, flush, 50)
+    ctx.sync_status(sh)
+    rc_entry = {"frame_ms": round(t_rc, 4), "mpix_s": round(W * H / t_rc / 1e3, 1),
+                "volume": "rc_world [-60,-40,-110]..[60,40,0], synthetic 64x1024 RGBA16F probes"}
+    if with_oracle:
+        ref, pc, _ = oracle.shade_ex(w.camera.record, glb_rc, w.gbuffer, sc.lights, ("froxels", idx_h, off_h, p_np),
+                                     shadows=shadows, rc=probes, pair_counts=True)
+        e = metrics.radiance_error(rad.double().cpu().numpy(), ref, st.cpu().numpy().view(np.uint32)[..., 2],
+                                   pc[..., 2])
+        rc_entry["error_vs_fp64_oracle"] = {"max": float(f"{e['max']:.3e}"), "p9999": float(f"{e['p9999']:.3e}"),
+                                            "n_over_2e3": e["n_over_2e3"], "n": e["n"]}
+    entry["with_rc_gi"] = rc_entry
     del dyn, sta
     torch.cuda.empty_cache()
     return entry

@@ -55,8 +55,8 @@ hl_status shade_common(hl_ctx* ctx, const void* camera, const void* globals, con
     if (rc) {
         const uint32_t need_w = HL_RC_PROBE_DIM * HL_RC_DIR_DIM, need_h = HL_RC_PROBE_DIM * HL_RC_PROBE_DIM * HL_RC_DIR_DIM;
         if (!rc->texels) return fail(ctx, HL_ERR_INVALID_ARGUMENT, "rc cascade texels are NULL");
-        if (!aligned(rc->texels, 8) || rc->pitch % 8 != 0)
-            return fail(ctx, HL_ERR_LAYOUT, "rc cascade pointer/pitch not 8-byte aligned (RGBA16F)");
+        if (!aligned(rc->texels, 16) || rc->pitch % 16 != 0)
+            return fail(ctx, HL_ERR_LAYOUT, "rc cascade pointer/pitch not 16-byte aligned");
         if (rc->width < need_w || rc->height < need_h || rc->pitch < uint64_t(rc->width) * 8)
             return fail(ctx, HL_ERR_SIZE, "rc cascade is %ux%u (pitch %llu), needs at least %ux%u", rc->width,
                         rc->height, (unsigned long long)rc->pitch, need_w, need_h);

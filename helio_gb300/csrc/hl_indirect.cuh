@@ -40,26 +40,35 @@ __device__ __forceinline__ float smooth01(float lo, float hi, float x) {
 }
 
 // rc_corner_irradiance_precomp (:842-864): the cosine-weighted mean of one probe's
-// directions.
+// directions (those with weight > 0.001). The 4 directions dx of one row dy are 32
+// contiguous bytes, so a probe is read as 8 unconditional 16-byte loads and the skipped
+// directions are masked after loading.
 __device__ __forceinline__ void corner(const ExtView& ev, uint32_t px, uint32_t py, uint32_t pz, const float* cw,
                                        float& r, float& g, float& b) {
     const uint32_t cpx = min(px, kProbeDim - 1u), cpy = min(py, kProbeDim - 1u), cpz = min(pz, kProbeDim - 1u);
+    const unsigned char* base = ev.rc + 8ull * (cpx * kDirDim) + ev.rc_pitch * ((cpy * kProbeDim + cpz) * kDirDim);
+    uint4 t[kDirDim][2];
+#pragma unroll
+    for (uint32_t ddy = 0; ddy < kDirDim; ++ddy) {
+        const uint4* row = reinterpret_cast<const uint4*>(base + ev.rc_pitch * ddy);
+        t[ddy][0] = __ldg(row);
+        t[ddy][1] = __ldg(row + 1);
+    }
     float ir = 0.0f, ig = 0.0f, ib = 0.0f, ws = 0.0f;
 #pragma unroll
     for (uint32_t ddx = 0; ddx < kDirDim; ++ddx) {
 #pragma unroll
         for (uint32_t ddy = 0; ddy < kDirDim; ++ddy) {
             const float w = cw[ddx * kDirDim + ddy];
-            if (w > 0.001f) {
-                const uint32_t ax = cpx * kDirDim + ddx, ay = (cpy * kProbeDim + cpz) * kDirDim + ddy;
-                const uint2 t = __ldg(reinterpret_cast<const uint2*>(ev.rc + ev.rc_pitch * ay) + ax);
-                const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&t.x));
-                const float2 ba = __half22float2(*reinterpret_cast<const __half2*>(&t.y));
-                ir += rg.x * w;
-                ig += rg.y * w;
-                ib += ba.x * w;
-                ws += w;
-            }
+            const uint4 q = t[ddy][ddx >> 1];
+            const uint32_t lo = (ddx & 1u) ? q.z : q.x, hi = (ddx & 1u) ? q.w : q.y;
+            const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&lo));
+            const float2 bb = __half22float2(*reinterpret_cast<const __half2*>(&hi));
+            const bool use = w > 0.001f;
+            ir += use ? rg.x * w : 0.0f;
+            ig += use ? rg.y * w : 0.0f;
+            ib += use ? bb.x * w : 0.0f;
+            ws += use ? w : 0.0f;
         }
     }
     const float d = fmaxf(ws, 0.001f);

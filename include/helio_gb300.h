@@ -291,7 +291,7 @@ hl_status hl_shade_shadowed(hl_ctx* ctx, const void* camera, const void* globals
 #define HL_RC_PROBE_DIM 16u
 #define HL_RC_DIR_DIM 4u
 typedef struct hl_rc_cascade {
-    const void* texels;     /* device, RGBA16F, rows of `pitch` bytes                  */
+    const void* texels;     /* device, RGBA16F, rows of `pitch` bytes; both 16-byte aligned */
     uint64_t pitch;
     uint32_t width, height; /* at least 64 x 1024 (probe_dim*dir_dim x probe_dim^2*dir_dim) */
 } hl_rc_cascade;
