@@ -5,6 +5,8 @@
     python -m helio_gb300.profile_run --batched --frames 3              # 98-view plan
     python -m helio_gb300.profile_run --workload 1 --frames 3 --fragments  # + fragment loop
     python -m helio_gb300.profile_run --gbuffer-write --frames 3        # G-buffer pass only
+    python -m helio_gb300.profile_run --workload 1 --shadows --atlas 256 --frames 3  # + shadow term
+    python -m helio_gb300.profile_run --workload 1 --rc --frames 3      # + radiance-cascade GI
 
 Every frame launches the same kernels as one bench step (froxel binning: 4 launches,
 shading: 1, adjoint: 2), so ``ncu -k <kernel> -s <n> -c 1`` can pick one warm launch.
@@ -25,6 +27,10 @@ def main(argv=None):
                     help="also light one raster-ordered fragment per pixel (transparent mode)")
     ap.add_argument("--gbuffer-write", action="store_true",
                     help="only the G-buffer pass: hl_write_gbuffer over the bench's 1080p material scene")
+    ap.add_argument("--shadows", action="store_true",
+                    help="shade with the shadow term: lights 0-41 cast shadows (hl_shade_ex)")
+    ap.add_argument("--atlas", type=int, default=1024, help="shadow atlas size in texels")
+    ap.add_argument("--rc", action="store_true", help="shade with radiance-cascade GI (hl_shade_ex)")
     ap.add_argument("--scale", type=float, default=1.0)
     args = ap.parse_args(argv)
 
@@ -87,10 +93,28 @@ def main(argv=None):
         prm = S.fragment_params(L.FRAGMENTS_TRANSPARENT, L.tile_grid(W, H)[0])
         fpar = N.FragmentParams(int(prm["mode"][0]), int(prm["num_tiles_x"][0]), float(prm["ambient_intensity"][0]),
                                 (N.C.c_float * 3)(*[float(v) for v in prm["ambient_color"][0]]))
+    maps = rcs = None
+    glb = df.globals_
+    if args.shadows:
+        sc = S.shadow_scene(w.camera, w.lights, L.MAX_SHADOW_LIGHTS)
+        dyn, sta = S.shadow_atlases(sc.kinds, args.atlas, seed=1, xp=torch, device="cuda")
+        mats = torch.from_numpy(sc.matrices).cuda()
+        cfg = FR.bytes_tensor(sc.config)
+        maps = N.shadow_maps_struct(dyn, sta, mats, cfg, sc.max_lights)
+        df = FR.upload(w.camera.record, w.globals_, sc.lights, w.gbuffer)
+        glb = df.globals_
+    if args.rc:
+        d_rc = torch.from_numpy(S.rc_probes(7)).cuda()
+        rcs = N.rc_cascade_struct(d_rc)
+        glb = FR.bytes_tensor(S.rc_globals(w.globals_, (-60.0, -40.0, -110.0), (60.0, 40.0, 0.0)))
     for _ in range(args.frames):
         ev0.record()
         ctx.bin_froxels(df.camera, df.lights, df.n_lights, fp, off, idx, cap)
-        ctx.shade(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, N.target_struct(out))
+        if args.shadows or args.rc:
+            ctx.shade_ex(df.camera, glb, df.gbuffer, df.lights, df.n_lights, grid, N.target_struct(out),
+                         shadows=maps, rc=rcs)
+        else:
+            ctx.shade(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, N.target_struct(out))
         if args.adjoint:
             ctx.shade_adjoint(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, d_rad, W * 16, d_l,
                               d_p)
