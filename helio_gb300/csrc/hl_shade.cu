@@ -166,7 +166,7 @@ __device__ __noinline__ int precise_pair(const GpuCamera* cam, uint32_t x, uint3
                                          float ry, float rz, float& cr, float& cg, float& cb) {
     Pixel p = pin;
     const float camx = cam->position_near[0], camy = cam->position_near[1], camz = cam->position_near[2];
-    reconstruct<true>(cam->inv_view_proj, x, y, W, H, depth, p.Px, p.Py, p.Pz, p.Plx, p.Ply, p.Plz);
+    reconstruct<true, false>(cam->inv_view_proj, x, y, W, H, depth, p.Px, p.Py, p.Pz, p.Plx, p.Ply, p.Plz);
     const DF ax = two_sum(p.Px, -camx), ay = two_sum(p.Py, -camy), az = two_sum(p.Pz, -camz);
     const DF bx = two_sum(ax.hi, ax.lo + p.Plx), by = two_sum(ay.hi, ay.lo + p.Ply), bz = two_sum(az.hi, az.lo + p.Plz);
     p.Px = bx.hi; p.Plx = bx.lo - rx;
@@ -229,8 +229,8 @@ __device__ __noinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>
             float wx = p.Px + p.Plx, wy = p.Py + p.Ply, wz = p.Pz + p.Plz;
             if (!PRECISE) {
                 float hx, hy, hz, lx, ly, lz;
-                reconstruct<true>(cam->inv_view_proj, x0 + q % TW, y0 + q / TW, W, H, fabsf(dq), hx, hy, hz, lx, ly,
-                                  lz);
+                reconstruct<true, false>(cam->inv_view_proj, x0 + q % TW, y0 + q / TW, W, H, fabsf(dq), hx, hy, hz,
+                                         lx, ly, lz);
                 wx = hx + lx;
                 wy = hy + ly;
                 wz = hz + lz;
@@ -371,8 +371,8 @@ __device__ __forceinline__ void shade_tile(
                                         tx.f0g, tx.f0b, 0.0f, 0.0f, 0.0f);
                     if (p.NdV < kFastMinNdV) {
                         // grazing view: precise set-up, camera-relative double-float position
-                        reconstruct<true>(cam->inv_view_proj, x, y, W, H, tx.depth, p.Px, p.Py, p.Pz, p.Plx, p.Ply,
-                                          p.Plz);
+                        reconstruct<true, false>(cam->inv_view_proj, x, y, W, H, tx.depth, p.Px, p.Py, p.Pz, p.Plx,
+                                                 p.Ply, p.Plz);
                         const DF ax = two_sum(p.Px, -camx), ay = two_sum(p.Py, -camy), az = two_sum(p.Pz, -camz);
                         const DF bx = two_sum(ax.hi, ax.lo + p.Plx), by = two_sum(ay.hi, ay.lo + p.Ply),
                                  bz = two_sum(az.hi, az.lo + p.Plz);

@@ -205,7 +205,9 @@ HL_HD void reconstruct_relative(const float* rel, const float* w, float ndc_x, f
 
 // World position of a pixel centre: inv_view_proj (column major, 16 floats) times
 // (ndc_x, ndc_y, depth, 1), ndc of pixel centre (x+0.5, y+0.5) of a W x H target.
-template <bool PRECISE>
+// RENORM (precise): renormalise the rows before the division, which keeps P to ~2^-44
+// relative (without it ~4e-10 at far depth, ample for the FP16 G-buffer's paths).
+template <bool PRECISE, bool RENORM = true>
 HL_HD void reconstruct(const float* m, uint32_t x, uint32_t y, float W, float H, float depth, float& Px, float& Py,
                        float& Pz, float& Plx, float& Ply, float& Plz) {
     if (!PRECISE) {
@@ -250,9 +252,14 @@ HL_HD void reconstruct(const float* m, uint32_t x, uint32_t y, float W, float H,
         s = fma_(m[4 + r], ndy.lo, s);
         // renormalise: after cancellation (the w row at far depth) s can be ~1e-5 of p,
         // and the quotient's correction below assumes |lo| <= ulp(hi)
-        const DF n = two_sum(p, s);
-        hh[r] = n.hi;
-        hl[r] = n.lo;
+        if (RENORM) {
+            const DF n = two_sum(p, s);
+            hh[r] = n.hi;
+            hl[r] = n.lo;
+        } else {
+            hh[r] = p;
+            hl[r] = s;
+        }
     }
     const float w = hh[3], wl = hl[3];
     float* outs[3] = {&Px, &Py, &Pz};
