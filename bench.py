@@ -810,6 +810,20 @@ def gbuffer_write_form(ctx, dev, stream, flush, w, df, fp, off, idx, cap, grid, 
     entry["reference_layout_frame"] = {
         "steps": "hl_write_gbuffer + hl_bin_froxels + hl_shade (HL_GBUF_REFERENCE, 28 B/px), w1 lights",
         "ms": round(t_f, 4), "mpix_s": round(W * H / t_f / 1e3, 1)}
+    # The reflection draw over the lit frame: SSR and planar hits and lightmap UVs
+    # (synthetic, 1920x1080). Algorithmic bytes per pixel: the G-buffer planes the draw
+    # reads (normal 8, orm 4, emissive 8, depth 4), the three images (8 + 8 + 4) and the
+    # RGBA32F target's read-modify-write (16 + 16).
+    ssr, planar, lm = (torch.from_numpy(a).to(dev) for a in S.reflection_images(W, H, 77))
+    t_r = _median_ms(lambda: ctx.shade_reflections(df.camera, df.globals_, gbs, tgt, ssr=ssr, planar=planar,
+                                                   lightmap_uv=lm, stream=sh), stream, flush, 50)
+    ctx.sync_status(sh)
+    alg_r = W * H * 76
+    entry["reflections"] = {
+        "steps": "hl_shade_reflections (fs_reflection: SSR + planar, lightmap UVs, no RC) over the written "
+                 "HL_GBUF_REFERENCE G-buffer, RGBA32F target", "ms": round(t_r, 4),
+        "mpix_s": round(W * H / t_r / 1e3, 1), "algorithmic_bytes": alg_r,
+        "hbm_frac": round(alg_r / (t_r / 1e3) / 1e9 / hbm_peak, 4)}
     return entry
 
 

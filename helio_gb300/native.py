@@ -113,6 +113,14 @@ class ShadeBindings(C.Structure):
     _fields_ = [("shadows", C.POINTER(ShadowMaps)), ("rc", C.POINTER(RcCascade))]
 
 
+class ReflectionInputs(C.Structure):
+    """hl_reflection_inputs: SSR and planar hit images (RGBA16F), lightmap UVs (RG16F) and
+    radiance-cascade probes, each optional (NULL)."""
+    _fields_ = [("ssr", C.c_void_p), ("ssr_pitch", C.c_uint64), ("planar", C.c_void_p),
+                ("planar_pitch", C.c_uint64), ("lightmap_uv", C.c_void_p), ("lightmap_uv_pitch", C.c_uint64),
+                ("rc", C.POINTER(RcCascade))]
+
+
 class GBufferTargets(C.Structure):
     """hl_gbuffer_targets: albedo, normal, orm, emissive (required), lightmap_uv, sss,
     extra, velocity (optional)."""
@@ -125,7 +133,7 @@ EXPORTS = [
     "hl_tile_count", "hl_bin_tiles_ref", "hl_froxel_slice_table", "hl_bin_froxels", "hl_shade", "hl_shade_stats",
     "hl_shade_adjoint", "hl_batch_plan_create", "hl_batch_execute", "hl_batch_plan_view_grid",
     "hl_batch_plan_destroy", "hl_probe_fp32_peak", "hl_bin_froxels_noalloc", "hl_shade_fragments",
-    "hl_write_gbuffer", "hl_shade_shadowed", "hl_shade_ex",
+    "hl_write_gbuffer", "hl_shade_shadowed", "hl_shade_ex", "hl_shade_reflections",
 ]
 
 _lock = threading.Lock()
@@ -200,6 +208,8 @@ def _bind(l):
     l.hl_shade_shadowed.restype = i32
     l.hl_shade_ex.argtypes = [vp, vp, vp, P(GBuffer), vp, u32, P(LightGrid), P(ShadeBindings), P(Target), vp]
     l.hl_shade_ex.restype = i32
+    l.hl_shade_reflections.argtypes = [vp, vp, vp, P(GBuffer), P(ReflectionInputs), P(Target), vp]
+    l.hl_shade_reflections.restype = i32
 
 
 def status_string(status: int) -> str:
@@ -330,6 +340,20 @@ class Context:
         self._check(self._l.hl_shade_ex(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer), _ptr(lights),
                                         n_lights, C.byref(grid), C.byref(b), C.byref(target), _stream(stream)),
                     "hl_shade_ex")
+
+    def shade_reflections(self, camera, globals_, gbuffer: GBuffer, target: Target, ssr=None, planar=None,
+                          lightmap_uv=None, rc: "RcCascade" = None, stream=None):
+        """The reflection draw (fs_reflection) added over ``target``; ``ssr`` / ``planar``:
+        device float16 tensors (H, W, 4), ``lightmap_uv``: (H, W, 2), each optional."""
+        inp = ReflectionInputs()
+        for name, t in (("ssr", ssr), ("planar", planar), ("lightmap_uv", lightmap_uv)):
+            if t is not None:
+                setattr(inp, name, _ptr(t))
+                setattr(inp, name + "_pitch", int(t.stride(0) * t.element_size()))
+        inp.rc = C.pointer(rc) if rc is not None else None
+        self._check(self._l.hl_shade_reflections(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer),
+                                                 C.byref(inp), C.byref(target), _stream(stream)),
+                    "hl_shade_reflections")
 
     def shade_stats(self, camera, globals_, gbuffer: GBuffer, lights, n_lights, grid: LightGrid, counts, stream=None):
         self._check(self._l.hl_shade_stats(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer), _ptr(lights),

@@ -733,3 +733,29 @@ def rc_globals(globals_rec: np.ndarray, world_min, world_max) -> np.ndarray:
     g["rc_world_min"] = (*world_min, 0.0)
     g["rc_world_max"] = (*world_max, 0.0)
     return g
+
+
+def reflection_images(width: int, height: int, seed: int):
+    """Synthetic inputs of the reflection draw: (ssr, planar, lightmap_uv) as float16
+    arrays (H, W, 4), (H, W, 4), (H, W, 2). SSR hits carry colour in [0, 4) and a
+    confidence that is 0 on about a third of the pixels, partial elsewhere and 1 on a
+    tenth; planar hits cover a horizontal band (confidence 0 outside it); lightmap UVs
+    mix the no-lightmap sentinel (-1, -1), the virtual-geometry sentinel (-2, -2) and
+    atlas UVs in [0, 1)."""
+    rng = np.random.default_rng(seed)
+    H, W = height, width
+    ssr = np.empty((H, W, 4), np.float32)
+    ssr[..., :3] = rng.uniform(0.0, 4.0, (H, W, 3))
+    a = rng.uniform(0.0, 1.0, (H, W))
+    a[rng.uniform(size=(H, W)) < 0.33] = 0.0
+    a[rng.uniform(size=(H, W)) < 0.1] = 1.0
+    ssr[..., 3] = a
+    planar = np.zeros((H, W, 4), np.float32)
+    band = slice(H // 2, H // 2 + max(1, H // 4))
+    planar[band, :, :3] = rng.uniform(0.0, 2.0, (planar[band].shape[0], W, 3))
+    planar[band, :, 3] = rng.uniform(0.2, 1.0, (planar[band].shape[0], W))
+    lm = rng.uniform(0.0, 1.0, (H, W, 2)).astype(np.float32)
+    k = rng.integers(0, 3, (H, W))
+    lm[k == 0] = -1.0
+    lm[k == 1] = -2.0
+    return ssr.astype(np.float16), planar.astype(np.float16), lm.astype(np.float16)

@@ -315,6 +315,47 @@ hl_status hl_shade_ex(hl_ctx* ctx, const void* camera, const void* globals, cons
                       const void* lights, uint32_t n_lights, const hl_light_grid* grid,
                       const hl_shade_bindings* bindings, const hl_target* radiance, void* stream);
 
+/* The per-pixel inputs of the pass's reflection draw (deferred_lighting.wgsl:176-180,
+ * 1265-1341), each a W x H image read at the pixel's own coordinates and each optional:
+ *   ssr         screen-space reflection hits, RGBA16F (rgb colour, a confidence), as the
+ *               SSR pass writes them at full resolution (helio-pass-ssr/src/lib.rs:16);
+ *               NULL = the pass's black fallback, no contribution
+ *   planar      planar reflections, RGBA16F, same encoding; NULL = black fallback
+ *   lightmap_uv the G-buffer's lightmap UVs, RG16F (x < -1.5 marks virtual geometry,
+ *               x >= 0 a lightmapped surface); NULL = every pixel carries the G-buffer's
+ *               no-lightmap sentinel (-1, -1) (gbuffer.wgsl:245)
+ *   rc          the radiance-cascade probes for the rough-specular fallback.
+ * Pitches in bytes; ssr, planar and the rc texels 8-byte aligned, lightmap_uv 4. */
+typedef struct hl_reflection_inputs {
+    const void* ssr;
+    uint64_t ssr_pitch;
+    const void* planar;
+    uint64_t planar_pitch;
+    const void* lightmap_uv;
+    uint64_t lightmap_uv_pitch;
+    const hl_rc_cascade* rc;
+} hl_reflection_inputs;
+
+/* The indirect specular of fs_reflection (deferred_lighting.wgsl:1265-1341), added to
+ * `radiance` as the pass's additive second draw does (colour One + One, alpha kept;
+ * deferred-light/src/lib.rs:448-489): for every pixel with depth < 1,
+ *   spec = 0 (the environment term under the pass's fallback environment: no capture
+ *          cubemaps are bound, so env_cube is the black fallback cube, lib.rs:542)
+ *   spec = mix(spec, ssr.rgb F_ibl, ssr.a)       when enable_reflections and ssr.a > 0
+ *   spec = mix(spec, planar.rgb F_ibl, planar.a) when enable_reflections and planar.a > 0
+ *   spec = mix(spec, rc_specular, smoothstep(0.6, 0.9, r) 0.4)  when has_rc_gi, r > 0.6
+ *   radiance.rgb += lightmapped ? spec : spec * ao
+ * with F_ibl = fresnel_schlick_roughness(NdV, F0, roughness), R = reflect(-V, N) and
+ * rc_specular the probe irradiance along normalize(mix(R, N, 0.5 roughness))
+ * (sample_rc_specular, :928-980) and ao = the G-buffer's ao (the SSAO fallback is white).
+ * Debug modes 30 / 31 replace the pixel with (ssr.a, ssr.a, ssr.a, 1) / (ssr.rgb, 1), the
+ * pass's replacement pipeline (lib.rs:1188-1193); modes 1, 2, 4, 5, 10, 11, 20, 21 add
+ * nothing. has_rc_gi != 0 with roughness > 0.6 and no probes bound is reported through
+ * hl_sync_status as HL_ERR_NOT_SUPPORTED. Replaces the fs_reflection draw of
+ * DeferredLightPass::execute (lib.rs:1188-1197). */
+hl_status hl_shade_reflections(hl_ctx* ctx, const void* camera, const void* globals, const hl_gbuffer* gbuffer,
+                               const hl_reflection_inputs* inputs, const hl_target* radiance, void* stream);
+
 /* Per-pixel pair statistics of the same shading pass, for FLOP accounting: for every
  * pixel (x,y), counts[(y*W+x)*3 + {0,1,2}] = lights listed for the pixel, lights in
  * range (the reference's light-loop test, deferred_lighting.wgsl:1128-1131), and full

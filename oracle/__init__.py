@@ -65,6 +65,8 @@ def _bind(l):
     l.oracle_shade_f32.argtypes = shade_args
     l.oracle_shade_ex_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, vp, vp, f64p,
                                       u32p, u32, u32, vp]
+    l.oracle_reflections_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, C.c_uint64, vp, C.c_uint64, vp,
+                                         C.c_uint64, vp, f64p, vp]
     l.oracle_shade_adjoint_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, f64p, f64p, f64p]
     frag_args = [vp, vp, vp, u32, vp, u32, u32p, vp, u32, u32, u32p, u32p, vp, f64p]
     l.oracle_shade_fragments_f64.argtypes = frag_args
@@ -218,6 +220,45 @@ def shade_ex(camera_rec, globals_rec, gb, lights, grid, shadows=None, rc=None, r
                               _ptr(desc) if desc is not None else None, _ptr(rcd) if rcd is not None else None,
                               _ptr(out), _ptr(pc) if pc is not None else None, r0, r1, _ptr(bounds))
     return out, pc, bool(bounds[0])
+
+
+def _rc_desc(rc):
+    """(descriptor record, texel array) of an RC probe texture, or (None, None)."""
+    from helio_gb300 import layouts as L
+
+    if rc is None:
+        return None, None
+    rct = np.ascontiguousarray(rc, np.float16)
+    rcd = np.zeros(1, L.RC_CASCADE)
+    rcd["texels"], rcd["pitch"] = rct.ctypes.data, rct.strides[0]
+    rcd["height"], rcd["width"] = rct.shape[0], rct.shape[1]
+    return rcd, rct
+
+
+def reflections(camera_rec, globals_rec, gb, base, ssr=None, planar=None, lightmap_uv=None, rc=None):
+    """fs_reflection (f64) blended over ``base`` (H, W, 4), the lit target: returns
+    (result (H, W, 4) float64, unsupported flag). ``ssr`` / ``planar``: (H, W, 4) float16
+    hit images, ``lightmap_uv``: (H, W, 2) float16, ``rc``: the probe texture; each None
+    for the pass's fallback."""
+    W, H = gb.width, gb.height
+    out = np.array(base, np.float64, copy=True, order="C")
+    assert out.shape == (H, W, 4)
+    arrs, ptrs, pitch = _planes(gb)
+    imgs = []
+    for a, ch in ((ssr, 4), (planar, 4), (lightmap_uv, 2)):
+        if a is None:
+            imgs += [None, 0]
+            continue
+        a = np.ascontiguousarray(a, np.float16)
+        assert a.shape == (H, W, ch)
+        arrs.append(a)
+        imgs += [_ptr(a), a.strides[0]]
+    rcd, rct = _rc_desc(rc)
+    flag = np.zeros(1, np.int32)
+    lib().oracle_reflections_f64(_ptr(np.ascontiguousarray(camera_rec)), _ptr(np.ascontiguousarray(globals_rec)),
+                                 gb.layout, W, H, ptrs, pitch, *imgs, _ptr(rcd) if rcd is not None else None,
+                                 _ptr(out), _ptr(flag))
+    return out, bool(flag[0])
 
 
 def shade_fragments(camera_rec, params, fragments, lights, grid, entity_indices=None, transforms=None,

@@ -706,6 +706,105 @@ void shade_impl(const void* camera, const void* globals, const GBufferDesc& g, c
     }
 }
 
+// ---- the reflection draw (fs_reflection, deferred_lighting.wgsl:1265-1341) ----
+
+struct ReflectImages {  // hl_reflection_inputs with host pointers; rc: null = unbound
+    const unsigned char* ssr;
+    uint64_t ssr_pitch;
+    const unsigned char* planar;
+    uint64_t planar_pitch;
+    const unsigned char* lmuv;
+    uint64_t lmuv_pitch;
+    const rc_oracle::RcDesc* rc;
+};
+
+inline void half4(const unsigned char* p, double* o) {
+    for (int i = 0; i < 4; ++i) {
+        uint16_t v;
+        std::memcpy(&v, p + 2 * i, 2);
+        o[i] = half_to_double(v);
+    }
+}
+
+// out_rgba holds the lit target (fs_main's output) and receives the blended result:
+// rgb += contribution (One + One), alpha kept (deferred-light/src/lib.rs:464-475); debug
+// modes 30/31 replace the pixel (the replacement pipeline, lib.rs:1188-1193).
+// *unsupported is set when a pixel needs the RC fallback and no probes are bound.
+template <class T>
+void reflect_impl(const void* camera, const void* globals, const GBufferDesc& g, const ReflectImages& im,
+                  double* out_rgba, int* unsupported) {
+    Cam<T> c = load_camera<T>(camera);
+    RawGlobals gl;
+    std::memcpy(&gl, globals, sizeof gl);
+    const uint32_t W = g.W, H = g.H;
+    for (uint32_t y = 0; y < H; ++y) {
+        for (uint32_t x = 0; x < W; ++x) {
+            Surface<T> s = load_surface<T>(g, x, y);
+            if (!(s.depth < T(1))) continue;  // discard (:1268)
+            double* o = out_rgba + (size_t(y) * W + x) * 4;
+            double ssr[4] = {0, 0, 0, 0};  // black fallback
+            if (im.ssr) half4(im.ssr + im.ssr_pitch * y + 8ull * x, ssr);
+            const uint32_t dm = gl.debug_mode;
+            if (dm == 30 || dm == 31) {  // :1271-1276
+                for (int k = 0; k < 3; ++k) o[k] = dm == 30 ? ssr[3] : ssr[k];
+                o[3] = 1.0;
+                continue;
+            }
+            if (dm == 1 || dm == 2 || dm == 4 || dm == 5 || dm == 10 || dm == 11 || dm == 20 || dm == 21) continue;
+            const V3<T> N = normalize(s.n_raw);
+            const T rough = s.rough;
+            const T F0[3] = {clampt(s.f0.x, T(0), T(0.999)), clampt(s.f0.y, T(0), T(0.999)),
+                             clampt(s.f0.z, T(0), T(0.999))};
+            // lightmap sentinel (:1300-1303); without the image every pixel holds (-1, -1)
+            T lm_x = T(-1);
+            if (im.lmuv) {
+                uint16_t v;
+                std::memcpy(&v, im.lmuv + im.lmuv_pitch * y + 4ull * x, 2);
+                lm_x = T(half_to_double(v));
+            }
+            const bool has_lightmap = !(lm_x < T(-1.5)) && lm_x >= T(0);
+            // world position, V, F_ibl, R (:1305-1311)
+            const T u = (T(x) + T(0.5)) / T(W), v = (T(y) + T(0.5)) / T(H);
+            T h[4];
+            mat4_mul(c.inv_view_proj, u * T(2) - T(1), T(1) - v * T(2), s.depth, T(1), h);
+            const V3<T> P = v3<T>(h[0] / h[3], h[1] / h[3], h[2] / h[3]);
+            const V3<T> V = normalize(c.pos - P);
+            const T NdV = tmax(dot(N, V), T(0));
+            const T q = clampt(T(1) - NdV, T(0), T(1));
+            const T p5 = q * q * q * q * q;
+            T F[3];
+            for (int k = 0; k < 3; ++k) F[k] = F0[k] + (tmax(T(1) - rough, F0[k]) - F0[k]) * p5;
+            const T nv = dot(N, V);
+            const V3<T> R = v3<T>(T(2) * nv * N.x - V.x, T(2) * nv * N.y - V.y, T(2) * nv * N.z - V.z);
+            T spec[3] = {0, 0, 0};  // environment term: the black fallback cube (lib.rs:542)
+            if (gl.enable_reflections != 0u && T(ssr[3]) > T(0))
+                for (int k = 0; k < 3; ++k) spec[k] = mixt(spec[k], T(ssr[k]) * F[k], T(ssr[3]));
+            if (gl.enable_reflections != 0u && im.planar) {
+                double pl[4];
+                half4(im.planar + im.planar_pitch * y + 8ull * x, pl);
+                if (T(pl[3]) > T(0))
+                    for (int k = 0; k < 3; ++k) spec[k] = mixt(spec[k], T(pl[k]) * F[k], T(pl[3]));
+            }
+            if (gl.has_rc_gi > 0u && rough > T(0.6)) {
+                if (!im.rc) {
+                    *unsupported = 1;
+                    continue;
+                }
+                // sample_rc_specular (:928-980): the RC irradiance along mix(R, N, 0.5 r)
+                const T hr = rough * T(0.5);
+                const V3<T> look = normalize(v3<T>(mixt(R.x, N.x, hr), mixt(R.y, N.y, hr), mixt(R.z, N.z, hr)));
+                T irr[3];
+                rc_oracle::irradiance<T>(*im.rc, gl.rc_world_min, gl.rc_world_max, P.x, P.y, P.z, look.x, look.y,
+                                         look.z, irr);
+                const T w = smoothstept(T(0.6), T(0.9), rough) * T(0.4);
+                for (int k = 0; k < 3; ++k) spec[k] = mixt(spec[k], irr[k], w);
+            }
+            const T ao = has_lightmap ? T(1) : s.ao * T(1);  // screen AO: the white fallback
+            for (int k = 0; k < 3; ++k) o[k] += double(spec[k] * ao);
+        }
+    }
+}
+
 // ---- fragment lighting (forward_lit.wgsl:443-494, transparent_base.wgsl:181-220) ----
 
 struct RawFragment {
@@ -1105,6 +1204,19 @@ void oracle_shade_ex_f64(const void* cam, const void* globals, uint32_t layout, 
     shade_impl<double>(cam, globals, g, lights, n, gr, out_rgba, pair_counts, row0, row1,
                        static_cast<const shadow_oracle::ShadowDesc*>(shadows), bounds,
                        static_cast<const rc_oracle::RcDesc*>(rc));
+}
+
+// The reflection draw over a lit target (out_rgba: W*H*4 doubles, updated in place).
+void oracle_reflections_f64(const void* cam, const void* globals, uint32_t layout, uint32_t W, uint32_t H,
+                            const void* const* planes, const uint64_t* pitch, const void* ssr, uint64_t ssr_pitch,
+                            const void* planar, uint64_t planar_pitch, const void* lmuv, uint64_t lmuv_pitch,
+                            const void* rc, double* out_rgba, int* unsupported) {
+    GBufferDesc g = make_gbuf(layout, W, H, planes, pitch);
+    ReflectImages im{static_cast<const unsigned char*>(ssr), ssr_pitch, static_cast<const unsigned char*>(planar),
+                     planar_pitch, static_cast<const unsigned char*>(lmuv), lmuv_pitch,
+                     static_cast<const rc_oracle::RcDesc*>(rc)};
+    *unsupported = 0;
+    reflect_impl<double>(cam, globals, g, im, out_rgba, unsupported);
 }
 
 void oracle_shade_f32(const void* cam, const void* globals, uint32_t layout, uint32_t W, uint32_t H, const void* const* planes,

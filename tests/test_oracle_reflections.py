@@ -1,0 +1,146 @@
+"""The oracle's reflection draw (fs_reflection, deferred_lighting.wgsl:1265-1341) against
+known answers: an independent numpy restatement of the SSR and planar blends, the debug
+modes, the switches and the radiance-cascade rough-specular fallback."""
+import numpy as np
+import pytest
+
+import oracle
+from helio_gb300 import layouts as L
+from helio_gb300 import synthetic as S
+
+RC_MIN, RC_MAX = (-60.0, -40.0, -110.0), (60.0, 40.0, 0.0)
+
+
+def _frame(layout=S.LAYOUT_REFERENCE, W=48, H=32, seed=5, **glb_kw):
+    cam = S.default_camera(W, H)
+    gb = S.make_gbuffer(cam, layout, seed=seed)
+    tx, _ = L.tile_grid(W, H)
+    glb = L.make_globals(tx, 0)
+    for k, v in glb_kw.items():
+        glb[k] = v
+    base = np.random.default_rng(seed).uniform(0.0, 3.0, (H, W, 4))
+    return cam, gb, glb, base
+
+
+def _numpy_reflections(cam, gb, glb, base, ssr, planar, lm):
+    """fs_reflection without RC, restated over whole images in float64."""
+    t = gb.truth
+    H, W = base.shape[:2]
+    depth = t["depth"].astype(np.float64)
+    if gb.layout == S.LAYOUT_REFERENCE:
+        nr = gb.planes[1].astype(np.float64)
+        orm = gb.planes[2].astype(np.float64) / 255.0
+        em = gb.planes[3].astype(np.float64)
+        n_raw, ao, rough = nr[..., :3], orm[..., 0], orm[..., 1]
+        f0 = np.stack([nr[..., 3], orm[..., 3], em[..., 3]], -1)
+        depth = gb.planes[4].astype(np.float64)
+    else:
+        raise NotImplementedError
+    N = n_raw / np.linalg.norm(n_raw, axis=-1, keepdims=True)
+    f0 = np.clip(f0, 0.0, 0.999)
+    xs, ys = np.meshgrid(np.arange(W) + 0.5, np.arange(H) + 0.5)
+    ndc = np.stack([xs / W * 2 - 1, 1 - ys / H * 2, depth, np.ones_like(depth)], -1)
+    inv = np.asarray(cam.record["inv_view_proj"], np.float64).reshape(4, 4)  # column major: rows of M^T
+    h = ndc @ inv
+    P = h[..., :3] / h[..., 3:4]
+    eye = np.asarray(cam.record["position_near"], np.float64).reshape(-1)[:3]
+    V = eye - P
+    V /= np.linalg.norm(V, axis=-1, keepdims=True)
+    ndv = np.maximum((N * V).sum(-1), 0.0)
+    p5 = np.clip(1 - ndv, 0, 1) ** 5
+    F = f0 + (np.maximum((1 - rough)[..., None], f0) - f0) * p5[..., None]
+    spec = np.zeros((H, W, 3))
+    s = ssr.astype(np.float64)
+    pl = planar.astype(np.float64)
+    if glb["enable_reflections"][0]:
+        a = s[..., 3:4]
+        spec = np.where(a > 0, spec * (1 - a) + s[..., :3] * F * a, spec)
+        a = pl[..., 3:4]
+        spec = np.where(a > 0, spec * (1 - a) + pl[..., :3] * F * a, spec)
+    u = lm[..., 0].astype(np.float64) if lm is not None else np.full((H, W), -1.0)
+    has_lm = ~(u < -1.5) & (u >= 0)
+    out = base.copy()
+    out[..., :3] += spec * np.where(has_lm, 1.0, ao)[..., None]
+    sky = ~(depth < 1)
+    out[sky] = base[sky]
+    return out
+
+
+def test_no_inputs_leave_the_target():
+    for layout in (S.LAYOUT_REFERENCE, S.LAYOUT_F32, S.LAYOUT_F16):
+        cam, gb, glb, base = _frame(layout)
+        out, unsupported = oracle.reflections(cam.record, glb, gb, base)
+        assert not unsupported
+        np.testing.assert_array_equal(out, base)
+
+
+@pytest.mark.parametrize("with_lightmap", [False, True])
+def test_ssr_and_planar_match_numpy(with_lightmap):
+    cam, gb, glb, base = _frame()
+    ssr, planar, lm = S.reflection_images(gb.width, gb.height, 3)
+    lm = lm if with_lightmap else None
+    out, unsupported = oracle.reflections(cam.record, glb, gb, base, ssr=ssr, planar=planar, lightmap_uv=lm)
+    assert not unsupported
+    ref = _numpy_reflections(cam, gb, glb, base, ssr, planar, lm)
+    np.testing.assert_allclose(out, ref, rtol=1e-12, atol=1e-12)
+    covered = gb.planes[4] < 1
+    assert (np.abs(out - base)[covered][:, :3] > 0).any(-1).mean() > 0.5
+    np.testing.assert_array_equal(out[..., 3], base[..., 3])  # alpha kept
+
+
+def test_reflections_switched_off():
+    cam, gb, glb, base = _frame(enable_reflections=0)
+    ssr, planar, lm = S.reflection_images(gb.width, gb.height, 4)
+    out, _ = oracle.reflections(cam.record, glb, gb, base, ssr=ssr, planar=planar, lightmap_uv=lm)
+    np.testing.assert_array_equal(out, base)
+
+
+def test_full_confidence_ssr_is_fresnel_times_hit():
+    """With confidence 1 the SSR term replaces the environment term: spec = hit * F_ibl,
+    so doubling the hit colour doubles the added light."""
+    cam, gb, glb, base = _frame()
+    ssr, _, _ = S.reflection_images(gb.width, gb.height, 6)
+    ssr[..., 3] = 1.0
+    ssr[..., :3] = np.float16(0.5)
+    a, _ = oracle.reflections(cam.record, glb, gb, base, ssr=ssr)
+    ssr[..., :3] = np.float16(1.0)
+    b, _ = oracle.reflections(cam.record, glb, gb, base, ssr=ssr)
+    np.testing.assert_allclose(b - base, 2 * (a - base), rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("mode", [30, 31])
+def test_ssr_debug_modes_replace(mode):
+    cam, gb, glb, base = _frame(debug_mode=mode)
+    ssr, planar, _ = S.reflection_images(gb.width, gb.height, 8)
+    out, _ = oracle.reflections(cam.record, glb, gb, base, ssr=ssr, planar=planar)
+    covered = gb.planes[4] < 1
+    s = ssr.astype(np.float64)
+    want = np.concatenate([np.repeat(s[..., 3:4], 3, -1) if mode == 30 else s[..., :3], np.ones_like(s[..., :1])], -1)
+    np.testing.assert_array_equal(out[covered], want[covered])
+    np.testing.assert_array_equal(out[~covered], base[~covered])
+
+
+@pytest.mark.parametrize("mode", [1, 2, 4, 5, 10, 11, 20, 21])
+def test_lighting_debug_modes_add_nothing(mode):
+    cam, gb, glb, base = _frame(debug_mode=mode)
+    ssr, planar, _ = S.reflection_images(gb.width, gb.height, 9)
+    out, _ = oracle.reflections(cam.record, glb, gb, base, ssr=ssr, planar=planar)
+    np.testing.assert_array_equal(out, base)
+
+
+def test_rc_specular_only_on_rough_pixels():
+    cam, gb, glb, base = _frame(W=64, H=40)
+    g = S.rc_globals(glb, RC_MIN, RC_MAX)
+    probes = S.rc_probes(5)
+    with_rc, unsupported = oracle.reflections(cam.record, g, gb, base, rc=probes)
+    assert not unsupported
+    rough = gb.planes[2][..., 1].astype(np.float64) / 255.0
+    covered = gb.planes[4] < 1
+    changed = (with_rc != base).any(-1)
+    assert not changed[covered & (rough <= 0.6)].any()
+    assert changed[covered & (rough > 0.6)].mean() > 0.9
+    # blend weight smoothstep(0.6, 0.9, r) * 0.4 of a non-negative irradiance
+    assert (with_rc[..., :3] >= base[..., :3]).all()
+    # has_rc_gi without probes: the pixels that need them are reported
+    _, unsupported = oracle.reflections(cam.record, g, gb, base)
+    assert unsupported
