@@ -65,6 +65,7 @@ struct Globals {
 static_assert(sizeof(Camera) == HL_SIZEOF_GPU_CAMERA, "camera record");
 static_assert(sizeof(Light) == HL_SIZEOF_GPU_LIGHT, "light record");
 static_assert(sizeof(Globals) == HL_SIZEOF_DEFERRED_GLOBALS, "globals record");
+static_assert(sizeof(hl_reflection_inputs) == 56, "hl_reflection_inputs: 3 x (pointer, pitch) + rc pointer");
 
 // 4x4 inverse by Gauss-Jordan (column-major in and out).
 void invert(const double* m, double* out) {
@@ -248,6 +249,17 @@ void gpu_checks() {
           "hl_shade rejects a pitch shorter than a row");
     check(hl_shade(ctx, d_cam, d_glb, &gb, d_light, 1, &grid, &tgt, nullptr) == HL_OK, "hl_shade");
     check(hl_sync_status(ctx, nullptr) == HL_OK, "sync after hl_shade");
+    // the reflection draw with every input at its fallback adds nothing (checked below)
+    hl_reflection_inputs refl;
+    std::memset(&refl, 0, sizeof refl);
+    check(hl_shade_reflections(ctx, d_cam, d_glb, &gb, &refl, &tgt, nullptr) == HL_OK, "hl_shade_reflections");
+    check(hl_shade_reflections(ctx, d_cam, d_glb, &gb, nullptr, &tgt, nullptr) == HL_OK,
+          "hl_shade_reflections without inputs");
+    refl.ssr = static_cast<const char*>(d_out) + 2;
+    refl.ssr_pitch = W * 8;
+    check(hl_shade_reflections(ctx, d_cam, d_glb, &gb, &refl, &tgt, nullptr) == HL_ERR_LAYOUT,
+          "hl_shade_reflections rejects a misaligned SSR image");
+    check(hl_sync_status(ctx, nullptr) == HL_OK, "sync after hl_shade_reflections");
     std::vector<float> out(W * H * 4);
     check_cuda(cudaMemcpy(out.data(), d_out, W * H * 16, cudaMemcpyDeviceToHost), "read radiance");
     bool sky_ok = true;
