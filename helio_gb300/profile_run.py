@@ -31,6 +31,8 @@ def main(argv=None):
                     help="shade with the shadow term: lights 0-41 cast shadows (hl_shade_ex)")
     ap.add_argument("--atlas", type=int, default=1024, help="shadow atlas size in texels")
     ap.add_argument("--rc", action="store_true", help="shade with radiance-cascade GI (hl_shade_ex)")
+    ap.add_argument("--reflections", action="store_true",
+                    help="the reflection draw (hl_shade_reflections) over a reference-layout G-buffer")
     ap.add_argument("--scale", type=float, default=1.0)
     args = ap.parse_args(argv)
 
@@ -53,6 +55,21 @@ def main(argv=None):
             ev1.record()
         ctx.sync_status()
         print(f"G-buffer write {cam.width}x{cam.height}: {ev0.elapsed_time(ev1) * 1e3:.1f} us per frame", flush=True)
+        return
+    if args.reflections:
+        cam = S.default_camera(max(16, int(1920 * args.scale)), max(16, int(1080 * args.scale)))
+        gb = S.make_gbuffer(cam, S.LAYOUT_REFERENCE, seed=23)
+        glb = L.make_globals(L.tile_grid(cam.width, cam.height)[0], 0)
+        df = FR.upload(cam.record, glb, [], gb)
+        imgs = [torch.from_numpy(a).cuda() for a in S.reflection_images(cam.width, cam.height, 77)]
+        out = torch.ones((cam.height, cam.width, 4), dtype=torch.float32, device="cuda")
+        for _ in range(args.frames):
+            ev0.record()
+            ctx.shade_reflections(df.camera, df.globals_, df.gbuffer, N.target_struct(out), ssr=imgs[0],
+                                  planar=imgs[1], lightmap_uv=imgs[2])
+            ev1.record()
+        ctx.sync_status()
+        print(f"reflections {cam.width}x{cam.height}: {ev0.elapsed_time(ev1) * 1e3:.1f} us per frame", flush=True)
         return
     if args.batched:
         views, lights = S.batched_views(args.scale)
