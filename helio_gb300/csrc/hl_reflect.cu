@@ -7,9 +7,9 @@
 // alpha kept). Only pixels rough enough for the radiance-cascade fallback
 // (roughness > 0.6 with has_rc_gi) gather the 8 probe corners, through the same
 // sampler as the ambient term of the lighting kernel (sample_rc_specular, :928-980, is
-// sample_rc_irradiance along another direction). The world position and the view
-// vector are reconstructed in double-float as in the precise lighting paths, so the
-// Fresnel term and the reflection vector carry f32 rounding only.
+// sample_rc_irradiance along another direction). The world position is reconstructed
+// in double-float as in the precise lighting paths and V normalised from it in f32, so
+// the Fresnel term and the reflection vector carry f32 rounding only.
 #include <cuda_fp16.h>
 
 #include "hl_common.cuh"
@@ -132,14 +132,19 @@ __global__ void __launch_bounds__(kRefThreadsX* kRefThreadsY, 3)
                          fminf(fmaxf(t.f0b, 0.0f), 0.999f)};
     const bool has_lightmap = !(lmu < -1.5f) && lmu >= 0.0f;
 
-    // World position and V (:1305-1309) in double-float.
+    // World position (:1305-1307) as a double-float without the row renormalisation
+    // (~4e-10 relative at far depth); V (:1308) from camera - P with the low word folded
+    // in, normalised in f32: F_ibl and R need V to f32 accuracy only.
     const GpuCamera* cam = p.camera;
-    Pixel px;
-    PixelBrdf pb;
-    reconstruct<true, true>(cam->inv_view_proj, x, y, float(p.gb.width), float(p.gb.height), t.depth, px.Px, px.Py,
-                            px.Pz, px.Plx, px.Ply, px.Plz);
-    df_view(px, pb, cam->position_near[0], cam->position_near[1], cam->position_near[2]);
-    const float Vx = px.Vx, Vy = px.Vy, Vz = px.Vz;
+    float Px, Py, Pz, Plx, Ply, Plz;
+    reconstruct<true, false>(cam->inv_view_proj, x, y, float(p.gb.width), float(p.gb.height), t.depth, Px, Py, Pz,
+                             Plx, Ply, Plz);
+    float Vx = (cam->position_near[0] - Px) - Plx, Vy = (cam->position_near[1] - Py) - Ply,
+          Vz = (cam->position_near[2] - Pz) - Plz;
+    const float vn = sqrtf(Vx * Vx + Vy * Vy + Vz * Vz);
+    Vx /= vn;
+    Vy /= vn;
+    Vz /= vn;
     const float nv = Nx * Vx + Ny * Vy + Nz * Vz;
     const float ndv = fmaxf(nv, 0.0f);
     const float c = fminf(fmaxf(1.0f - ndv, 0.0f), 1.0f);
@@ -173,7 +178,7 @@ __global__ void __launch_bounds__(kRefThreadsX* kRefThreadsY, 3)
         ly /= ll;
         lz /= ll;
         float ir, ig, ib;
-        rc::irradiance(p.rc, glb, px.Px + px.Plx, px.Py + px.Ply, px.Pz + px.Plz, lx, ly, lz, ir, ig, ib);
+        rc::irradiance(p.rc, glb, Px + Plx, Py + Ply, Pz + Plz, lx, ly, lz, ir, ig, ib);
         const float w = smoothstep_(0.6f, 0.9f, rough) * 0.4f;
         spec[0] = spec[0] * (1.0f - w) + ir * w;
         spec[1] = spec[1] * (1.0f - w) + ig * w;
