@@ -24,9 +24,7 @@ def _frame(layout=S.LAYOUT_REFERENCE, W=48, H=32, seed=5, **glb_kw):
 
 def _numpy_reflections(cam, gb, glb, base, ssr, planar, lm):
     """fs_reflection without RC, restated over whole images in float64."""
-    t = gb.truth
     H, W = base.shape[:2]
-    depth = t["depth"].astype(np.float64)
     if gb.layout == S.LAYOUT_REFERENCE:
         nr = gb.planes[1].astype(np.float64)
         orm = gb.planes[2].astype(np.float64) / 255.0
@@ -34,6 +32,12 @@ def _numpy_reflections(cam, gb, glb, base, ssr, planar, lm):
         n_raw, ao, rough = nr[..., :3], orm[..., 0], orm[..., 1]
         f0 = np.stack([nr[..., 3], orm[..., 3], em[..., 3]], -1)
         depth = gb.planes[4].astype(np.float64)
+    elif gb.layout == S.LAYOUT_F32:  # ao 1, F0 = clamp(mix(0.04, albedo, metallic)) (gbuffer.wgsl:323-328)
+        p0, p1 = gb.planes[0].astype(np.float64), gb.planes[1].astype(np.float64)
+        n_raw, rough, metal = p1[..., :3], p0[..., 3], p1[..., 3]
+        ao = np.ones_like(rough)
+        f0 = 0.04 * (1 - metal[..., None]) + p0[..., :3] * metal[..., None]
+        depth = gb.planes[2].astype(np.float64)
     else:
         raise NotImplementedError
     N = n_raw / np.linalg.norm(n_raw, axis=-1, keepdims=True)
@@ -74,16 +78,17 @@ def test_no_inputs_leave_the_target():
         np.testing.assert_array_equal(out, base)
 
 
+@pytest.mark.parametrize("layout", [S.LAYOUT_REFERENCE, S.LAYOUT_F32])
 @pytest.mark.parametrize("with_lightmap", [False, True])
-def test_ssr_and_planar_match_numpy(with_lightmap):
-    cam, gb, glb, base = _frame()
+def test_ssr_and_planar_match_numpy(with_lightmap, layout):
+    cam, gb, glb, base = _frame(layout)
     ssr, planar, lm = S.reflection_images(gb.width, gb.height, 3)
     lm = lm if with_lightmap else None
     out, unsupported = oracle.reflections(cam.record, glb, gb, base, ssr=ssr, planar=planar, lightmap_uv=lm)
     assert not unsupported
     ref = _numpy_reflections(cam, gb, glb, base, ssr, planar, lm)
     np.testing.assert_allclose(out, ref, rtol=1e-12, atol=1e-12)
-    covered = gb.planes[4] < 1
+    covered = gb.planes[-1] < 1
     assert (np.abs(out - base)[covered][:, :3] > 0).any(-1).mean() > 0.5
     np.testing.assert_array_equal(out[..., 3], base[..., 3])  # alpha kept
 
