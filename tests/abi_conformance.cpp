@@ -151,6 +151,19 @@ void cpu_checks() {
     check(hl_froxel_slice_table(nullptr, tab.data()) == HL_ERR_INVALID_ARGUMENT, "NULL params rejected");
     check(hl_create(nullptr, 0) == HL_ERR_INVALID_ARGUMENT, "hl_create(NULL) rejected");
     check(hl_destroy(nullptr) == HL_OK, "hl_destroy(NULL) is a no-op");
+    // every pass entry point rejects a NULL context before touching a device
+    check(hl_shade(nullptr, nullptr, nullptr, nullptr, nullptr, 0, nullptr, nullptr, nullptr) ==
+              HL_ERR_INVALID_ARGUMENT,
+          "hl_shade(NULL ctx) rejected");
+    check(hl_shade_ex(nullptr, nullptr, nullptr, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr) ==
+              HL_ERR_INVALID_ARGUMENT,
+          "hl_shade_ex(NULL ctx) rejected");
+    check(hl_shade_reflections(nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr) ==
+              HL_ERR_INVALID_ARGUMENT,
+          "hl_shade_reflections(NULL ctx) rejected");
+    check(hl_write_gbuffer(nullptr, nullptr, nullptr, 0, nullptr, nullptr, 0, nullptr, 0, nullptr, nullptr) ==
+              HL_ERR_INVALID_ARGUMENT,
+          "hl_write_gbuffer(NULL ctx) rejected");
 }
 
 void gpu_checks() {
