@@ -38,8 +38,19 @@ def _numpy_reflections(cam, gb, glb, base, ssr, planar, lm):
         ao = np.ones_like(rough)
         f0 = 0.04 * (1 - metal[..., None]) + p0[..., :3] * metal[..., None]
         depth = gb.planes[2].astype(np.float64)
-    else:
-        raise NotImplementedError
+    else:  # F16: octahedral normal (Cigolle et al. 2014, z-up, signNotZero), metallic F0, ao 1
+        p0 = gb.planes[0].astype(np.float64)
+        o = gb.planes[1].astype(np.float64)
+        metal = gb.planes[2].astype(np.float64).reshape(p0.shape[:2])
+        u, v = o[..., 0], o[..., 1]
+        z = 1 - np.abs(u) - np.abs(v)
+        sx, sy = np.where(u >= 0, 1.0, -1.0), np.where(v >= 0, 1.0, -1.0)
+        x = np.where(z < 0, (1 - np.abs(v)) * sx, u)
+        y = np.where(z < 0, (1 - np.abs(u)) * sy, v)
+        n_raw, rough = np.stack([x, y, z], -1), p0[..., 3]
+        ao = np.ones_like(rough)
+        f0 = 0.04 * (1 - metal[..., None]) + p0[..., :3] * metal[..., None]
+        depth = gb.planes[3].astype(np.float64)
     N = n_raw / np.linalg.norm(n_raw, axis=-1, keepdims=True)
     f0 = np.clip(f0, 0.0, 0.999)
     xs, ys = np.meshgrid(np.arange(W) + 0.5, np.arange(H) + 0.5)
@@ -78,7 +89,7 @@ def test_no_inputs_leave_the_target():
         np.testing.assert_array_equal(out, base)
 
 
-@pytest.mark.parametrize("layout", [S.LAYOUT_REFERENCE, S.LAYOUT_F32])
+@pytest.mark.parametrize("layout", [S.LAYOUT_REFERENCE, S.LAYOUT_F32, S.LAYOUT_F16])
 @pytest.mark.parametrize("with_lightmap", [False, True])
 def test_ssr_and_planar_match_numpy(with_lightmap, layout):
     cam, gb, glb, base = _frame(layout)
