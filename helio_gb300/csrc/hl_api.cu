@@ -71,7 +71,7 @@ hl_status shade_common(hl_ctx* ctx, const void* camera, const void* globals, con
         return s;
     cudaError_t e = hl::launch_shade(gbuffer->layout, grid->kind, stats ? HL_TARGET_RGBA32F : radiance->format, camera,
                                      globals, gv, lights, n_lights, grv, tab, tv, stats, ctx->d_status,
-                                     ctx->shade_cand, as_stream(stream), (shadows || rc) ? &sv : nullptr);
+                                     ctx->shade_cand, ctx->pair_log, as_stream(stream), (shadows || rc) ? &sv : nullptr);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "shade launch");
     return HL_OK;
 }
@@ -244,6 +244,18 @@ hl_status hl_shade_stats(hl_ctx* ctx, const void* camera, const void* globals, c
                          void* stream) {
     if (!counts) return fail(ctx, HL_ERR_INVALID_ARGUMENT, "stats counts is NULL");
     return shade_common(ctx, camera, globals, gbuffer, lights, n_lights, grid, nullptr, counts, stream);
+}
+
+hl_status hl_set_pair_log(hl_ctx* ctx, uint32_t* pairs, uint32_t capacity, uint32_t* count) {
+    if (!ctx) return HL_ERR_INVALID_ARGUMENT;
+    if (!pairs) {
+        ctx->pair_log = hl::PairLog{nullptr, nullptr, 0};
+        return HL_OK;
+    }
+    if (!count || !aligned(pairs, 8) || !aligned(count, 4))
+        return fail(ctx, HL_ERR_INVALID_ARGUMENT, "pair log: count is NULL or pairs/count misaligned");
+    ctx->pair_log = hl::PairLog{reinterpret_cast<uint2*>(pairs), count, capacity};
+    return HL_OK;
 }
 
 hl_status hl_shade_adjoint(hl_ctx* ctx, const void* camera, const void* globals, const hl_gbuffer* gbuffer,

@@ -28,6 +28,7 @@ struct hl_ctx {
     uint32_t frag_lights_cap = 0;
     float* adjoint_partials = nullptr;  // per-CTA light-gradient partials of hl_shade_adjoint
     uint32_t adjoint_partials_cap = 0;
+    hl::PairLog pair_log{nullptr, nullptr, 0};  // lit-pair record of the shading launches (hl_set_pair_log)
     std::string last_error;
 };
 

@@ -84,11 +84,33 @@ struct ExtView {
     uint64_t rc_pitch;
 };
 
+// Record of the (pixel, light) pairs a shading launch lit: pairs[k] = (y * W + x, light
+// index) for k < min(*count, capacity); *count counts every lit pair. pairs == nullptr:
+// nothing is recorded (the normal case).
+struct PairLog {
+    uint2* pairs;
+    uint32_t* count;
+    uint32_t capacity;
+};
+
 // ext != nullptr selects the extended variant (hl_shade_ex, hl_shade_shadowed).
 cudaError_t launch_shade(uint32_t layout, uint32_t grid_kind, uint32_t target_format, const void* camera,
                          const void* globals, const GBufView& gb, const void* lights, uint32_t n_lights,
                          const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats,
-                         int* status, float4* cand, cudaStream_t stream, const ExtView* ext = nullptr);
+                         int* status, float4* cand, const PairLog& log, cudaStream_t stream,
+                         const ExtView* ext = nullptr);
+
+// The candidate-test light table of the shading kernels: per light its position
+// (camera-relative when `relative`) and range^2 (1 + 2^-9), or -1 for a directional
+// light. Launched as a dependent launch of its predecessor.
+cudaError_t launch_prep_cand(const void* camera, const void* lights, uint32_t n, bool relative, float4* cand,
+                             cudaStream_t stream);
+
+// Shading of an FP16 G-buffer over froxel lists (hl_shade's headline form).
+cudaError_t launch_shade_f16(uint32_t target_format, const void* camera, const void* globals, const GBufView& gb,
+                             const void* lights, uint32_t n_lights, const GridView& grid, const SliceTable& tab,
+                             const TargetView& out, int* status, float4* cand, const PairLog& log,
+                             cudaStream_t stream);
 
 // Adjoint of shading. partials: grid_size * n_lights * 8 floats of scratch.
 uint32_t adjoint_grid_size(int device, uint32_t width, uint32_t height);

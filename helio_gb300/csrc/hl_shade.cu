@@ -21,6 +21,7 @@
 #include "hl_indirect.cuh"
 #include "hl_shadow.cuh"
 #include "hl_texel.cuh"
+#include "hl_precise.cuh"
 
 namespace hl {
 
@@ -158,33 +159,13 @@ __device__ __forceinline__ void load_pixel(const Smem<NPX, NF>& s, int i, Pixel&
 
 }  // namespace sk
 
-// Precise re-evaluation of an ill-conditioned pair of the fast path: the pixel's
-// position as a camera-relative double-float (the light's rounding residual r folded
-// into its lo part), compensated NdV and NdL. Rare; kept out of line.
-__device__ __noinline__ int precise_pair(const GpuCamera* cam, uint32_t x, uint32_t y, float W, float H, float depth,
-                                         const Pixel& pin, float ar, float ag, float ab, const ShadeLight& l, float rx,
-                                         float ry, float rz, float& cr, float& cg, float& cb) {
-    Pixel p = pin;
-    const float camx = cam->position_near[0], camy = cam->position_near[1], camz = cam->position_near[2];
-    reconstruct<true, false>(cam->inv_view_proj, x, y, W, H, depth, p.Px, p.Py, p.Pz, p.Plx, p.Ply, p.Plz);
-    const DF ax = two_sum(p.Px, -camx), ay = two_sum(p.Py, -camy), az = two_sum(p.Pz, -camz);
-    const DF bx = two_sum(ax.hi, ax.lo + p.Plx), by = two_sum(ay.hi, ay.lo + p.Ply), bz = two_sum(az.hi, az.lo + p.Plz);
-    p.Px = bx.hi; p.Plx = bx.lo - rx;
-    p.Py = by.hi; p.Ply = by.lo - ry;
-    p.Pz = bz.hi; p.Plz = bz.lo - rz;
-    // V = -(true P): the camera sits at minus the residual
-    finish_pixel<true>(p, p.nrx, p.nry, p.nrz, ar, ag, ab, p.rough, p.metal, p.f0r, p.f0g, p.f0b, -rx, -ry, -rz);
-    const PixelBrdf pb = pixel_brdf(p);
-    return eval<true, false>(p, pb, l, cr, cg, cb);
-}
-
 // Evaluates nb queued pairs (ring positions head..head+nb-1), one per lane, and adds
 // them into the per-pixel Kahan accumulators in queue order. Out of line so that the
 // BRDF code exists once in the kernel.
 template <uint32_t LAYOUT, bool STATS, int TW, int NPX, bool EXT>
 __device__ __noinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>()>& s, const uint32_t* queue, uint32_t head, uint32_t nb,
                                          uint32_t lane, const GpuCamera* cam, const GpuLight* lights, uint32_t x0,
-                                         uint32_t y0, float W, float H, const ExtView* sv) {
+                                         uint32_t y0, float W, float H, const ExtView* sv, const PairLog log) {
     using namespace sk;
     constexpr bool PRECISE = (LAYOUT != HL_GBUF_F16);
     uint32_t (*cnt)[NPX] = reinterpret_cast<uint32_t (*)[NPX]>(s.acc);
@@ -244,6 +225,17 @@ __device__ __noinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>
         }
     }
     const bool lit = act && st == kLit;
+    if (!STATS && log.pairs) {  // record the pairs the kernel lit (branch decisions for verification)
+        const uint32_t m = __ballot_sync(0xffffffffu, lit);
+        if (m) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(log.count, uint32_t(__popc(m)));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            const uint32_t slot = base + __popc(m & lanemask_lt());
+            if (lit && slot < log.capacity)
+                log.pairs[slot] = make_uint2((y0 + q / TW) * uint32_t(W) + x0 + q % TW, li);
+        }
+    }
     if (STATS) {
         if (act && rng) atomicAdd(&cnt[1][q], 1u);
         if (lit) atomicAdd(&cnt[2][q], 1u);
@@ -276,7 +268,7 @@ __device__ __forceinline__ void shade_tile(
     const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const GBufView& gb,
     const GpuLight* __restrict__ lights, const float4* __restrict__ cand, uint32_t n_lights, const GridView& grid,
     const float* __restrict__ tabz, const TargetView& out, uint32_t* __restrict__ stats, int* __restrict__ status,
-    uint32_t bx, uint32_t by, const ExtView* sv = nullptr) {
+    uint32_t bx, uint32_t by, const ExtView* sv, const PairLog& log) {
     using namespace sk;
     constexpr bool FROXELS = (GRID == HL_GRID_FROXELS);
     constexpr int NPX = TW * TH;
@@ -541,7 +533,7 @@ __device__ __forceinline__ void shade_tile(
                     qlen += __popc(pm);
                     __syncwarp();
                     if (qlen >= 32) {
-                        flush_batch<LAYOUT, STATS, TW, NPX, EXT>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H, sv);
+                        flush_batch<LAYOUT, STATS, TW, NPX, EXT>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H, sv, log);
                         head += 32;
                         qlen -= 32;
                     }
@@ -576,13 +568,13 @@ __device__ __forceinline__ void shade_tile(
             }
             __syncwarp();
             while (qlen >= 32) {
-                flush_batch<LAYOUT, STATS, TW, NPX, EXT>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H, sv);
+                flush_batch<LAYOUT, STATS, TW, NPX, EXT>(s, queue, head, 32, lane, cam, lights, x0, y0, W, H, sv, log);
                 head += 32;
                 qlen -= 32;
             }
         }
     }
-    if (qlen > 0) flush_batch<LAYOUT, STATS, TW, NPX, EXT>(s, queue, head, qlen, lane, cam, lights, x0, y0, W, H, sv);
+    if (qlen > 0) flush_batch<LAYOUT, STATS, TW, NPX, EXT>(s, queue, head, qlen, lane, cam, lights, x0, y0, W, H, sv, log);
 
     // ---- 5. output -----------------------------------------------------------------
     __syncthreads();
@@ -678,9 +670,9 @@ __global__ void __launch_bounds__(sk::kThreads, 3) shade_kernel(
     const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const GBufView gb,
     const GpuLight* __restrict__ lights, uint32_t n_lights, const GridView grid, const __grid_constant__ SliceTable tab,
     const TargetView out, uint32_t* __restrict__ stats, int* __restrict__ status, const float4* __restrict__ cand,
-    const __grid_constant__ ExtView sv) {
+    const __grid_constant__ ExtView sv, const __grid_constant__ PairLog log) {
     shade_tile<LAYOUT, GRID, TARGET, STATS, TW, TH, true, EXT>(cam, glb, gb, lights, cand, n_lights, grid, tab.z,
-                                                                  out, stats, status, blockIdx.x, blockIdx.y, &sv);
+                                                                  out, stats, status, blockIdx.x, blockIdx.y, &sv, log);
 }
 
 // Every tile of every view of a batch (froxel grids, 32x16 tiles): CTA b lights tile
@@ -701,7 +693,8 @@ __global__ void __launch_bounds__(sk::kThreads, 3) shade_batched_kernel(
     const TargetView out = v.out;
     shade_tile<LAYOUT, HL_GRID_FROXELS, TARGET, false, 32, 16>(static_cast<const GpuCamera*>(v.camera), glb, gb, lights,
                                                                v.cand, n_lights, grid, v.tabz, out, nullptr, status,
-                                                               local % v.tiles_x, local / v.tiles_x);
+                                                               local % v.tiles_x, local / v.tiles_x, nullptr,
+                                                               PairLog{nullptr, nullptr, 0});
 }
 
 // The light table of the candidate tests: position (camera-relative on the FP16
@@ -758,7 +751,7 @@ cudaError_t launch_batched(const ShadeViewDesc* descs, uint32_t n_views, uint32_
 template <uint32_t LAYOUT, uint32_t GRID, uint32_t TARGET, bool STATS, bool EXT = false>
 cudaError_t launch_one(const void* camera, const void* globals, const GBufView& gb, const void* lights, uint32_t n,
                        const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats, int* status, float4* cand,
-                       cudaStream_t stream, const ExtView* sv = nullptr) {
+                       const PairLog& log, cudaStream_t stream, const ExtView* sv = nullptr) {
     constexpr bool FROXELS = (GRID == HL_GRID_FROXELS);
     constexpr int TW = FROXELS ? 32 : 16, TH = 16;
     auto kern = shade_kernel<LAYOUT, GRID, TARGET, STATS, TW, TH, EXT>;
@@ -782,59 +775,70 @@ cudaError_t launch_one(const void* camera, const void* globals, const GBufView& 
     if (sv) svv = *sv;
     return launch_pdl(kern, g, dim3(sk::kThreads), smem, stream, static_cast<const GpuCamera*>(camera),
                       static_cast<const DeferredGlobals*>(globals), gb, static_cast<const GpuLight*>(lights), n, grid,
-                      tab, out, stats, status, static_cast<const float4*>(cand), svv);
+                      tab, out, stats, status, static_cast<const float4*>(cand), svv, log);
 }
 
 template <uint32_t LAYOUT, uint32_t GRID>
 cudaError_t dispatch_target(uint32_t target, const void* camera, const void* globals, const GBufView& gb,
                             const void* lights, uint32_t n, const GridView& grid, const SliceTable& tab,
-                            const TargetView& out, uint32_t* stats, int* status, float4* cand, cudaStream_t stream,
-                            const ExtView* sv) {
+                            const TargetView& out, uint32_t* stats, int* status, float4* cand, const PairLog& log,
+                            cudaStream_t stream, const ExtView* sv) {
     if (sv && !stats) {
         if (target == HL_TARGET_RGBA16F)
             return launch_one<LAYOUT, GRID, HL_TARGET_RGBA16F, false, true>(camera, globals, gb, lights, n, grid, tab,
-                                                                            out, stats, status, cand, stream, sv);
+                                                                            out, stats, status, cand, log, stream, sv);
         return launch_one<LAYOUT, GRID, HL_TARGET_RGBA32F, false, true>(camera, globals, gb, lights, n, grid, tab, out,
-                                                                        stats, status, cand, stream, sv);
+                                                                        stats, status, cand, log, stream, sv);
     }
     if (stats)
         return launch_one<LAYOUT, GRID, HL_TARGET_RGBA32F, true>(camera, globals, gb, lights, n, grid, tab, out, stats,
-                                                                 status, cand, stream);
+                                                                 status, cand, log, stream);
     if (target == HL_TARGET_RGBA16F)
         return launch_one<LAYOUT, GRID, HL_TARGET_RGBA16F, false>(camera, globals, gb, lights, n, grid, tab, out,
-                                                                  stats, status, cand, stream);
+                                                                  stats, status, cand, log, stream);
     return launch_one<LAYOUT, GRID, HL_TARGET_RGBA32F, false>(camera, globals, gb, lights, n, grid, tab, out, stats,
-                                                              status, cand, stream);
+                                                              status, cand, log, stream);
 }
 
 template <uint32_t LAYOUT>
 cudaError_t dispatch_grid(uint32_t grid_kind, uint32_t target, const void* camera, const void* globals,
                           const GBufView& gb, const void* lights, uint32_t n, const GridView& grid,
                           const SliceTable& tab, const TargetView& out, uint32_t* stats, int* status, float4* cand,
-                          cudaStream_t stream, const ExtView* sv) {
+                          const PairLog& log, cudaStream_t stream, const ExtView* sv) {
     if (grid_kind == HL_GRID_FROXELS)
         return dispatch_target<LAYOUT, HL_GRID_FROXELS>(target, camera, globals, gb, lights, n, grid, tab, out, stats,
-                                                        status, cand, stream, sv);
+                                                        status, cand, log, stream, sv);
     return dispatch_target<LAYOUT, HL_GRID_TILES>(target, camera, globals, gb, lights, n, grid, tab, out, stats,
-                                                  status, cand, stream, sv);
+                                                  status, cand, log, stream, sv);
 }
 
 }  // namespace
 
+cudaError_t launch_prep_cand(const void* camera, const void* lights, uint32_t n, bool relative, float4* cand,
+                             cudaStream_t stream) {
+    return launch_pdl(prep_cand_kernel, dim3((n + 255) / 256), dim3(256), 0, stream,
+                      static_cast<const GpuCamera*>(camera), static_cast<const GpuLight*>(lights), n,
+                      relative ? 1u : 0u, cand);
+}
+
 cudaError_t launch_shade(uint32_t layout, uint32_t grid_kind, uint32_t target_format, const void* camera,
                          const void* globals, const GBufView& gb, const void* lights, uint32_t n_lights,
                          const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats,
-                         int* status, float4* cand, cudaStream_t stream, const ExtView* shadows) {
+                         int* status, float4* cand, const PairLog& log, cudaStream_t stream,
+                         const ExtView* shadows) {
+    if (layout == HL_GBUF_F16 && grid_kind == HL_GRID_FROXELS && !stats && !shadows)
+        return launch_shade_f16(target_format, camera, globals, gb, lights, n_lights, grid, tab, out, status, cand, log,
+                                stream);
     switch (layout) {
         case HL_GBUF_REFERENCE:
             return dispatch_grid<HL_GBUF_REFERENCE>(grid_kind, target_format, camera, globals, gb, lights, n_lights,
-                                                    grid, tab, out, stats, status, cand, stream, shadows);
+                                                    grid, tab, out, stats, status, cand, log, stream, shadows);
         case HL_GBUF_F32:
             return dispatch_grid<HL_GBUF_F32>(grid_kind, target_format, camera, globals, gb, lights, n_lights, grid,
-                                              tab, out, stats, status, cand, stream, shadows);
+                                              tab, out, stats, status, cand, log, stream, shadows);
         default:
             return dispatch_grid<HL_GBUF_F16>(grid_kind, target_format, camera, globals, gb, lights, n_lights, grid,
-                                              tab, out, stats, status, cand, stream, shadows);
+                                              tab, out, stats, status, cand, log, stream, shadows);
     }
 }
 

@@ -1,0 +1,601 @@
+// hl_shade_f16.cu — deferred lighting (fs_main under fallback bindings) of an FP16
+// G-buffer over froxel lists, the headline form of hl_shade.
+//
+// One CTA of 256 threads lights a 32x16-pixel tile:
+//  1. threads decode the tile's G-buffer texels (coalesced along x) and set each pixel
+//     up into a shared-memory record: camera-relative position, unit normal, NdV, F0,
+//     albedo/pi and the view's BRDF constants, with its froxel;
+//  2. pixels are counting-sorted by froxel and, inside a froxel, by a depth sub-bin of
+//     its slice, so that a group of 32 consecutive sorted pixels spans one froxel (or
+//     a few of adjacent slices) and a narrow depth range;
+//  3. a warp takes a group. For each froxel of the group it culls the froxel's list
+//     against the bounding box of the group's pixels in that froxel (lanes test 32
+//     lights at once), and each of those pixels keeps the survivors as a bit mask. Then
+//     every lane walks its own mask, testing its pixel against each surviving light for
+//     range and the NdL sign. The box test applies the per-pixel test's own f32
+//     operations to box-clamped differences, so every pair the per-pixel test passes
+//     survives it: the queued pairs are exactly those of a walk over the pixel's whole
+//     list, in list order;
+//  4. queued (pixel, light) pairs are evaluated 32 at a time, one per lane, and added
+//     into per-pixel Kahan accumulators in queue order, which is list order for every
+//     pixel, as the reference's light loop (deferred_lighting.wgsl:1119-1146) adds them.
+//     The pairs left in the warps' queues at the end are evaluated together, 32 per
+//     warp, and each warp then adds its own in order;
+//  5. threads compose hemisphere ambient and store their pixels.
+#include "hl_common.cuh"
+#include "hl_internal.h"
+#include "hl_precise.cuh"
+#include "hl_shade_math.cuh"
+#include "hl_texel.cuh"
+
+namespace hl {
+
+namespace {
+
+using namespace sm;
+
+namespace f16k {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int TW = 32, TH = 16, NPX = TW * TH;
+constexpr int PPT = NPX / kThreads;  // pixels per thread in set-up and output
+constexpr int NG = NPX / 32;         // groups of 32 sorted pixels
+constexpr int kQueue = 64;           // per-warp pair ring: at most 31 + 32 pending
+constexpr int kBins = 512;           // keys of the pixel sort
+static_assert(31 + 32 <= kQueue, "pair ring too small");
+
+// Pixel record fields (structure of arrays).
+enum Field : int {
+    F_PX, F_PY, F_PZ,   // camera-relative position (f32)
+    F_NX, F_NY, F_NZ,   // unit normal
+    F_IP,               // 1 / |P|: V = -P / |P|
+    F_NDV,              // max(N.V, 0)
+    F_DEP,              // NDC depth; negative: seen at a grazing angle, every pair precise
+    F_F0R, F_F0G, F_F0B,
+    F_DR, F_DG, F_DB,   // albedo / pi
+    F_A2, F_K, F_GV,    // roughness^4, (r+1)^2/8, Schlick-GGX of the view
+    F_METAL,
+    F_COUNT
+};
+
+struct Smem {
+    float px[F_COUNT][NPX];
+    float acc[6][NPX];  // Kahan (sum, compensation) x RGB
+    union {
+        struct {
+            uint32_t hist[kBins];
+            float tab[kMaxSlices + 1];
+            uint16_t col_of[TW], row_of[TH];
+        } sort;
+        uint32_t queue[kWarps][kQueue];  // walk: ring of (pixel << 23) | light index
+    } u;
+    union {
+        struct {
+            uint32_t fidx[NPX];    // froxel of the pixel
+            uint16_t order[NPX];   // pixels sorted by key
+        } walk;
+        struct {
+            uint32_t left[kThreads];  // pairs left in the warps' queues
+            float4 res[kThreads];     // their contributions (w: status)
+        } tail;
+    } w;
+    uint32_t warp_tot[kWarps];
+    uint32_t n_valid, next_group, n_left;
+    uint32_t fx0, fy0, ncx, ncols, kshift, by_column;
+};
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Order-preserving map of f32 to s32 (for warp min/max reductions of coordinates).
+__device__ __forceinline__ int f2o(float v) {
+    const int k = __float_as_int(v);
+    return k ^ ((k >> 31) & 0x7fffffff);
+}
+__device__ __forceinline__ float o2f(int k) { return __int_as_float(k ^ ((k >> 31) & 0x7fffffff)); }
+
+__device__ __forceinline__ float h2f(uint32_t bits16) { return __half2float(__ushort_as_half(uint16_t(bits16))); }
+
+}  // namespace f16k
+
+// The precise evaluation of the pair (pixel (x, y), light li), from the pixel's texel
+// and the light buffer, so that only scalars cross the call. Returns (r, g, b, status).
+__device__ __noinline__ float4 precise_f16(const GBufView& gb, uint32_t x, uint32_t y, const GpuCamera* cam,
+                                           const GpuLight* lights, uint32_t li) {
+    const gbuf::Texel<HL_GBUF_F16> tx = gbuf::load_texel<HL_GBUF_F16>(gb, x, y);
+    Pixel p;
+    p.nrx = tx.nx; p.nry = tx.ny; p.nrz = tx.nz;
+    p.rough = tx.rough;
+    p.metal = tx.metal;
+    p.f0r = tx.f0r; p.f0g = tx.f0g; p.f0b = tx.f0b;
+    const float4* gl = reinterpret_cast<const float4*>(lights + li);
+    const float4 a = __ldg(gl + 0), b = __ldg(gl + 1), c = __ldg(gl + 2);
+    const uint4 d = __ldg(reinterpret_cast<const uint4*>(gl + 3));
+    const float camx = cam->position_near[0], camy = cam->position_near[1], camz = cam->position_near[2];
+    const DF ux = two_sum(a.x, -camx), uy = two_sum(a.y, -camy), uz = two_sum(a.z, -camz);
+    ShadeLight l;
+    l.px = ux.hi; l.py = uy.hi; l.pz = uz.hi;
+    l.range = a.w;
+    l.dx = b.x; l.dy = b.y; l.dz = b.z; l.cos_outer = b.w;
+    l.cr = c.x; l.cg = c.y; l.cb = c.z; l.intensity = c.w;
+    l.type = d.y;
+    l.cos_inner = __uint_as_float(d.z);
+    float4 o = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const int st = precise_pair(cam, x, y, float(gb.width), float(gb.height), tx.depth, p, tx.ar, tx.ag, tx.ab, l,
+                                ux.lo, uy.lo, uz.lo, o.x, o.y, o.z);
+    o.w = __int_as_float(st);
+    return o;
+}
+
+// pbr_direct_light of one queued pair (pixel q of the tile at x0, y0; light li) on the
+// fast path, handed to precise_f16 when the guard flags it or the pixel is grazing.
+// Returns (r, g, b) and the status in w.
+__device__ __forceinline__ float4 eval_pair(const f16k::Smem& s, uint32_t q, uint32_t li, const GpuCamera* cam,
+                                            const GpuLight* lights, const GBufView& gb, uint32_t x0, uint32_t y0) {
+    using namespace f16k;
+    Pixel p;
+    p.Px = s.px[F_PX][q]; p.Py = s.px[F_PY][q]; p.Pz = s.px[F_PZ][q];
+    p.Plx = p.Ply = p.Plz = 0.0f;
+    p.Nx = s.px[F_NX][q]; p.Ny = s.px[F_NY][q]; p.Nz = s.px[F_NZ][q];
+    const float ip = s.px[F_IP][q];
+    p.Vx = -p.Px * ip;
+    p.Vy = -p.Py * ip;
+    p.Vz = -p.Pz * ip;
+    p.NdV = s.px[F_NDV][q];
+    p.f0r = s.px[F_F0R][q]; p.f0g = s.px[F_F0G][q]; p.f0b = s.px[F_F0B][q];
+    p.dr = s.px[F_DR][q]; p.dg = s.px[F_DG][q]; p.db = s.px[F_DB][q];
+    PixelBrdf pb;
+    pb.a2 = s.px[F_A2][q];
+    pb.k = s.px[F_K][q];
+    pb.omk = 1.0f - pb.k;
+    pb.gv = s.px[F_GV][q];
+    pb.one_m_metal = 1.0f - s.px[F_METAL][q];
+    pb.nv4 = 4.0f * p.NdV;
+    pb.vlx = pb.vly = pb.vlz = 0.0f;
+    const float4* gl = reinterpret_cast<const float4*>(lights + li);
+    const float4 a = __ldg(gl + 0), b = __ldg(gl + 1), c = __ldg(gl + 2);
+    const uint4 d = __ldg(reinterpret_cast<const uint4*>(gl + 3));
+    ShadeLight l;
+    l.px = a.x - cam->position_near[0];  // camera-relative light position (high word of its two-sum)
+    l.py = a.y - cam->position_near[1];
+    l.pz = a.z - cam->position_near[2];
+    l.range = a.w;
+    l.dx = b.x; l.dy = b.y; l.dz = b.z; l.cos_outer = b.w;
+    l.cr = c.x; l.cg = c.y; l.cb = c.z; l.intensity = c.w;
+    l.type = d.y;
+    l.cos_inner = __uint_as_float(d.z);
+    float4 o = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    int st = kNeedsPrecise;
+    if (s.px[F_DEP][q] >= 0.0f) st = eval<false>(p, pb, l, o.x, o.y, o.z, fast_guard(p));
+    if (st == kNeedsPrecise) return precise_f16(gb, x0 + q % TW, y0 + q / TW, cam, lights, li);
+    o.w = __int_as_float(st);
+    return o;
+}
+
+// Records lit pairs for a verifier (hl_set_pair_log); a no-op without a log.
+__device__ __forceinline__ void log_pair(const PairLog& log, bool lit, uint32_t lane, uint32_t x, uint32_t y,
+                                         uint32_t W, uint32_t li) {
+    if (!log.pairs) return;
+    const uint32_t m = __ballot_sync(0xffffffffu, lit);
+    if (!m) return;
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(log.count, uint32_t(__popc(m)));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    const uint32_t slot = base + __popc(m & f16k::lanemask_lt());
+    if (lit && slot < log.capacity) log.pairs[slot] = make_uint2(y * W + x, li);
+}
+
+// Adds each lane's contribution (when lit) to pixel q's accumulators, lanes in order
+// where several hold the same pixel.
+__device__ __forceinline__ void accumulate(f16k::Smem& s, bool lit, uint32_t q, float cr, float cg, float cb) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t peers = __match_any_sync(0xffffffffu, lit ? q : (0x10000u | lane));
+    const uint32_t rank = __popc(peers & f16k::lanemask_lt());
+    const uint32_t rounds = __reduce_max_sync(0xffffffffu, lit ? rank + 1 : 0u);
+    for (uint32_t r = 0; r < rounds; ++r) {
+        if (lit && rank == r) {
+            kahan_add(s.acc[0][q], s.acc[3][q], cr);
+            kahan_add(s.acc[1][q], s.acc[4][q], cg);
+            kahan_add(s.acc[2][q], s.acc[5][q], cb);
+        }
+        __syncwarp();
+    }
+}
+
+// Evaluates the 32 queued pairs at ring positions head..head+31 and accumulates them.
+__device__ __noinline__ void flush32(f16k::Smem& s, const uint32_t* queue, uint32_t head, uint32_t lane,
+                                     const GpuCamera* cam, const GpuLight* lights, const GBufView& gb, uint32_t x0,
+                                     uint32_t y0, const PairLog& log) {
+    using namespace f16k;
+    const uint32_t e = queue[(head + lane) & (kQueue - 1)];
+    const uint32_t q = e >> 23, li = e & 0x7fffffu;
+    const float4 o = eval_pair(s, q, li, cam, lights, gb, x0, y0);
+    const bool lit = __float_as_int(o.w) == kLit;
+    log_pair(log, lit, lane, x0 + q % TW, y0 + q / TW, gb.width, li);
+    accumulate(s, lit, q, o.x, o.y, o.z);
+    __syncwarp();
+}
+
+template <uint32_t TARGET>
+__global__ void __launch_bounds__(f16k::kThreads, 3) shade_f16_kernel(
+    const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const __grid_constant__ GBufView gb,
+    const GpuLight* __restrict__ lights, uint32_t n_lights, const GridView grid,
+    const __grid_constant__ SliceTable tabz, const TargetView out, int* __restrict__ status,
+    const float4* __restrict__ cand, const __grid_constant__ PairLog log) {
+    using namespace f16k;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem& s = *reinterpret_cast<Smem*>(smem_raw);
+    const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t bx = blockIdx.x, by = blockIdx.y;
+    const uint32_t x0 = bx * TW, y0 = by * TH;
+    const hl_froxel_params& fp = grid.fp;
+
+    for (uint32_t b = t; b < uint32_t(kBins); b += kThreads) s.u.sort.hist[b] = 0;
+    for (uint32_t k = t; k <= fp.grid_z; k += kThreads) s.u.sort.tab[k] = tabz.z[k];
+    // froxel column of each pixel column and row of the tile (x * grid_x < 2^32 for
+    // viewports of at most 65536 pixels per side)
+    if (t < uint32_t(TW)) {
+        s.u.sort.col_of[t] = uint16_t(((x0 + t) * fp.grid_x) / fp.width);
+    } else if (t < uint32_t(TW + TH)) {
+        s.u.sort.row_of[t - TW] = uint16_t(((y0 + t - TW) * fp.grid_y) / fp.height);
+    } else if (t == uint32_t(TW + TH)) {
+        // the tile's froxel columns and the key layout: (slice, column) keys, slice-major,
+        // each split into 2^kshift depth sub-bins, within the 512 bins
+        const uint32_t xe = min(x0 + TW, gb.width) - 1, ye = min(y0 + TH, gb.height) - 1;
+        const uint32_t fx0 = (x0 * fp.grid_x) / fp.width, fy0 = (y0 * fp.grid_y) / fp.height;
+        const uint32_t ncx = (xe * fp.grid_x) / fp.width - fx0 + 1;
+        const uint32_t ncols = ncx * ((ye * fp.grid_y) / fp.height - fy0 + 1);
+        const bool by_column = ncols * fp.grid_z <= uint32_t(kBins);
+        const uint32_t nk = by_column ? ncols * fp.grid_z : fp.grid_z;
+        s.fx0 = fx0;
+        s.fy0 = fy0;
+        s.ncx = ncx;
+        s.ncols = ncols;
+        s.by_column = by_column;
+        s.kshift = 31u - __clz(uint32_t(kBins) / nk);
+    }
+#pragma unroll
+    for (int k = 0; k < PPT; ++k)
+        for (int c = 0; c < 6; ++c) s.acc[c][t + k * kThreads] = 0.0f;
+    if (t == 0) s.n_left = 0;
+    __syncthreads();
+
+    const float camx = cam->position_near[0], camy = cam->position_near[1], camz = cam->position_near[2];
+    const float W = float(gb.width), H = float(gb.height);
+    // slices are exponential from slice_near to tab[grid_z]: slice ~ log2(d / near) * scale
+    const float slice_inv_near = rcpn_(fp.slice_near);
+    const float slice_scale =
+        float(fp.grid_z) * rcpn_(__log2f(fmaxf(s.u.sort.tab[fp.grid_z] * slice_inv_near, 2.0f)));
+    const float nr = cam->position_near[3], fr = cam->forward_far[3];
+    const float nrfr = nr * fr, frmnr = fr - nr;
+    const uint32_t fx0 = s.fx0, fy0 = s.fy0, ncx = s.ncx, ncols = s.ncols, kshift = s.kshift;
+    const bool by_column = s.by_column != 0u;
+
+    // ---- 1. pixel set-up -------------------------------------------------------------
+    float rel[12], wrow[4];
+    camera_relative_rows(cam->inv_view_proj, camx, camy, camz, rel, wrow);
+    const float iW = rcp_(W), iH = rcp_(H);
+    bool valid[PPT];
+    uint32_t key[PPT], slot[PPT];
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+        const uint32_t i = t + k * kThreads;
+        const uint32_t x = x0 + i % TW, y = y0 + i / TW;
+        valid[k] = false;
+        key[k] = 0;
+        slot[k] = 0;
+        if (x < gb.width && y < gb.height) {
+            const uint2 a = *reinterpret_cast<const uint2*>(gb.plane[0] + gb.pitch[0] * y + 8ull * x);
+            const uint32_t on = *reinterpret_cast<const uint32_t*>(gb.plane[1] + gb.pitch[1] * y + 4ull * x);
+            const uint16_t mt = *reinterpret_cast<const uint16_t*>(gb.plane[2] + gb.pitch[2] * y + 2ull * x);
+            const float depth = *reinterpret_cast<const float*>(gb.plane[3] + gb.pitch[3] * y + 4ull * x);
+            valid[k] = depth < 1.0f;
+            if (valid[k]) {
+                const float ndx = fma_(float(2u * x + 1u), iW, -1.0f);
+                const float ndy = fma_(float(2u * y + 1u), -iH, 1.0f);
+                float Px, Py, Pz;
+                reconstruct_relative(rel, wrow, ndx, ndy, depth, Px, Py, Pz);
+                float nx, ny, nz;
+                oct_decode(f16k::h2f(on & 0xffffu), f16k::h2f(on >> 16), nx, ny, nz);
+                const float in = rsqrt_(fma_(nz, nz, fma_(ny, ny, nx * nx)));
+                // V = -P / |P| (camera at the origin), NdV as the fast path's set-up forms it
+                const float iv = rsqrt_(fma_(Pz, Pz, fma_(Py, Py, Px * Px)));
+                const float ndv = fmax_(fma_(nz, -Pz, fma_(ny, -Py, nx * -Px)) * in * iv, 0.0f);
+                const float ar = f16k::h2f(a.x & 0xffffu), ag = f16k::h2f(a.x >> 16), ab = f16k::h2f(a.y & 0xffffu);
+                const float rough = f16k::h2f(a.y >> 16), metal = f16k::h2f(mt);
+                s.px[F_PX][i] = Px; s.px[F_PY][i] = Py; s.px[F_PZ][i] = Pz;
+                s.px[F_NX][i] = nx * in; s.px[F_NY][i] = ny * in; s.px[F_NZ][i] = nz * in;
+                s.px[F_IP][i] = iv;
+                s.px[F_NDV][i] = ndv;
+                // grazing view: every pair of the pixel goes to the precise evaluation
+                s.px[F_DEP][i] = ndv < kFastMinNdV ? -depth : depth;
+                s.px[F_F0R][i] = fmin_(fmax_(metallic_f0(ar, metal), 0.0f), 0.999f);
+                s.px[F_F0G][i] = fmin_(fmax_(metallic_f0(ag, metal), 0.0f), 0.999f);
+                s.px[F_F0B][i] = fmin_(fmax_(metallic_f0(ab, metal), 0.0f), 0.999f);
+                s.px[F_DR][i] = ar * kInvPi; s.px[F_DG][i] = ag * kInvPi; s.px[F_DB][i] = ab * kInvPi;
+                const float ra = rough * rough, r1 = rough + 1.0f;
+                const float kk = (r1 * r1) * 0.125f;
+                s.px[F_A2][i] = ra * ra;
+                s.px[F_K][i] = kk;
+                s.px[F_GV][i] = divn_(ndv, fma_(ndv, 1.0f - kk, kk + 0.0001f));
+                s.px[F_METAL][i] = metal;
+                // own froxel: column of (x, y), slice of the linear view depth (the lists
+                // are conservative by 2^-10 of the slice depth, so the slice only needs
+                // the depth to a few ulp)
+                const float dv = nrfr * rcpn_(fma_(-depth, frmnr, fr));
+                const float sf = __log2f(dv * slice_inv_near) * slice_scale;
+                uint32_t sl = uint32_t(min(max(int(sf), 0), int(fp.grid_z) - 1));
+                while (sl + 1 < fp.grid_z && s.u.sort.tab[sl + 1] <= dv) ++sl;
+                while (sl > 0 && s.u.sort.tab[sl] > dv) --sl;
+                const uint32_t fx = s.u.sort.col_of[x - x0];
+                const uint32_t fy = s.u.sort.row_of[y - y0];
+                s.w.walk.fidx[i] = (fy * fp.grid_x + fx) * fp.grid_z + sl;
+                // depth sub-bin: the position inside the slice on its logarithmic scale
+                const uint32_t nsub = 1u << kshift;
+                const uint32_t sub = uint32_t(min(max(int((sf - float(sl)) * float(nsub)), 0), int(nsub) - 1));
+                const uint32_t kb = by_column ? sl * ncols + (fy - fy0) * ncx + (fx - fx0) : sl;
+                key[k] = (kb << kshift) | sub;
+                slot[k] = atomicAdd(&s.u.sort.hist[key[k]], 1u);
+            }
+        }
+    }
+    __syncthreads();
+    {   // exclusive scan of the key histogram, two bins per thread
+        const uint32_t a = s.u.sort.hist[2 * t], b = s.u.sort.hist[2 * t + 1];
+        uint32_t v = a + b;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t n = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= uint32_t(o)) v += n;
+        }
+        if (lane == 31) s.warp_tot[warp] = v;
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t wt = s.warp_tot[w];
+            before += (uint32_t(w) < warp) ? wt : 0u;
+            total += wt;
+        }
+        const uint32_t excl = before + v - (a + b);
+        __syncthreads();
+        s.u.sort.hist[2 * t] = excl;
+        s.u.sort.hist[2 * t + 1] = excl + a;
+        if (t == 0) {
+            s.n_valid = total;
+            s.next_group = 0;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < PPT; ++k)
+        if (valid[k]) s.w.walk.order[s.u.sort.hist[key[k]] + slot[k]] = uint16_t(t + k * kThreads);
+
+    {   // ask L2 for the G-buffer rows of the tile one wave (3 CTAs x SMs) further on:
+        // 32 x 128 B of plane 0 (8 B/px), 16 x 128 B of planes 1 and 3, 16 x 64 B of plane 2
+        uint32_t nsm;
+        asm("mov.u32 %0, %%nsmid;" : "=r"(nsm));
+        const uint32_t next = by * gridDim.x + bx + 3u * nsm;
+        if (t < 80u && next < gridDim.x * gridDim.y) {
+            const uint32_t nx0 = (next % gridDim.x) * TW, ny0 = (next / gridDim.x) * TH;
+            const uint32_t pl = t < 32u ? 0u : t < 48u ? 1u : t < 64u ? 2u : 3u;
+            const uint32_t row = t < 32u ? t >> 1 : (t - 16u) & 15u;
+            const uint32_t bpp = pl == 0u ? 8u : pl == 2u ? 2u : 4u;
+            const uint32_t yy = ny0 + row;
+            if (yy < gb.height) {
+                const uint32_t b0 = nx0 * bpp + (t < 32u ? (t & 1u) * 128u : 0u);
+                const uint32_t bend = gb.width * bpp - 1u;
+                gbuf::prefetch_l2(gb.plane[pl] + gb.pitch[pl] * yy + min(b0, bend));
+            }
+        }
+    }
+    pdl_wait();  // the lists and the candidate table are written
+    __syncthreads();
+
+    // ---- 2-4. groups of 32 sorted pixels -------------------------------------------------
+    const uint32_t n_valid = s.n_valid;
+    uint32_t* queue = s.u.queue[warp];
+    uint32_t head = 0, qlen = 0;  // ring position of the oldest pending pair, pending pairs
+#pragma unroll 1
+    for (;;) {
+        // warps take groups as they finish, last group first: the far slices sort last
+        // and hold the longest lists, so the long work starts early
+        uint32_t g = 0;
+        if (lane == 0) g = atomicAdd(&s.next_group, 1u);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= uint32_t(NG)) break;
+        g = uint32_t(NG - 1) - g;
+        if (g * 32u >= n_valid) continue;  // empty group
+        const uint32_t gs = g * 32 + lane;
+        const bool own = gs < n_valid;
+        const uint32_t i = own ? s.w.walk.order[gs] : 0u;
+        float px = 0, py = 0, pz = 0, nx = 0, ny = 0, nz = 0;
+        uint32_t f = 0xffffffffu, lb = 0, le = 0;
+        if (own) {
+            px = s.px[F_PX][i]; py = s.px[F_PY][i]; pz = s.px[F_PZ][i];
+            nx = s.px[F_NX][i]; ny = s.px[F_NY][i]; nz = s.px[F_NZ][i];
+            f = s.w.walk.fidx[i];
+            lb = __ldg(grid.counts + f);
+            le = __ldg(grid.counts + f + 1);
+            if (!(lb <= le && le <= grid.lists_capacity)) {
+                raise_status(status, HL_ERR_DEVICE_BOUNDS);
+                le = lb;
+            }
+        }
+        // |N.t| within |P| 2^-20 of zero is left to the exact NdL cut
+        const float slack = fma_(pz, pz, fma_(py, py, px * px)) * (1.0f / 1099511627776.0f);
+#pragma unroll 1
+        for (uint32_t c0 = 0;; c0 += 32) {
+            const bool act = own && lb + c0 < le;
+            uint32_t pending = __ballot_sync(0xffffffffu, act);
+            if (!pending) break;
+            // A: per froxel of the group, the 32 list entries from c0 on, culled against the
+            // bounding box of the group's pixels in that froxel
+            uint32_t smask = 0;
+            while (pending) {
+                const uint32_t leader = __ffs(pending) - 1;
+                const uint32_t fk = __shfl_sync(0xffffffffu, f, leader);
+                const bool mine = act && f == fk;
+                pending &= ~__ballot_sync(0xffffffffu, mine);
+                const float b0x = o2f(__reduce_min_sync(0xffffffffu, mine ? f2o(px) : 0x7fffffff));
+                const float b0y = o2f(__reduce_min_sync(0xffffffffu, mine ? f2o(py) : 0x7fffffff));
+                const float b0z = o2f(__reduce_min_sync(0xffffffffu, mine ? f2o(pz) : 0x7fffffff));
+                const float b1x = o2f(__reduce_max_sync(0xffffffffu, mine ? f2o(px) : int(0x80000000)));
+                const float b1y = o2f(__reduce_max_sync(0xffffffffu, mine ? f2o(py) : int(0x80000000)));
+                const float b1z = o2f(__reduce_max_sync(0xffffffffu, mine ? f2o(pz) : int(0x80000000)));
+                const uint32_t j = __shfl_sync(0xffffffffu, lb, leader) + c0 + lane;
+                const uint32_t je = __shfl_sync(0xffffffffu, le, leader);
+                const uint32_t lj = j < je ? __ldg(grid.lists + j) : 0xffffffffu;
+                const bool ok = lj < n_lights;
+                if (j < je && !ok) raise_status(status, HL_ERR_DEVICE_BOUNDS);
+                const float4 c = ok ? __ldg(cand + lj) : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+                // the per-pixel test's operations on the box-clamped differences: for a pixel
+                // in the box each |difference| rounds no smaller, so a light the box rejects
+                // fails the range test at every pixel of the box
+                const float dx = fmax_(fmax_(b0x - c.x, c.x - b1x), 0.0f);
+                const float dy = fmax_(fmax_(b0y - c.y, c.y - b1y), 0.0f);
+                const float dz = fmax_(fmax_(b0z - c.z, c.z - b1z), 0.0f);
+                const bool keep = ok && (c.w < 0.0f || fma_(dz, dz, fma_(dy, dy, dx * dx)) <= c.w);
+                const uint32_t m = __ballot_sync(0xffffffffu, keep);
+                if (mine) smask = m;
+            }
+            // B: every lane walks the survivors of its own froxel, in list order
+            const uint32_t cb = lb + c0;
+#pragma unroll 1
+            while (__any_sync(0xffffffffu, smask != 0u)) {
+                bool pass = false;
+                uint32_t li = 0;
+                if (smask) {
+                    const uint32_t bit = __ffs(smask) - 1;
+                    smask &= smask - 1;
+                    li = __ldg(grid.lists + cb + bit);
+                    const float4 a = __ldg(cand + li);
+                    pass = a.w < 0.0f || candidate(px, py, pz, 0.0f, 0.0f, 0.0f, nx, ny, nz, a.x, a.y, a.z, a.w,
+                                                   slack, true);
+                }
+                const uint32_t pm = __ballot_sync(0xffffffffu, pass);
+                if (pass) queue[(head + qlen + __popc(pm & lanemask_lt())) & (kQueue - 1)] = (i << 23) | li;
+                qlen += __popc(pm);
+                __syncwarp();
+                if (qlen >= 32) {
+                    flush32(s, queue, head, lane, cam, lights, gb, x0, y0, log);
+                    head += 32;
+                    qlen -= 32;
+                }
+            }
+        }
+    }
+
+    // ---- the pairs left in the queues: evaluated together, accumulated by their warp ------
+    __syncthreads();  // every warp has walked: the walk's arrays are free
+    uint32_t base = 0;
+    if (lane == 0 && qlen > 0) base = atomicAdd(&s.n_left, qlen);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (lane < qlen) s.w.tail.left[base + lane] = queue[(head + lane) & (kQueue - 1)];
+    __syncthreads();
+    const uint32_t n_left = s.n_left;
+    for (uint32_t c0 = warp * 32; c0 < n_left; c0 += kThreads) {
+        const bool act = c0 + lane < n_left;
+        const uint32_t e = act ? s.w.tail.left[c0 + lane] : 0u;
+        const uint32_t q = e >> 23, li = e & 0x7fffffu;
+        float4 o = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(kCut));
+        if (act) o = eval_pair(s, q, li, cam, lights, gb, x0, y0);
+        log_pair(log, act && __float_as_int(o.w) == kLit, lane, x0 + q % TW, y0 + q / TW, gb.width, li);
+        if (act) s.w.tail.res[c0 + lane] = o;
+    }
+    __syncthreads();
+    if (qlen > 0) {
+        const bool act = lane < qlen;
+        const uint32_t e = act ? s.w.tail.left[base + lane] : 0u;
+        const float4 o = act ? s.w.tail.res[base + lane] : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(kCut));
+        accumulate(s, act && __float_as_int(o.w) == kLit, e >> 23, o.x, o.y, o.z);
+    }
+
+    // ---- 5. output -----------------------------------------------------------------------
+    __syncthreads();
+    const uint32_t debug_mode = glb->debug_mode;
+    if (t == 0 && (glb->has_rc_gi != 0u || debug_mode == 10u || debug_mode == 11u))
+        raise_status(status, HL_ERR_NOT_SUPPORTED);
+    const float amb = glb->ambient_intensity;
+    const float skr = glb->ambient_color[0] * amb, skg = glb->ambient_color[1] * amb,
+                skb = glb->ambient_color[2] * amb;
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+        const uint32_t i = t + k * kThreads;
+        const uint32_t x = x0 + i % TW, y = y0 + i / TW;
+        if (!valid[k]) continue;
+        // albedo read again from the G-buffer (an L2 hit: the tile was read at set-up)
+        const uint2 alb = *reinterpret_cast<const uint2*>(gb.plane[0] + gb.pitch[0] * y + 8ull * x);
+        const float ar = f16k::h2f(alb.x & 0xffffu), ag = f16k::h2f(alb.x >> 16), ab = f16k::h2f(alb.y & 0xffffu);
+        const float ny = s.px[F_NY][i];
+        const float ht = fma_(ny, 0.5f, 0.5f);
+        // hemisphere ambient (deferred_lighting.wgsl:1196-1199) times ao (1, white SSAO)
+        const float hr = fma_(skr, ht, skr * 0.15f * (1.0f - ht)) * ar;
+        const float hg = fma_(skg, ht, skg * 0.15f * (1.0f - ht)) * ag;
+        const float hb = fma_(skb, ht, skb * 0.15f * (1.0f - ht)) * ab;
+        float4 c;
+        c.x = s.acc[0][i] + hr;
+        c.y = s.acc[1][i] + hg;
+        c.z = s.acc[2][i] + hb;
+        c.w = 1.0f;
+        if (debug_mode == 1u || debug_mode == 2u || debug_mode == 4u || debug_mode == 20u || debug_mode == 21u) {
+            c = make_float4(ar, ag, ab, 1.0f);
+        } else if (debug_mode == 5u) {
+            c = make_float4(fma_(s.px[F_NX][i], 0.5f, 0.5f), fma_(ny, 0.5f, 0.5f), fma_(s.px[F_NZ][i], 0.5f, 0.5f),
+                            1.0f);
+        }
+        unsigned char* row = out.data + out.pitch * y;
+        if (TARGET == HL_TARGET_RGBA32F) {
+            reinterpret_cast<float4*>(row)[x] = c;
+        } else {
+            const __half2 lo = __floats2half2_rn(c.x, c.y), hi = __floats2half2_rn(c.z, c.w);
+            uint2 v;
+            v.x = *reinterpret_cast<const uint32_t*>(&lo);
+            v.y = *reinterpret_cast<const uint32_t*>(&hi);
+            reinterpret_cast<uint2*>(row)[x] = v;
+        }
+    }
+}
+
+template <uint32_t TARGET>
+cudaError_t launch_target(const void* camera, const void* globals, const GBufView& gb, const void* lights, uint32_t n,
+                          const GridView& grid, const SliceTable& tab, const TargetView& out, int* status,
+                          float4* cand, const PairLog& log, cudaStream_t stream) {
+    auto kern = shade_f16_kernel<TARGET>;
+    const int smem = int(sizeof(f16k::Smem));
+    static unsigned long long attr_devices = 0;  // devices on which the smem limit is raised
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 64 && !(attr_devices & (1ull << dev))) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr_devices |= 1ull << dev;
+    }
+    if (n > 0) {
+        cudaError_t e = launch_prep_cand(camera, lights, n, true, cand, stream);
+        if (e != cudaSuccess) return e;
+    }
+    const dim3 g((gb.width + f16k::TW - 1) / f16k::TW, (gb.height + f16k::TH - 1) / f16k::TH);
+    return launch_pdl(kern, g, dim3(f16k::kThreads), smem, stream, static_cast<const GpuCamera*>(camera),
+                      static_cast<const DeferredGlobals*>(globals), gb, static_cast<const GpuLight*>(lights), n, grid,
+                      tab, out, status, static_cast<const float4*>(cand), log);
+}
+
+}  // namespace
+
+cudaError_t launch_shade_f16(uint32_t target_format, const void* camera, const void* globals, const GBufView& gb,
+                             const void* lights, uint32_t n_lights, const GridView& grid, const SliceTable& tab,
+                             const TargetView& out, int* status, float4* cand, const PairLog& log,
+                             cudaStream_t stream) {
+    if (target_format == HL_TARGET_RGBA16F)
+        return launch_target<HL_TARGET_RGBA16F>(camera, globals, gb, lights, n_lights, grid, tab, out, status, cand,
+                                                 log, stream);
+    return launch_target<HL_TARGET_RGBA32F>(camera, globals, gb, lights, n_lights, grid, tab, out, status, cand, log,
+                                             stream);
+}
+
+}  // namespace hl

@@ -133,7 +133,7 @@ EXPORTS = [
     "hl_tile_count", "hl_bin_tiles_ref", "hl_froxel_slice_table", "hl_bin_froxels", "hl_shade", "hl_shade_stats",
     "hl_shade_adjoint", "hl_batch_plan_create", "hl_batch_execute", "hl_batch_plan_view_grid",
     "hl_batch_plan_destroy", "hl_probe_fp32_peak", "hl_bin_froxels_noalloc", "hl_shade_fragments",
-    "hl_write_gbuffer", "hl_shade_shadowed", "hl_shade_ex", "hl_shade_reflections",
+    "hl_write_gbuffer", "hl_shade_shadowed", "hl_shade_ex", "hl_shade_reflections", "hl_set_pair_log",
 ]
 
 _lock = threading.Lock()
@@ -186,6 +186,8 @@ def _bind(l):
     l.hl_shade.restype = i32
     l.hl_shade_stats.argtypes = [vp, vp, vp, P(GBuffer), vp, u32, P(LightGrid), vp, vp]
     l.hl_shade_stats.restype = i32
+    l.hl_set_pair_log.argtypes = [vp, vp, u32, vp]
+    l.hl_set_pair_log.restype = i32
     l.hl_shade_adjoint.argtypes = [vp, vp, vp, P(GBuffer), vp, u32, P(LightGrid), vp, C.c_uint64, vp, vp, vp]
     l.hl_shade_adjoint.restype = i32
     l.hl_batch_plan_create.argtypes = [vp, P(View), u32, vp, u32, vp, P(BatchConfig), P(vp), vp]
@@ -358,6 +360,16 @@ class Context:
     def shade_stats(self, camera, globals_, gbuffer: GBuffer, lights, n_lights, grid: LightGrid, counts, stream=None):
         self._check(self._l.hl_shade_stats(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer), _ptr(lights),
                                            n_lights, C.byref(grid), _ptr(counts), _stream(stream)), "hl_shade_stats")
+
+    def set_pair_log(self, pairs=None, count=None):
+        """Record the (pixel, light) pairs later shading launches light into ``pairs``
+        (int32 device tensor (capacity, 2)) and ``count`` (int32 device tensor, zeroed by
+        the caller); ``pairs=None`` stops recording."""
+        if pairs is None:
+            self._check(self._l.hl_set_pair_log(self._h, None, 0, None), "hl_set_pair_log")
+        else:
+            self._check(self._l.hl_set_pair_log(self._h, _ptr(pairs), int(pairs.shape[0]), _ptr(count)),
+                        "hl_set_pair_log")
 
     def shade_adjoint(self, camera, globals_, gbuffer: GBuffer, lights, n_lights, grid: LightGrid, d_radiance,
                       d_radiance_pitch, d_lights, d_pixels, stream=None):

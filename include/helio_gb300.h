@@ -365,6 +365,18 @@ hl_status hl_shade_stats(hl_ctx* ctx, const void* camera, const void* globals, c
                          const void* lights, uint32_t n_lights, const hl_light_grid* grid,
                          uint32_t* counts, void* stream);
 
+/* Records which (pixel, light) pairs the context's later shading launches (hl_shade,
+ * hl_shade_shadowed, hl_shade_ex) light, i.e. pass the range, NdL and radiance cuts of
+ * pbr_direct_light (deferred_lighting.wgsl:725,779,781) and are added to the pixel. The
+ * launches are the ordinary ones; only this record is added. For every lit pair the
+ * kernel increments *count and, when the previous value k < capacity, writes
+ * pairs[2k] = y*width + x and pairs[2k+1] = the light index, in no particular order.
+ * pairs and count are device memory the caller owns and zeroes; pairs == NULL stops
+ * recording. A verifier re-evaluates the FP64 reference formula with these branch
+ * decisions, so that pixels whose f32 and f64 evaluations fall on different sides of a
+ * cut are checked rather than skipped. No reference counterpart. */
+hl_status hl_set_pair_log(hl_ctx* ctx, uint32_t* pairs, uint32_t capacity, uint32_t* count);
+
 /* ---------------------------------------------------------------------------------
  * Adjoint of the direct-lighting term (no reference counterpart)
  * -------------------------------------------------------------------------------*/
