@@ -65,6 +65,8 @@ def _bind(l):
     l.oracle_shade_f32.argtypes = shade_args
     l.oracle_shade_ex_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, vp, vp, f64p,
                                       u32p, u32, u32, vp]
+    l.oracle_shade_forced_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, vp, u32p,
+                                          u32p, f64p, u32p, u32, u32, vp]
     l.oracle_reflections_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, C.c_uint64, vp, C.c_uint64, vp,
                                          C.c_uint64, vp, f64p, vp]
     l.oracle_shade_adjoint_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, f64p, f64p, f64p]
@@ -220,6 +222,62 @@ def shade_ex(camera_rec, globals_rec, gb, lights, grid, shadows=None, rc=None, r
                               _ptr(desc) if desc is not None else None, _ptr(rcd) if rcd is not None else None,
                               _ptr(out), _ptr(pc) if pc is not None else None, r0, r1, _ptr(bounds))
     return out, pc, bool(bounds[0])
+
+
+def forced_csr(pairs, n_pixels):
+    """(offsets[n_pixels+1], lights) of (pixel, light) pairs, each pixel's lights
+    ascending and without duplicates."""
+    pr = np.asarray(pairs, np.uint64).reshape(-1, 2)
+    key = np.unique((pr[:, 0] << np.uint64(32)) | pr[:, 1])
+    pix = (key >> np.uint64(32)).astype(np.int64)
+    if pix.size and pix.max() >= n_pixels:
+        raise ValueError("pair pixel index beyond the image")
+    offsets = np.zeros(n_pixels + 1, np.uint32)
+    np.cumsum(np.bincount(pix, minlength=n_pixels), out=offsets[1:])
+    return offsets, (key & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+
+
+def _shadow_desc(shadows):
+    from helio_gb300 import layouts as L
+
+    dyn = np.ascontiguousarray(shadows["dynamic"], np.float32)
+    sta = np.ascontiguousarray(shadows["static"], np.float32)
+    mats = np.ascontiguousarray(shadows["matrices"], np.float32)
+    cfg = np.ascontiguousarray(shadows["config"])
+    desc = np.zeros(1, L.SHADOW_MAPS)
+    desc["dynamic_atlas"], desc["static_atlas"] = dyn.ctypes.data, sta.ctypes.data
+    desc["matrices"], desc["config"] = mats.ctypes.data, cfg.ctypes.data
+    desc["size"], desc["layers"] = dyn.shape[1], dyn.shape[0]
+    desc["max_shadow_lights"] = shadows["max_lights"]
+    return desc, (dyn, sta, mats, cfg)
+
+
+def shade_forced(camera_rec, globals_rec, gb, lights, grid, lit_pairs, shadows=None, rows=None):
+    """``shade`` (f64) with another evaluation's branch decisions: ``lit_pairs`` (K, 2)
+    are the (y * W + x, light) pairs that evaluation lit (as hl_set_pair_log records
+    them). Those pairs are evaluated as lit whatever the f64 cuts decide, every other
+    listed pair contributes nothing, so the radiance is comparable at every pixel,
+    including those where f32 and f64 fall on different sides of a cut. Returns
+    (radiance, flips, unlisted): per pixel the number of listed pairs whose f64 decision
+    differs, and of lit pairs whose light is not in the pixel's list (must be 0)."""
+    W, H = gb.width, gb.height
+    r0, r1 = (0, H) if rows is None else rows
+    out = np.full((H, W, 4), np.nan, np.float64)
+    fl = np.zeros((H, W), np.uint32)
+    arrs, ptrs, pitch = _planes(gb)
+    kind, lists, counts, params = _grid_args(grid)
+    lts = np.ascontiguousarray(lights)
+    off, fls = forced_csr(lit_pairs, W * H)
+    if fls.size == 0:
+        fls = np.zeros(1, np.uint32)
+    desc, keep = _shadow_desc(shadows) if shadows is not None else (None, None)
+    bounds = np.zeros(1, np.int32)
+    lib().oracle_shade_forced_f64(_ptr(np.ascontiguousarray(camera_rec)), _ptr(np.ascontiguousarray(globals_rec)),
+                                  gb.layout, W, H, ptrs, pitch, _ptr(lts) if len(lts) else None, len(lts), kind,
+                                  _ptr(lists), _ptr(counts), _ptr(params) if params is not None else None,
+                                  _ptr(desc) if desc is not None else None, _ptr(off), _ptr(fls), _ptr(out), _ptr(fl),
+                                  r0, r1, _ptr(bounds))
+    return out, (fl & 0xFFFF).astype(np.uint32), (fl >> 16).astype(np.uint32)
 
 
 def _rc_desc(rc):

@@ -504,10 +504,14 @@ template <class T> struct PairStats {
 };
 
 // pbr_direct_light, non-anisotropic, no SSS, sf = 1. Returns true when the full
-// BRDF was evaluated (passed the NdL and radiance cuts).
+// BRDF was evaluated (passed the NdL and radiance cuts). force: the pair is evaluated
+// as lit whatever the cuts decide (range, NdL == 0, radiance < 0.002: :725, :779,
+// :781), i.e. with another evaluation's branch decisions; beyond the range the falloff
+// max(0, 1 - (d/r)^4) and below the horizon max(N.L, 0) make the value 0, so only the
+// radiance cut changes the result.
 template <class T>
 bool pbr_direct_light(const RawLight& l, V3<T> P, V3<T> N, V3<T> V, V3<T> F0, V3<T> albedo, T rough,
-                      T metal, V3<T>& out, bool radiance_cut = true) {
+                      T metal, V3<T>& out, bool radiance_cut = true, bool force = false) {
     V3<T> L, radiance;
     const V3<T> color = v3<T>(l.color[0], l.color[1], l.color[2]);
     const T intensity = T(l.intensity);
@@ -517,7 +521,7 @@ bool pbr_direct_light(const RawLight& l, V3<T> P, V3<T> N, V3<T> V, V3<T> F0, V3
     } else {
         V3<T> to_light = v3<T>(l.pos[0], l.pos[1], l.pos[2]) - P;
         T dist = tsqrt(dot(to_light, to_light));
-        if (dist > T(l.range)) { out = v3<T>(0, 0, 0); return false; }
+        if (dist > T(l.range) && !force) { out = v3<T>(0, 0, 0); return false; }
         L = to_light / dist;
         T atten = T(1) / (dist * dist + T(0.0001));
         T nd = dist / T(l.range);
@@ -529,9 +533,9 @@ bool pbr_direct_light(const RawLight& l, V3<T> P, V3<T> N, V3<T> V, V3<T> F0, V3
         radiance = (color * intensity) * atten;
     }
     T NdL = tmax(dot(N, L), T(0));
-    if (NdL == T(0)) { out = v3<T>(0, 0, 0); return false; }
+    if (NdL == T(0) && !force) { out = v3<T>(0, 0, 0); return false; }
     const T cut = T(0.002);
-    if (radiance_cut && radiance.x < cut && radiance.y < cut && radiance.z < cut) {
+    if (radiance_cut && !force && radiance.x < cut && radiance.y < cut && radiance.z < cut) {
         out = v3<T>(0, 0, 0);
         return false;
     }
@@ -591,7 +595,8 @@ void shade_impl(const void* camera, const void* globals, const GBufferDesc& g, c
                 uint32_t n_lights, const GridDesc& grid, double* out_rgba /* W*H*4 */,
                 uint32_t* pair_counts /* W*H*3 or null */, uint32_t row0, uint32_t row1,
                 const shadow_oracle::ShadowDesc* shadows = nullptr, int* shadow_bounds = nullptr,
-                const rc_oracle::RcDesc* rc = nullptr) {
+                const rc_oracle::RcDesc* rc = nullptr, const uint32_t* forced_off = nullptr,
+                const uint32_t* forced_lights = nullptr, uint32_t* flips = nullptr) {
     Cam<T> c = load_camera<T>(camera);
     RawGlobals gl;
     std::memcpy(&gl, globals, sizeof gl);
@@ -641,20 +646,38 @@ void shade_impl(const void* camera, const void* globals, const GBufferDesc& g, c
                 list = grid.lists + grid.counts[f];
             }
             V3<T> Lo = v3<T>(0, 0, 0);
-            uint32_t n_range = 0, n_full = 0;
+            uint32_t n_range = 0, n_full = 0, n_flip = 0;
+            // forced branches: the ascending lights another evaluation lit at this pixel
+            const bool forced = forced_off != nullptr;
+            const uint32_t* fb = forced ? forced_lights + forced_off[pix] : nullptr;
+            const uint32_t* fe = forced ? forced_lights + forced_off[pix + 1] : nullptr;
             for (uint32_t j = 0; j < count; ++j) {
                 const uint32_t idx = list[j];
                 if (idx >= n_lights) continue;
                 const RawLight& l = L[idx];
+                bool forced_lit = false;
+                if (forced) {
+                    while (fb < fe && *fb < idx) ++fb;  // lit lights missing from the list: counted below
+                    forced_lit = fb < fe && *fb == idx;
+                    if (forced_lit) ++fb;
+                }
+                bool in_range = true;
                 if (l.type != 0u) {
                     V3<T> dl = v3<T>(l.pos[0], l.pos[1], l.pos[2]) - P;
                     T dist = tsqrt(dot(dl, dl));
-                    if (dist > T(l.range)) continue;
+                    in_range = !(dist > T(l.range));
                 }
-                ++n_range;
-                V3<T> contrib;
-                if (pbr_direct_light(l, P, N, V, F0, s.albedo, s.rough, s.metal, contrib)) {
-                    ++n_full;
+                if (!in_range && !forced_lit) continue;
+                if (in_range) ++n_range;
+                V3<T> contrib = v3<T>(0, 0, 0);
+                const bool own = in_range && pbr_direct_light(l, P, N, V, F0, s.albedo, s.rough, s.metal, contrib);
+                if (forced) {
+                    if (own != forced_lit) ++n_flip;
+                    if (!forced_lit) contrib = v3<T>(0, 0, 0);
+                    else if (!own) pbr_direct_light(l, P, N, V, F0, s.albedo, s.rough, s.metal, contrib, true, true);
+                }
+                if (forced ? forced_lit : own) {
+                    if (own) ++n_full;
                     // the pair's shadow factor sf (deferred_lighting.wgsl:1136-1141, 819)
                     if (shadows && idx < shadows->max_lights && l.shadow_index != shadow_oracle::kNoShadow) {
                         const double sf = shadow_oracle::shadow_factor<T>(
@@ -701,6 +724,20 @@ void shade_impl(const void* camera, const void* globals, const GBufferDesc& g, c
                 pair_counts[pix * 3] = count;
                 pair_counts[pix * 3 + 1] = n_range;
                 pair_counts[pix * 3 + 2] = n_full;
+            }
+            if (flips) {
+                // the forced pairs the list walk never reached: lit lights absent from the list
+                uint32_t unlisted = 0;
+                if (forced) {
+                    const uint32_t* a = forced_lights + forced_off[pix];
+                    const uint32_t* b = forced_lights + forced_off[pix + 1];
+                    for (; a < b; ++a) {
+                        bool found = false;
+                        for (uint32_t j = 0; j < count && !found; ++j) found = list[j] == *a;
+                        unlisted += found ? 0u : 1u;
+                    }
+                }
+                flips[pix] = n_flip | (unlisted << 16);
             }
         }
     }
@@ -1188,6 +1225,24 @@ void oracle_shade_f64(const void* cam, const void* globals, uint32_t layout, uin
     GBufferDesc g = make_gbuf(layout, W, H, planes, pitch);
     GridDesc gr = make_grid(grid_kind, lists, counts, froxel);
     shade_impl<double>(cam, globals, g, lights, n, gr, out_rgba, pair_counts, row0, row1);
+}
+
+// oracle_shade_f64 with forced branch decisions: forced_off[W*H+1] / forced_lights (CSR,
+// each pixel's lights ascending) name the (pixel, light) pairs another evaluation lit;
+// those are evaluated as lit whatever the f64 cuts decide and every other pair
+// contributes nothing. flips[W*H] = pairs whose f64 decision differs, plus 65536 x
+// lit pairs whose light is not in the pixel's list.
+void oracle_shade_forced_f64(const void* cam, const void* globals, uint32_t layout, uint32_t W, uint32_t H,
+                             const void* const* planes, const uint64_t* pitch, const void* lights, uint32_t n,
+                             uint32_t grid_kind, const uint32_t* lists, const uint32_t* counts, const void* froxel,
+                             const void* shadows, const uint32_t* forced_off, const uint32_t* forced_lights,
+                             double* out_rgba, uint32_t* flips, uint32_t row0, uint32_t row1, int* bounds) {
+    GBufferDesc g = make_gbuf(layout, W, H, planes, pitch);
+    GridDesc gr = make_grid(grid_kind, lists, counts, froxel);
+    *bounds = 0;
+    shade_impl<double>(cam, globals, g, lights, n, gr, out_rgba, nullptr, row0, row1,
+                       static_cast<const shadow_oracle::ShadowDesc*>(shadows), bounds, nullptr, forced_off,
+                       forced_lights, flips);
 }
 
 // oracle_shade_f64 with the pass's optional bindings: shadows (an hl_shadow_maps whose
