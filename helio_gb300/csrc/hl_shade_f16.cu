@@ -45,23 +45,21 @@ constexpr int kQueue = 64;           // per-warp pair ring: at most 31 + 32 pend
 constexpr int kBins = 512;           // keys of the pixel sort
 static_assert(31 + 32 <= kQueue, "pair ring too small");
 
-// Pixel record fields (structure of arrays).
-enum Field : int {
-    F_PX, F_PY, F_PZ,   // camera-relative position (f32)
-    F_NX, F_NY, F_NZ,   // unit normal
-    F_IP,               // 1 / |P|: V = -P / |P|
-    F_NDV,              // max(N.V, 0)
-    F_DEP,              // NDC depth; negative: seen at a grazing angle, every pair precise
-    F_F0R, F_F0G, F_F0B,
-    F_DR, F_DG, F_DB,   // albedo / pi
-    F_A2, F_K, F_GV,    // roughness^4, (r+1)^2/8, Schlick-GGX of the view
-    F_METAL,
-    F_COUNT
+// Pixel record: five float4 per pixel, so that a lane evaluating a pair of a random
+// pixel reads it with five 16-byte loads (an odd stride of float4: the eight lanes of a
+// shared-memory wavefront that store consecutive pixels hit distinct banks).
+struct Rec {
+    float4 p;   // camera-relative position (f32), 1 / |P| (V = -P / |P|)
+    float4 n;   // unit normal, max(N.V, 0)
+    float4 f0;  // F0 rgb, NDC depth (negative: seen at a grazing angle, every pair precise)
+    float4 d;   // albedo / pi rgb, metallic
+    float4 b;   // roughness^4, (r+1)^2/8, Schlick-GGX of the view, unused
 };
+static_assert(sizeof(Rec) == 80, "pixel record");
 
 struct Smem {
-    float px[F_COUNT][NPX];
-    float acc[6][NPX];  // Kahan (sum, compensation) x RGB
+    Rec rec[NPX];
+    float4 acc[2][NPX];  // Kahan sum and compensation (rgb)
     union {
         struct {
             uint32_t hist[kBins];
@@ -137,23 +135,24 @@ __device__ __noinline__ float4 precise_f16(const GBufView& gb, uint32_t x, uint3
 __device__ __forceinline__ float4 eval_pair(const f16k::Smem& s, uint32_t q, uint32_t li, const GpuCamera* cam,
                                             const GpuLight* lights, const GBufView& gb, uint32_t x0, uint32_t y0) {
     using namespace f16k;
+    const Rec& r = s.rec[q];
+    const float4 r0 = r.p, r1 = r.n, r2 = r.f0, r3 = r.d, r4 = r.b;
     Pixel p;
-    p.Px = s.px[F_PX][q]; p.Py = s.px[F_PY][q]; p.Pz = s.px[F_PZ][q];
+    p.Px = r0.x; p.Py = r0.y; p.Pz = r0.z;
     p.Plx = p.Ply = p.Plz = 0.0f;
-    p.Nx = s.px[F_NX][q]; p.Ny = s.px[F_NY][q]; p.Nz = s.px[F_NZ][q];
-    const float ip = s.px[F_IP][q];
-    p.Vx = -p.Px * ip;
-    p.Vy = -p.Py * ip;
-    p.Vz = -p.Pz * ip;
-    p.NdV = s.px[F_NDV][q];
-    p.f0r = s.px[F_F0R][q]; p.f0g = s.px[F_F0G][q]; p.f0b = s.px[F_F0B][q];
-    p.dr = s.px[F_DR][q]; p.dg = s.px[F_DG][q]; p.db = s.px[F_DB][q];
+    p.Nx = r1.x; p.Ny = r1.y; p.Nz = r1.z;
+    p.Vx = -p.Px * r0.w;
+    p.Vy = -p.Py * r0.w;
+    p.Vz = -p.Pz * r0.w;
+    p.NdV = r1.w;
+    p.f0r = r2.x; p.f0g = r2.y; p.f0b = r2.z;
+    p.dr = r3.x; p.dg = r3.y; p.db = r3.z;
     PixelBrdf pb;
-    pb.a2 = s.px[F_A2][q];
-    pb.k = s.px[F_K][q];
+    pb.a2 = r4.x;
+    pb.k = r4.y;
     pb.omk = 1.0f - pb.k;
-    pb.gv = s.px[F_GV][q];
-    pb.one_m_metal = 1.0f - s.px[F_METAL][q];
+    pb.gv = r4.z;
+    pb.one_m_metal = 1.0f - r3.w;
     pb.nv4 = 4.0f * p.NdV;
     pb.vlx = pb.vly = pb.vlz = 0.0f;
     const float4* gl = reinterpret_cast<const float4*>(lights + li);
@@ -170,7 +169,7 @@ __device__ __forceinline__ float4 eval_pair(const f16k::Smem& s, uint32_t q, uin
     l.cos_inner = __uint_as_float(d.z);
     float4 o = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     int st = kNeedsPrecise;
-    if (s.px[F_DEP][q] >= 0.0f) st = eval<false>(p, pb, l, o.x, o.y, o.z, fast_guard(p));
+    if (r2.w >= 0.0f) st = eval<false>(p, pb, l, o.x, o.y, o.z, fast_guard(p));
     if (st == kNeedsPrecise) return precise_f16(gb, x0 + q % TW, y0 + q / TW, cam, lights, li);
     o.w = __int_as_float(st);
     return o;
@@ -198,9 +197,12 @@ __device__ __forceinline__ void accumulate(f16k::Smem& s, bool lit, uint32_t q, 
     const uint32_t rounds = __reduce_max_sync(0xffffffffu, lit ? rank + 1 : 0u);
     for (uint32_t r = 0; r < rounds; ++r) {
         if (lit && rank == r) {
-            kahan_add(s.acc[0][q], s.acc[3][q], cr);
-            kahan_add(s.acc[1][q], s.acc[4][q], cg);
-            kahan_add(s.acc[2][q], s.acc[5][q], cb);
+            float4 sum = s.acc[0][q], cmp = s.acc[1][q];
+            kahan_add(sum.x, cmp.x, cr);
+            kahan_add(sum.y, cmp.y, cg);
+            kahan_add(sum.z, cmp.z, cb);
+            s.acc[0][q] = sum;
+            s.acc[1][q] = cmp;
         }
         __syncwarp();
     }
@@ -259,8 +261,10 @@ __global__ void __launch_bounds__(f16k::kThreads, 3) shade_f16_kernel(
         s.kshift = 31u - __clz(uint32_t(kBins) / nk);
     }
 #pragma unroll
-    for (int k = 0; k < PPT; ++k)
-        for (int c = 0; c < 6; ++c) s.acc[c][t + k * kThreads] = 0.0f;
+    for (int k = 0; k < PPT; ++k) {
+        s.acc[0][t + k * kThreads] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        s.acc[1][t + k * kThreads] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
     if (t == 0) s.n_left = 0;
     __syncthreads();
 
@@ -307,22 +311,18 @@ __global__ void __launch_bounds__(f16k::kThreads, 3) shade_f16_kernel(
                 const float ndv = fmax_(fma_(nz, -Pz, fma_(ny, -Py, nx * -Px)) * in * iv, 0.0f);
                 const float ar = f16k::h2f(a.x & 0xffffu), ag = f16k::h2f(a.x >> 16), ab = f16k::h2f(a.y & 0xffffu);
                 const float rough = f16k::h2f(a.y >> 16), metal = f16k::h2f(mt);
-                s.px[F_PX][i] = Px; s.px[F_PY][i] = Py; s.px[F_PZ][i] = Pz;
-                s.px[F_NX][i] = nx * in; s.px[F_NY][i] = ny * in; s.px[F_NZ][i] = nz * in;
-                s.px[F_IP][i] = iv;
-                s.px[F_NDV][i] = ndv;
+                Rec& r = s.rec[i];
+                r.p = make_float4(Px, Py, Pz, iv);
+                r.n = make_float4(nx * in, ny * in, nz * in, ndv);
                 // grazing view: every pair of the pixel goes to the precise evaluation
-                s.px[F_DEP][i] = ndv < kFastMinNdV ? -depth : depth;
-                s.px[F_F0R][i] = fmin_(fmax_(metallic_f0(ar, metal), 0.0f), 0.999f);
-                s.px[F_F0G][i] = fmin_(fmax_(metallic_f0(ag, metal), 0.0f), 0.999f);
-                s.px[F_F0B][i] = fmin_(fmax_(metallic_f0(ab, metal), 0.0f), 0.999f);
-                s.px[F_DR][i] = ar * kInvPi; s.px[F_DG][i] = ag * kInvPi; s.px[F_DB][i] = ab * kInvPi;
+                r.f0 = make_float4(fmin_(fmax_(metallic_f0(ar, metal), 0.0f), 0.999f),
+                                   fmin_(fmax_(metallic_f0(ag, metal), 0.0f), 0.999f),
+                                   fmin_(fmax_(metallic_f0(ab, metal), 0.0f), 0.999f),
+                                   ndv < kFastMinNdV ? -depth : depth);
+                r.d = make_float4(ar * kInvPi, ag * kInvPi, ab * kInvPi, metal);
                 const float ra = rough * rough, r1 = rough + 1.0f;
                 const float kk = (r1 * r1) * 0.125f;
-                s.px[F_A2][i] = ra * ra;
-                s.px[F_K][i] = kk;
-                s.px[F_GV][i] = divn_(ndv, fma_(ndv, 1.0f - kk, kk + 0.0001f));
-                s.px[F_METAL][i] = metal;
+                r.b = make_float4(ra * ra, kk, divn_(ndv, fma_(ndv, 1.0f - kk, kk + 0.0001f)), 0.0f);
                 // own froxel: column of (x, y), slice of the linear view depth (the lists
                 // are conservative by 2^-10 of the slice depth, so the slice only needs
                 // the depth to a few ulp)
@@ -416,8 +416,9 @@ __global__ void __launch_bounds__(f16k::kThreads, 3) shade_f16_kernel(
         float px = 0, py = 0, pz = 0, nx = 0, ny = 0, nz = 0;
         uint32_t f = 0xffffffffu, lb = 0, le = 0;
         if (own) {
-            px = s.px[F_PX][i]; py = s.px[F_PY][i]; pz = s.px[F_PZ][i];
-            nx = s.px[F_NX][i]; ny = s.px[F_NY][i]; nz = s.px[F_NZ][i];
+            const float4 rp = s.rec[i].p, rn = s.rec[i].n;
+            px = rp.x; py = rp.y; pz = rp.z;
+            nx = rn.x; ny = rn.y; nz = rn.z;
             f = s.w.walk.fidx[i];
             lb = __ldg(grid.counts + f);
             le = __ldg(grid.counts + f + 1);
@@ -531,22 +532,23 @@ __global__ void __launch_bounds__(f16k::kThreads, 3) shade_f16_kernel(
         // albedo read again from the G-buffer (an L2 hit: the tile was read at set-up)
         const uint2 alb = *reinterpret_cast<const uint2*>(gb.plane[0] + gb.pitch[0] * y + 8ull * x);
         const float ar = f16k::h2f(alb.x & 0xffffu), ag = f16k::h2f(alb.x >> 16), ab = f16k::h2f(alb.y & 0xffffu);
-        const float ny = s.px[F_NY][i];
+        const float4 rn = s.rec[i].n;
+        const float ny = rn.y;
         const float ht = fma_(ny, 0.5f, 0.5f);
         // hemisphere ambient (deferred_lighting.wgsl:1196-1199) times ao (1, white SSAO)
         const float hr = fma_(skr, ht, skr * 0.15f * (1.0f - ht)) * ar;
         const float hg = fma_(skg, ht, skg * 0.15f * (1.0f - ht)) * ag;
         const float hb = fma_(skb, ht, skb * 0.15f * (1.0f - ht)) * ab;
+        const float4 sum = s.acc[0][i];
         float4 c;
-        c.x = s.acc[0][i] + hr;
-        c.y = s.acc[1][i] + hg;
-        c.z = s.acc[2][i] + hb;
+        c.x = sum.x + hr;
+        c.y = sum.y + hg;
+        c.z = sum.z + hb;
         c.w = 1.0f;
         if (debug_mode == 1u || debug_mode == 2u || debug_mode == 4u || debug_mode == 20u || debug_mode == 21u) {
             c = make_float4(ar, ag, ab, 1.0f);
         } else if (debug_mode == 5u) {
-            c = make_float4(fma_(s.px[F_NX][i], 0.5f, 0.5f), fma_(ny, 0.5f, 0.5f), fma_(s.px[F_NZ][i], 0.5f, 0.5f),
-                            1.0f);
+            c = make_float4(fma_(rn.x, 0.5f, 0.5f), fma_(ny, 0.5f, 0.5f), fma_(rn.z, 0.5f, 0.5f), 1.0f);
         }
         unsigned char* row = out.data + out.pitch * y;
         if (TARGET == HL_TARGET_RGBA32F) {

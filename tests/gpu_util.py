@@ -74,3 +74,24 @@ def gpu_shade(ctx, df: FR.DeviceFrame, grid: N.LightGrid, target_format=N.TARGET
     ctx.shade(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, N.target_struct(out, target_format))
     ctx.sync_status()
     return out.float().cpu().numpy().astype(np.float64)
+
+
+def gpu_shade_logged(ctx, df: FR.DeviceFrame, grid: N.LightGrid, target_format=N.TARGET_RGBA32F, fill=7.0,
+                     capacity=None):
+    """hl_shade with the lit-pair record on (hl_set_pair_log): returns the image as
+    gpu_shade does and the (K, 2) uint32 (y * W + x, light) pairs the kernel lit."""
+    T = torch()
+    cap = capacity if capacity is not None else max(1 << 16, df.width * df.height * 4)
+    while True:
+        pairs = T.zeros((cap, 2), dtype=T.int32, device="cuda")
+        count = T.zeros((1,), dtype=T.int32, device="cuda")
+        ctx.set_pair_log(pairs, count)
+        try:
+            img = gpu_shade(ctx, df, grid, target_format=target_format, fill=fill)
+        finally:
+            ctx.set_pair_log(None)
+        n = int(count.item())
+        if n <= cap:
+            return img, pairs[:n].cpu().numpy().view(np.uint32)
+        cap = n  # the count covers every lit pair: one more launch records them all
+        del pairs
