@@ -196,12 +196,13 @@ hl_status hl_bin_froxels(hl_ctx* ctx, const void* camera, const void* lights, ui
     if (out->capacity > 0 && !out->indices) return fail(ctx, HL_ERR_INVALID_ARGUMENT, "froxel indices is NULL");
     DeviceGuard dg(ctx->device);
     if (!dg.ok) return fail(ctx, HL_ERR_CUDA, "cudaSetDevice(%d) failed", ctx->device);
-    if ((s = ensure(ctx, ctx->bin_lights, ctx->bin_lights_cap, n > 0 ? n : 1, "bin light scratch")) != HL_OK) return s;
-    // single-pass binning state: chain words (zeroed when allocated: epoch 0 is never
-    // used) and the column ticket counter
-    const uint32_t cols = p->grid_x * p->grid_y;
+    // single-launch binning state: chain words (zeroed when allocated: epoch 0 is never
+    // used) and the work-item ticket counter
+    const uint32_t groups = hl::bin_item_groups(ctx->device, *p);
+    const uint64_t items = uint64_t(p->grid_x) * p->grid_y * groups;
+    if (items > 0x7FFFFFFFull) return fail(ctx, HL_ERR_SIZE, "froxel grid has %llu work items", (unsigned long long)items);
     unsigned long long* old_chain = ctx->froxel_chain;
-    if ((s = ensure(ctx, ctx->froxel_chain, ctx->froxel_chain_cap, cols, "froxel chain scratch")) != HL_OK) return s;
+    if ((s = ensure(ctx, ctx->froxel_chain, ctx->froxel_chain_cap, items, "froxel chain scratch")) != HL_OK) return s;
     cudaStream_t st = as_stream(stream);
     cudaError_t e = cudaSuccess;
     if (ctx->froxel_chain != old_chain)
@@ -214,11 +215,20 @@ hl_status hl_bin_froxels(hl_ctx* ctx, const void* camera, const void* lights, ui
     hl::SliceTable tab;
     std::memset(&tab, 0, sizeof tab);
     slice_table(*p, tab.z);
-    e = hl::launch_prep_bin_lights(camera, lights, n, true, ctx->bin_lights, st);
-    if (e == cudaSuccess)
-        e = hl::launch_bin_froxels_fused(camera, ctx->bin_lights, n, *p, tab, out->offsets, out->indices,
-                                         out->capacity, ctx->d_status, ctx->froxel_chain, ctx->bin_state, st);
+    const uint32_t stall_item = ctx->stall_item, stall_spins = ctx->stall_spins;
+    ctx->stall_item = ~0u;  // one call only
+    e = hl::launch_bin_froxels_items(camera, lights, n, *p, tab, groups, out->offsets, out->indices, out->capacity,
+                                     ctx->d_status, ctx->froxel_chain, ctx->bin_state, stall_item, stall_spins, st);
     return e == cudaSuccess ? HL_OK : cuda_fail(ctx, e, "bin_froxels launch");
+}
+
+hl_status hl_inject_binning_stall(hl_ctx* ctx, uint32_t item, uint32_t spins) {
+    if (!ctx) return HL_ERR_INVALID_ARGUMENT;
+    if (spins == 0 || spins > (1u << 20))
+        return fail(ctx, HL_ERR_INVALID_ARGUMENT, "stall test: %u polls (1..2^20)", spins);
+    ctx->stall_item = item;
+    ctx->stall_spins = spins;
+    return HL_OK;
 }
 
 hl_status hl_shade(hl_ctx* ctx, const void* camera, const void* globals, const hl_gbuffer* gbuffer, const void* lights,

@@ -12,6 +12,7 @@
 //
 // All floating-point work here uses correctly rounded __f*_rn operations in the
 // documented order, so the lists are bit-identical to the f32 CPU restatement.
+#include "hl_bin_item.cuh"
 #include "hl_common.cuh"
 #include "hl_internal.h"
 
@@ -19,71 +20,9 @@ namespace hl {
 
 namespace {
 
-constexpr int kBinWarps = 8;
-constexpr int kBinThreads = kBinWarps * 32;
-
-__device__ __forceinline__ uint32_t lanemask_lt() {
-    uint32_t m;
-    asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-    return m;
-}
-
-// make_plane_from_ndc_edge (light_cull.wgsl:85-100)
-__device__ __forceinline__ f3 plane_from_ndc_edge(float p00, float p11, float p0x, float p0y, float p1x, float p1y) {
-    f3 r0 = xnormalize(mk3(xdiv(p0x, p00), xdiv(p0y, p11), -1.0f));
-    f3 r1 = xnormalize(mk3(xdiv(p1x, p00), xdiv(p1y, p11), -1.0f));
-    return xnormalize(xcross(r0, r1));
-}
-
-struct Planes {
-    f3 n[4];
-};
-
-// Left, right, top, bottom planes of an NDC rectangle (light_cull.wgsl:148-151).
-__device__ __forceinline__ Planes rect_planes(float p00, float p11, float left, float right, float top, float bottom) {
-    Planes p;
-    p.n[0] = plane_from_ndc_edge(p00, p11, left, bottom, left, top);
-    p.n[1] = plane_from_ndc_edge(p00, p11, right, top, right, bottom);
-    p.n[2] = plane_from_ndc_edge(p00, p11, left, top, right, top);
-    p.n[3] = plane_from_ndc_edge(p00, p11, right, bottom, left, bottom);
-    return p;
-}
-
-// sphere_inside_tile_frustum (light_cull.wgsl:105-117); plane w = 0.
-__device__ __forceinline__ bool sphere_in_planes(const Planes& p, float cx, float cy, float cz, float r) {
-    const f3 c = mk3(cx, cy, cz);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        float dist = xadd(xdot(p.n[i], c), 0.0f);
-        if (dist < -r) return false;
-    }
-    return true;
-}
-
-// One light in the camera's view space, with its culling radius (widened for froxels).
-__device__ __forceinline__ BinLight prep_light(const GpuCamera* __restrict__ cam, const GpuLight& l,
-                                               uint32_t froxel_margin) {
-    const float* v = cam->view;
-    const float px = l.position_range[0], py = l.position_range[1], pz = l.position_range[2];
-    BinLight b;
-    b.cx = xmat_row(v, 0, px, py, pz, 1.0f);
-    b.cy = xmat_row(v, 1, px, py, pz, 1.0f);
-    b.cz = xmat_row(v, 2, px, py, pz, 1.0f);
-    const float r = l.position_range[3];
-    b.r = froxel_margin ? xadd(r, xmul(xadd(r, 1.0f), 1.0f / 1024.0f)) : r;
-    const float dx = l.direction_outer[0], dy = l.direction_outer[1], dz = l.direction_outer[2];
-    f3 a = xnormalize(mk3(xmat_row(v, 0, dx, dy, dz, 0.0f), xmat_row(v, 1, dx, dy, dz, 0.0f),
-                          xmat_row(v, 2, dx, dy, dz, 0.0f)));
-    b.ax = a.x;
-    b.ay = a.y;
-    b.az = a.z;
-    b.cos_o = l.direction_outer[3];
-    b.sin_o = xsqrt(xmax(xsub(1.0f, xmul(b.cos_o, b.cos_o)), 0.0f));
-    b.type = l.light_type;
-    b.cone = (l.light_type == 2u) && (0.0f < b.cos_o) && (b.cos_o < l.inner_angle);
-    b.pad = 0;
-    return b;
-}
+using namespace bin;
+constexpr int kBinWarps = bin::kWarps;
+constexpr int kBinThreads = bin::kThreads;
 
 __global__ void __launch_bounds__(256) prep_bin_lights_kernel(const GpuCamera* __restrict__ cam,
                                                               const GpuLight* __restrict__ lights, uint32_t n,
@@ -163,80 +102,6 @@ __global__ void __launch_bounds__(kBinThreads) bin_tiles_ref_kernel(const GpuCam
 // Froxel clustering
 // ----------------------------------------------------------------------------------
 constexpr int kColCap = 4096;  // column-list entries held in shared memory per round
-constexpr uint32_t kGatherU = 4;  // 256-light sub-rounds per gather step
-
-struct ColumnGeom {
-    Planes planes;
-    float kx0, kx1, ky_bot, ky_top;
-};
-
-__device__ __forceinline__ uint32_t ceil_div_u64(uint64_t a, uint64_t b) { return uint32_t((a + b - 1) / b); }
-
-__device__ __forceinline__ ColumnGeom column_geom(const GpuCamera* cam, const hl_froxel_params& p, uint32_t fx,
-                                                  uint32_t fy) {
-    const uint32_t px0 = ceil_div_u64(uint64_t(fx) * p.width, p.grid_x);
-    const uint32_t px1 = ceil_div_u64(uint64_t(fx + 1) * p.width, p.grid_x);
-    const uint32_t py0 = ceil_div_u64(uint64_t(fy) * p.height, p.grid_y);
-    const uint32_t py1 = ceil_div_u64(uint64_t(fy + 1) * p.height, p.grid_y);
-    const float fw = float(p.width), fh = float(p.height);
-    const float left = xsub(xmul(xdiv(float(px0), fw), 2.0f), 1.0f);
-    const float right = xsub(xmul(xdiv(float(px1), fw), 2.0f), 1.0f);
-    const float top = xsub(1.0f, xmul(xdiv(float(py0), fh), 2.0f));
-    const float bottom = xsub(1.0f, xmul(xdiv(float(py1), fh), 2.0f));
-    const float p00 = cam->proj[0], p11 = cam->proj[5];
-    ColumnGeom g;
-    g.planes = rect_planes(p00, p11, left, right, top, bottom);
-    g.kx0 = xdiv(left, p00);
-    g.kx1 = xdiv(right, p00);
-    g.ky_bot = xdiv(bottom, p11);
-    g.ky_top = xdiv(top, p11);
-    return g;
-}
-
-struct Box {
-    float lox, loy, loz, hix, hiy, hiz;
-    float cx, cy, cz, radius;
-};
-
-__device__ __forceinline__ Box froxel_box(const ColumnGeom& g, float z0, float z1) {
-    Box b;
-    const float m = xadd(xmul(z1, 1.0f / 1024.0f), 1.0f / 4096.0f);
-    b.lox = xsub(xmin(xmul(g.kx0, z0), xmul(g.kx0, z1)), m);
-    b.hix = xadd(xmax(xmul(g.kx1, z0), xmul(g.kx1, z1)), m);
-    b.loy = xsub(xmin(xmul(g.ky_bot, z0), xmul(g.ky_bot, z1)), m);
-    b.hiy = xadd(xmax(xmul(g.ky_top, z0), xmul(g.ky_top, z1)), m);
-    b.loz = xsub(-z1, m);
-    b.hiz = xadd(-z0, m);
-    b.cx = xmul(xadd(b.lox, b.hix), 0.5f);
-    b.cy = xmul(xadd(b.loy, b.hiy), 0.5f);
-    b.cz = xmul(xadd(b.loz, b.hiz), 0.5f);
-    const f3 e = mk3(xsub(b.hix, b.lox), xsub(b.hiy, b.loy), xsub(b.hiz, b.loz));
-    b.radius = xmul(xsqrt(xdot(e, e)), 0.5f);
-    return b;
-}
-
-__device__ __forceinline__ float axis_gap(float c, float lo, float hi) {
-    return c < lo ? xsub(lo, c) : (hi < c ? xsub(c, hi) : 0.0f);
-}
-
-__device__ __forceinline__ bool light_meets_froxel(const BinLight& l, const Box& b) {
-    if (l.type == 0u) return true;
-    const float dx = axis_gap(l.cx, b.lox, b.hix);
-    const float dy = axis_gap(l.cy, b.loy, b.hiy);
-    const float dz = axis_gap(l.cz, b.loz, b.hiz);
-    const float d2 = xadd(xadd(xmul(dx, dx), xmul(dy, dy)), xmul(dz, dz));
-    if (!(d2 <= xmul(l.r, l.r))) return false;
-    if (l.cone) {
-        const f3 v = mk3(xsub(b.cx, l.cx), xsub(b.cy, l.cy), xsub(b.cz, l.cz));
-        const float vlen2 = xdot(v, v);
-        const float v1 = xdot(v, mk3(l.ax, l.ay, l.az));
-        const float closest = xsub(xmul(l.cos_o, xsqrt(xmax(xsub(vlen2, xmul(v1, v1)), 0.0f))), xmul(v1, l.sin_o));
-        if (closest > b.radius) return false;
-        if (v1 > xadd(b.radius, l.r)) return false;
-        if (v1 < -b.radius) return false;
-    }
-    return true;
-}
 
 struct BinSmem {
     uint32_t col[kColCap];
@@ -336,255 +201,42 @@ __global__ void __launch_bounds__(kBinThreads) bin_froxels_kernel(const GpuCamer
     bin_column<FILL>(sm, cam, bl, n, p, tab.z, blockIdx.x, counts, offsets, indices, capacity, status);
 }
 
-// ---- single pass: count, chained scan across columns, fill — one launch ----------
+// ---- single launch: count, chained scan across work items, fill ---------------------
 //
-// Each CTA takes a column by ticket (a device counter, so CTA k waits only for columns
-// that started before it), counts its slices, publishes its total, finds the entries
-// of all earlier columns by looking back along the chain of published totals
-// (decoupled look-back: a predecessor's inclusive prefix ends the walk, its bare total
-// is added and the walk goes on), publishes its own inclusive prefix, writes its
-// offsets and fills its lists. Chain words hold epoch << 32 | state << 30 | value; a
-// word of another launch's epoch reads as "not yet published". The ticket base and the
-// epoch live on the device and the last CTA of a launch advances them, so a launch
-// recorded in a CUDA graph can be replayed.
-constexpr uint32_t kFlagAggregate = 1u, kFlagPrefix = 2u;
-constexpr uint32_t kChainValueMax = (1u << 30) - 1u;
-constexpr uint32_t kLookbackSpins = 1u << 20;  // ~0.1 s of polling before HL_ERR_TIMEOUT
-
-constexpr uint32_t kMaskCap = 4096;  // (slice, 32-light chunk) results kept from the count for the fill
-
-struct FusedSmem {
-    BinSmem b;
-    uint32_t slice_dst[kMaxSlices];  // first entry of each slice of this column
-    uint32_t mask[kMaskCap];         // ballot of chunk c of slice s at [s * chunks + c]
-    uint32_t col, excl, total;
-};
-
-__device__ __forceinline__ unsigned long long ld_chain(const unsigned long long* p) {
-    return *reinterpret_cast<const volatile unsigned long long*>(p);
-}
-
-__device__ __forceinline__ void st_chain(unsigned long long* p, uint32_t epoch, uint32_t state, uint32_t value) {
-    __threadfence();
-    *reinterpret_cast<volatile unsigned long long*>(p) =
-        (static_cast<unsigned long long>(epoch) << 32) | (state << 30) | min(value, kChainValueMax);
-}
-
-// Appends to sm.col, in light-index order, the lights from `base` on that may touch the
-// column (directional, or a sphere not outside its four planes), until the lights run out
-// or the next step could overflow kColCap. A step tests kGatherU x 256 lights, their
-// loads in flight together, with two barriers.
-__device__ __forceinline__ uint32_t gather_round(BinSmem& sm, const ColumnGeom& g, const BinLight* __restrict__ bl,
-                                                 uint32_t n, uint32_t& base) {
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint32_t col_len = 0;
-    __syncthreads();
-    while (base < n && col_len + kGatherU * kBinThreads <= kColCap) {
-        bool pass[kGatherU];
-        uint32_t mask[kGatherU];
-#pragma unroll
-        for (uint32_t u = 0; u < kGatherU; ++u) {
-            const uint32_t i = base + u * kBinThreads + threadIdx.x;
-            pass[u] = false;
-            if (i < n) {
-                const BinLight l = bl[i];
-                pass[u] = (l.type == 0u) || sphere_in_planes(g.planes, l.cx, l.cy, l.cz, l.r);
-            }
-        }
-#pragma unroll
-        for (uint32_t u = 0; u < kGatherU; ++u) {
-            mask[u] = __ballot_sync(0xffffffffu, pass[u]);
-            if (lane == 0) sm.warp_tot[u * kBinWarps + warp] = __popc(mask[u]);
-        }
-        __syncthreads();
-#pragma unroll
-        for (uint32_t u = 0; u < kGatherU; ++u) {
-            uint32_t before = 0, total = 0;
-#pragma unroll
-            for (int w = 0; w < kBinWarps; ++w) {
-                const uint32_t t = sm.warp_tot[u * kBinWarps + w];
-                before += (uint32_t(w) < warp) ? t : 0u;
-                total += t;
-            }
-            if (pass[u]) sm.col[col_len + before + __popc(mask[u] & lanemask_lt())] = base + u * kBinThreads + threadIdx.x;
-            col_len += total;
-        }
-        base += kGatherU * kBinThreads;
-        __syncthreads();
-    }
-    return col_len;
-}
-
-// Tests a gathered round against every slice box of the column: counts into
-// sm.slice_run, and with FILL writes the lists from sm.slice_dst. A warp takes a slice
-// and four 32-light chunks at a time, their light loads in flight together. With MASKS
-// the count keeps each chunk's ballot and the fill replays them instead of testing again.
-template <bool FILL>
-__device__ __forceinline__ void test_slices(FusedSmem& fs, const ColumnGeom& g, const BinLight* __restrict__ bl,
-                                            const hl_froxel_params& p, const float* __restrict__ tabz, float zlast,
-                                            uint32_t col_len, uint32_t* __restrict__ indices, uint32_t capacity,
-                                            bool masks) {
-    constexpr uint32_t kU = 4;
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t chunks = (col_len + 31) / 32;
-    for (uint32_t s = warp; s < p.grid_z; s += kBinWarps) {
-        uint32_t run = fs.b.slice_run[s];
-        const uint32_t dst0 = FILL ? fs.slice_dst[s] : 0u;
-        uint32_t* sm_mask = fs.mask + s * chunks;
-        if (FILL && masks) {
-            for (uint32_t c = 0; c < chunks; ++c) {
-                const uint32_t mask = sm_mask[c];
-                if ((mask >> lane) & 1u) {
-                    const uint64_t dst = uint64_t(dst0) + run + __popc(mask & lanemask_lt());
-                    if (dst < capacity) indices[dst] = fs.b.col[c * 32 + lane];
-                }
-                run += __popc(mask);
-            }
-        } else {
-            const float z0 = tabz[s];
-            const float z1 = (s + 1 == p.grid_z) ? zlast : tabz[s + 1];
-            const Box b = froxel_box(g, z0, z1);
-            for (uint32_t c0 = 0; c0 < chunks; c0 += kU) {
-                uint32_t li[kU];
-                BinLight l[kU];
-#pragma unroll
-                for (uint32_t u = 0; u < kU; ++u) {
-                    const uint32_t j = (c0 + u) * 32 + lane;
-                    li[u] = j < col_len ? fs.b.col[j] : 0xffffffffu;
-                    if (li[u] != 0xffffffffu) l[u] = bl[li[u]];
-                }
-#pragma unroll
-                for (uint32_t u = 0; u < kU; ++u) {
-                    if (c0 + u >= chunks) break;  // warp-uniform
-                    const bool pass = li[u] != 0xffffffffu && light_meets_froxel(l[u], b);
-                    const uint32_t mask = __ballot_sync(0xffffffffu, pass);
-                    if (FILL && pass) {
-                        const uint64_t dst = uint64_t(dst0) + run + __popc(mask & lanemask_lt());
-                        if (dst < capacity) indices[dst] = li[u];
-                    }
-                    if (!FILL && masks && lane == 0) sm_mask[c0 + u] = mask;
-                    run += __popc(mask);
-                }
-            }
-        }
-        if (lane == 0) fs.b.slice_run[s] = run;
-    }
-}
-
-__global__ void __launch_bounds__(kBinThreads) bin_froxels_fused_kernel(
-    const GpuCamera* __restrict__ cam, const BinLight* __restrict__ bl, uint32_t n, hl_froxel_params p,
-    const __grid_constant__ SliceTable tab, uint32_t* __restrict__ offsets, uint32_t* __restrict__ indices,
-    uint32_t capacity, int* __restrict__ status, unsigned long long* __restrict__ chain,
-    BinChainState* __restrict__ state) {
-    __shared__ FusedSmem fs;
-    __shared__ uint32_t s_epoch;
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t cols = p.grid_x * p.grid_y;
+// Each CTA takes a work item by ticket (a device counter, so item k waits only for
+// items that started before it) and bins it (bin::bin_item: its lights transformed to
+// view space as it gathers them, so no separate preparation launch). The ticket base
+// and the epoch live on the device and the last CTA of a launch advances them, so a
+// launch recorded in a CUDA graph can be replayed.
+__global__ void __launch_bounds__(kBinThreads, 3) bin_froxels_items_kernel(
+    const GpuCamera* __restrict__ cam, const GpuLight* __restrict__ lights, uint32_t n, hl_froxel_params p,
+    const __grid_constant__ SliceTable tab, uint32_t groups, uint32_t* __restrict__ offsets,
+    uint32_t* __restrict__ indices, uint32_t capacity, int* __restrict__ status,
+    unsigned long long* __restrict__ chain, BinChainState* __restrict__ state, StallTest test) {
+    __shared__ ItemSmem sm;
+    __shared__ uint32_t s_item, s_epoch;
+    const uint32_t items = p.grid_x * p.grid_y * groups;
     if (threadIdx.x == 0) {
         // every CTA of the previous launch has finished before this one starts (stream
         // order), so base and epoch are that launch's final values
         const unsigned long long base = *reinterpret_cast<volatile unsigned long long*>(&state->base);
         s_epoch = *reinterpret_cast<volatile uint32_t*>(&state->epoch) + 1u;
-        fs.col = uint32_t(atomicAdd(&state->ticket, 1ull) - base);
+        s_item = uint32_t(atomicAdd(&state->ticket, 1ull) - base);
     }
     __syncthreads();
-    const uint32_t col = fs.col, epoch = s_epoch;
-    if (col >= cols) {  // launches overlapping on one context: refused
+    const uint32_t item = s_item, epoch = s_epoch;
+    if (item >= items) {  // launches overlapping on one context: refused
         if (threadIdx.x == 0) raise_status(status, HL_ERR_DEVICE_BOUNDS);
         return;
     }
-    const ColumnGeom g = column_geom(cam, p, col % p.grid_x, col / p.grid_x);
-    const float zlast = xmax(tab.z[p.grid_z], cam->forward_far[3]);
-    for (uint32_t s = threadIdx.x; s < p.grid_z; s += blockDim.x) fs.b.slice_run[s] = 0;
     pdl_launch_dependents();  // the shading launch's light table and pixel set-up may start
-    pdl_wait();               // the view-space lights are written
-
-    // ---- 1. count ----
-    uint32_t base = 0, col_len = 0;
-    bool one_round = true, masks = false;
-    for (bool first = true;; first = false) {
-        col_len = gather_round(fs.b, g, bl, n, base);
-        if (!first) one_round = false;
-        // a column gathered in one round keeps its chunk ballots when they fit
-        masks = one_round && base >= n && p.grid_z * ((col_len + 31) / 32) <= kMaskCap;
-        test_slices<false>(fs, g, bl, p, tab.z, zlast, col_len, indices, capacity, masks);
-        if (base >= n) break;
-    }
-    __syncthreads();
-
-    // ---- 2. chained scan over columns ----
-    if (warp == 0) {
-        if (lane == 0) {
-            uint32_t acc = 0;
-            for (uint32_t s = 0; s < p.grid_z; ++s) {
-                fs.slice_dst[s] = acc;
-                acc += fs.b.slice_run[s];
-            }
-            fs.total = acc;
-            st_chain(chain + col, epoch, col == 0 ? kFlagPrefix : kFlagAggregate, acc);
-        }
-        __syncwarp();
-        uint32_t excl = 0;
-        int32_t pred = int32_t(col) - 1;
-        uint32_t spins = 0;
-        while (pred >= 0) {
-            const int32_t c = pred - int32_t(lane);
-            uint32_t st = kFlagPrefix, val = 0;  // before column 0: a prefix of 0
-            if (c >= 0) {
-                const unsigned long long w = ld_chain(chain + c);
-                st = uint32_t(w >> 32) == epoch ? (uint32_t(w) >> 30) : 0u;
-                val = uint32_t(w) & kChainValueMax;
-            }
-            const uint32_t pm = __ballot_sync(0xffffffffu, st == kFlagPrefix);
-            const int stop = pm ? __ffs(pm) - 1 : 31;  // lanes 0..stop are summed
-            const uint32_t upto = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
-            if (__ballot_sync(0xffffffffu, st == 0u) & upto) {
-                if (++spins > kLookbackSpins) {
-                    if (lane == 0) raise_status(status, HL_ERR_TIMEOUT);
-                    break;
-                }
-                __nanosleep(64);
-                continue;
-            }
-            excl += __reduce_add_sync(0xffffffffu, uint32_t(lane) <= uint32_t(stop) ? val : 0u);
-            if (pm) break;
-            pred -= 32;
-        }
-        if (lane == 0) {
-            if (col > 0) st_chain(chain + col, epoch, kFlagPrefix, excl + fs.total);
-            fs.excl = excl;
-            if (uint64_t(excl) + fs.total > capacity) raise_status(status, HL_ERR_CAPACITY);
-            if (uint64_t(excl) + fs.total > kChainValueMax) raise_status(status, HL_ERR_SIZE);
-        }
-    }
-    __syncthreads();
-    const uint32_t excl = fs.excl;
-    for (uint32_t s = threadIdx.x; s < p.grid_z; s += blockDim.x) {
-        fs.slice_dst[s] += excl;
-        offsets[col * p.grid_z + s] = fs.slice_dst[s];
-        fs.b.slice_run[s] = 0;
-    }
-    if (col == cols - 1 && threadIdx.x == 0) offsets[cols * p.grid_z] = excl + fs.total;
-    __syncthreads();
-
-    // ---- 3. fill (from the round still in shared memory when there was only one) ----
-    if (one_round) {
-        test_slices<true>(fs, g, bl, p, tab.z, zlast, col_len, indices, capacity, masks);
-    } else {
-        base = 0;
-        for (;;) {
-            col_len = gather_round(fs.b, g, bl, n, base);
-            test_slices<true>(fs, g, bl, p, tab.z, zlast, col_len, indices, capacity, false);
-            if (base >= n) break;
-        }
-    }
+    bin_item(sm, cam, lights, n, p, tab.z, item, groups, epoch, chain, offsets, indices, capacity, status, test);
     // the last CTA to finish advances the ticket base and the epoch for the next launch
-    __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
-        if (atomicAdd(&state->done, 1u) == cols - 1u) {
+        if (atomicAdd(&state->done, 1u) == items - 1u) {
             state->done = 0u;
-            state->base += cols;
+            state->base += items;
             state->epoch = epoch;
             __threadfence();
         }
@@ -730,19 +382,23 @@ cudaError_t launch_bin_froxels_batched(const BinViewDesc* descs, uint32_t n_view
     return cudaGetLastError();
 }
 
-cudaError_t launch_bin_froxels_fused(const void* camera, const BinLight* bl, uint32_t n, const hl_froxel_params& p,
-                                     const SliceTable& tab, uint32_t* offsets, uint32_t* indices, uint32_t capacity,
-                                     int* status, unsigned long long* chain, BinChainState* state,
-                                     cudaStream_t stream) {
-    const uint32_t cols = p.grid_x * p.grid_y;
-    // as a dependent launch only right after this call's light preparation: two binning
-    // launches of one context must never overlap (ticket and epoch)
-    if (n > 0)
-        return launch_pdl(bin_froxels_fused_kernel, dim3(cols), dim3(kBinThreads), 0, stream,
-                          static_cast<const GpuCamera*>(camera), bl, n, p, tab, offsets, indices, capacity, status,
-                          chain, state);
-    bin_froxels_fused_kernel<<<cols, kBinThreads, 0, stream>>>(static_cast<const GpuCamera*>(camera), bl, n, p, tab,
-                                                               offsets, indices, capacity, status, chain, state);
+uint32_t bin_item_groups(int device, const hl_froxel_params& p) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) sms = 1;
+    return item_groups(p, 2u * uint32_t(sms > 0 ? sms : 1));
+}
+
+cudaError_t launch_bin_froxels_items(const void* camera, const void* lights, uint32_t n, const hl_froxel_params& p,
+                                     const SliceTable& tab, uint32_t groups, uint32_t* offsets, uint32_t* indices,
+                                     uint32_t capacity, int* status, unsigned long long* chain, BinChainState* state,
+                                     uint32_t stall_item, uint32_t stall_spins, cudaStream_t stream) {
+    const uint32_t items = p.grid_x * p.grid_y * groups;
+    const StallTest test{stall_item, stall_item == ~0u ? kLookbackSpins : stall_spins};
+    // launched plainly: it starts after its predecessor has finished, so two binning
+    // launches of one context (sharing ticket and chain) never overlap
+    bin_froxels_items_kernel<<<items, kBinThreads, 0, stream>>>(
+        static_cast<const GpuCamera*>(camera), static_cast<const GpuLight*>(lights), n, p, tab, groups, offsets,
+        indices, capacity, status, chain, state, test);
     return cudaGetLastError();
 }
 

@@ -19,8 +19,9 @@ struct hl_ctx {
     uint32_t bin_lights_cap = 0;
     uint32_t* froxel_counts = nullptr;
     uint32_t froxel_counts_cap = 0;
-    unsigned long long* froxel_chain = nullptr;  // per-column words of the single-pass binning
+    unsigned long long* froxel_chain = nullptr;  // per-item words of the single-launch binning
     uint32_t froxel_chain_cap = 0;
+    uint32_t stall_item = ~0u, stall_spins = 0;  // one-shot failure injection (hl_inject_binning_stall)
     hl::BinChainState* bin_state = nullptr;      // ticket counter and epoch of the single-pass binning
     float4* shade_cand = nullptr;       // candidate-test light table of hl_shade
     uint32_t shade_cand_cap = 0;

@@ -53,13 +53,17 @@ struct ShadeViewDesc {
     uint32_t tile_start;   // first CTA of this view in the batched launch
 };
 
-// Single-launch froxel binning (count, chained scan, fill). chain: one word per column
-// and state: both zeroed when allocated; launches sharing them must not overlap.
+// Single-launch froxel binning (count, chained scan, fill) over work items of a
+// froxel column's slice group (groups per column from bin_item_groups). chain: one word
+// per item and state: both zeroed when allocated; launches sharing them must not
+// overlap. stall_item (~0u: none) never publishes its chain word and the look-back
+// gives up after stall_spins polls: a failure-injection test of the bounded wait.
 struct BinChainState;
-cudaError_t launch_bin_froxels_fused(const void* camera, const BinLight* bl, uint32_t n, const hl_froxel_params& p,
-                                     const SliceTable& tab, uint32_t* offsets, uint32_t* indices, uint32_t capacity,
-                                     int* status, unsigned long long* chain, BinChainState* state,
-                                     cudaStream_t stream);
+uint32_t bin_item_groups(int device, const hl_froxel_params& p);
+cudaError_t launch_bin_froxels_items(const void* camera, const void* lights, uint32_t n, const hl_froxel_params& p,
+                                     const SliceTable& tab, uint32_t groups, uint32_t* offsets, uint32_t* indices,
+                                     uint32_t capacity, int* status, unsigned long long* chain, BinChainState* state,
+                                     uint32_t stall_item, uint32_t stall_spins, cudaStream_t stream);
 
 // Froxel binning of every view of a batch (descs: device array of n_views).
 cudaError_t launch_bin_froxels_batched(const BinViewDesc* descs, uint32_t n_views, uint32_t total_columns,
@@ -111,6 +115,12 @@ cudaError_t launch_shade_f16(uint32_t target_format, const void* camera, const v
                              const void* lights, uint32_t n_lights, const GridView& grid, const SliceTable& tab,
                              const TargetView& out, int* status, float4* cand, const PairLog& log,
                              cudaStream_t stream);
+
+// The batched form of launch_shade_f16: one launch over every (view, tile) of a batch
+// (the views' candidate tables already written).
+cudaError_t launch_shade_f16_batched(uint32_t target_format, const ShadeViewDesc* descs, uint32_t n_views,
+                                     uint32_t total_tiles, const void* globals, const void* lights, uint32_t n,
+                                     int* status, cudaStream_t stream);
 
 // Adjoint of shading. partials: grid_size * n_lights * 8 floats of scratch.
 uint32_t adjoint_grid_size(int device, uint32_t width, uint32_t height);

@@ -743,6 +743,8 @@ cudaError_t launch_batched(const ShadeViewDesc* descs, uint32_t n_views, uint32_
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
+    if (LAYOUT == HL_GBUF_F16)  // the single-view FP16 path's tile code, so that every view matches it
+        return launch_shade_f16_batched(TARGET, descs, n_views, total_tiles, globals, lights, n, status, stream);
     kern<<<total_tiles, sk::kThreads, smem, stream>>>(descs, n_views, static_cast<const DeferredGlobals*>(globals),
                                                       static_cast<const GpuLight*>(lights), n, status);
     return cudaGetLastError();

@@ -222,22 +222,23 @@ __device__ __noinline__ void flush32(f16k::Smem& s, const uint32_t* queue, uint3
     __syncwarp();
 }
 
+// Lights the 32x16 tile (bx, by) of one view. prefetch_next: the tile index (row-major
+// over tiles_x tiles per row) whose G-buffer to ask L2 for, or ~0u.
 template <uint32_t TARGET>
-__global__ void __launch_bounds__(f16k::kThreads, 3) shade_f16_kernel(
-    const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const __grid_constant__ GBufView gb,
-    const GpuLight* __restrict__ lights, uint32_t n_lights, const GridView grid,
-    const __grid_constant__ SliceTable tabz, const TargetView out, int* __restrict__ status,
-    const float4* __restrict__ cand, const __grid_constant__ PairLog log) {
+__device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* __restrict__ cam,
+                                               const DeferredGlobals* __restrict__ glb, const GBufView& gb,
+                                               const GpuLight* __restrict__ lights, uint32_t n_lights,
+                                               const GridView& grid, const float* __restrict__ tabz,
+                                               const TargetView& out, int* __restrict__ status,
+                                               const float4* __restrict__ cand, const PairLog& log, uint32_t bx,
+                                               uint32_t by, uint32_t tiles_x, uint32_t prefetch_next) {
     using namespace f16k;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    Smem& s = *reinterpret_cast<Smem*>(smem_raw);
     const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const uint32_t bx = blockIdx.x, by = blockIdx.y;
     const uint32_t x0 = bx * TW, y0 = by * TH;
     const hl_froxel_params& fp = grid.fp;
 
     for (uint32_t b = t; b < uint32_t(kBins); b += kThreads) s.u.sort.hist[b] = 0;
-    for (uint32_t k = t; k <= fp.grid_z; k += kThreads) s.u.sort.tab[k] = tabz.z[k];
+    for (uint32_t k = t; k <= fp.grid_z; k += kThreads) s.u.sort.tab[k] = tabz[k];
     // froxel column of each pixel column and row of the tile (x * grid_x < 2^32 for
     // viewports of at most 65536 pixels per side)
     if (t < uint32_t(TW)) {
@@ -375,13 +376,12 @@ __global__ void __launch_bounds__(f16k::kThreads, 3) shade_f16_kernel(
     for (int k = 0; k < PPT; ++k)
         if (valid[k]) s.w.walk.order[s.u.sort.hist[key[k]] + slot[k]] = uint16_t(t + k * kThreads);
 
-    {   // ask L2 for the G-buffer rows of the tile one wave (3 CTAs x SMs) further on:
+    if (prefetch_next != ~0u) {
+        // ask L2 for the G-buffer rows of the tile the next wave will likely take:
         // 32 x 128 B of plane 0 (8 B/px), 16 x 128 B of planes 1 and 3, 16 x 64 B of plane 2
-        uint32_t nsm;
-        asm("mov.u32 %0, %%nsmid;" : "=r"(nsm));
-        const uint32_t next = by * gridDim.x + bx + 3u * nsm;
-        if (t < 80u && next < gridDim.x * gridDim.y) {
-            const uint32_t nx0 = (next % gridDim.x) * TW, ny0 = (next / gridDim.x) * TH;
+        const uint32_t next = prefetch_next;
+        if (t < 80u) {
+            const uint32_t nx0 = (next % tiles_x) * TW, ny0 = (next / tiles_x) * TH;
             const uint32_t pl = t < 32u ? 0u : t < 48u ? 1u : t < 64u ? 2u : 3u;
             const uint32_t row = t < 32u ? t >> 1 : (t - 16u) & 15u;
             const uint32_t bpp = pl == 0u ? 8u : pl == 2u ? 2u : 4u;
@@ -564,11 +564,48 @@ __global__ void __launch_bounds__(f16k::kThreads, 3) shade_f16_kernel(
 }
 
 template <uint32_t TARGET>
-cudaError_t launch_target(const void* camera, const void* globals, const GBufView& gb, const void* lights, uint32_t n,
-                          const GridView& grid, const SliceTable& tab, const TargetView& out, int* status,
-                          float4* cand, const PairLog& log, cudaStream_t stream) {
-    auto kern = shade_f16_kernel<TARGET>;
-    const int smem = int(sizeof(f16k::Smem));
+__global__ void __launch_bounds__(f16k::kThreads, 3) shade_f16_kernel(
+    const GpuCamera* __restrict__ cam, const DeferredGlobals* __restrict__ glb, const __grid_constant__ GBufView gb,
+    const GpuLight* __restrict__ lights, uint32_t n_lights, const __grid_constant__ GridView grid,
+    const __grid_constant__ SliceTable tabz, const __grid_constant__ TargetView out, int* __restrict__ status,
+    const float4* __restrict__ cand, const __grid_constant__ PairLog log) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    f16k::Smem& s = *reinterpret_cast<f16k::Smem*>(smem_raw);
+    // the tile one wave (3 CTAs x SMs) further on is the next to start on this SM
+    uint32_t nsm;
+    asm("mov.u32 %0, %%nsmid;" : "=r"(nsm));
+    const uint32_t next = blockIdx.y * gridDim.x + blockIdx.x + 3u * nsm;
+    shade_tile_f16<TARGET>(s, cam, glb, gb, lights, n_lights, grid, tabz.z, out, status, cand, log, blockIdx.x,
+                           blockIdx.y, gridDim.x, next < gridDim.x * gridDim.y ? next : ~0u);
+}
+
+// Every tile of every view of a batch: CTA b lights tile b - tile_start of the view
+// whose [tile_start, next tile_start) holds b.
+template <uint32_t TARGET>
+__global__ void __launch_bounds__(f16k::kThreads, 3) shade_f16_batched_kernel(const ShadeViewDesc* __restrict__ d,
+                                                                             uint32_t n_views,
+                                                                             const DeferredGlobals* __restrict__ glb,
+                                                                             const GpuLight* __restrict__ lights,
+                                                                             uint32_t n_lights, int* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    f16k::Smem& s = *reinterpret_cast<f16k::Smem*>(smem_raw);
+    uint32_t lo = 0, hi = n_views;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (__ldg(&d[mid].tile_start) <= blockIdx.x) lo = mid; else hi = mid;
+    }
+    const ShadeViewDesc& v = d[lo];
+    const uint32_t local = blockIdx.x - v.tile_start;
+    const GBufView gb = v.gb;
+    const GridView grid = v.grid;
+    const TargetView out = v.out;
+    shade_tile_f16<TARGET>(s, static_cast<const GpuCamera*>(v.camera), glb, gb, lights, n_lights, grid, v.tabz, out,
+                           status, v.cand, PairLog{nullptr, nullptr, 0}, local % v.tiles_x, local / v.tiles_x,
+                           v.tiles_x, ~0u);
+}
+
+template <class K>
+cudaError_t smem_attr(K kern, int smem) {
     static unsigned long long attr_devices = 0;  // devices on which the smem limit is raised
     int dev = 0;
     cudaGetDevice(&dev);
@@ -577,6 +614,17 @@ cudaError_t launch_target(const void* camera, const void* globals, const GBufVie
         if (e != cudaSuccess) return e;
         attr_devices |= 1ull << dev;
     }
+    return cudaSuccess;
+}
+
+template <uint32_t TARGET>
+cudaError_t launch_target(const void* camera, const void* globals, const GBufView& gb, const void* lights, uint32_t n,
+                          const GridView& grid, const SliceTable& tab, const TargetView& out, int* status,
+                          float4* cand, const PairLog& log, cudaStream_t stream) {
+    auto kern = shade_f16_kernel<TARGET>;
+    const int smem = int(sizeof(f16k::Smem));
+    cudaError_t ea = smem_attr(kern, smem);
+    if (ea != cudaSuccess) return ea;
     if (n > 0) {
         cudaError_t e = launch_prep_cand(camera, lights, n, true, cand, stream);
         if (e != cudaSuccess) return e;
@@ -588,6 +636,20 @@ cudaError_t launch_target(const void* camera, const void* globals, const GBufVie
 }
 
 }  // namespace
+
+cudaError_t launch_shade_f16_batched(uint32_t target_format, const ShadeViewDesc* descs, uint32_t n_views,
+                                     uint32_t total_tiles, const void* globals, const void* lights, uint32_t n,
+                                     int* status, cudaStream_t stream) {
+    const int smem = int(sizeof(f16k::Smem));
+    const bool h = target_format == HL_TARGET_RGBA16F;
+    auto kern = h ? shade_f16_batched_kernel<HL_TARGET_RGBA16F> : shade_f16_batched_kernel<HL_TARGET_RGBA32F>;
+    cudaError_t e = h ? smem_attr(shade_f16_batched_kernel<HL_TARGET_RGBA16F>, smem)
+                      : smem_attr(shade_f16_batched_kernel<HL_TARGET_RGBA32F>, smem);
+    if (e != cudaSuccess) return e;
+    kern<<<total_tiles, f16k::kThreads, smem, stream>>>(descs, n_views, static_cast<const DeferredGlobals*>(globals),
+                                                         static_cast<const GpuLight*>(lights), n, status);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_shade_f16(uint32_t target_format, const void* camera, const void* globals, const GBufView& gb,
                              const void* lights, uint32_t n_lights, const GridView& grid, const SliceTable& tab,

@@ -134,6 +134,7 @@ EXPORTS = [
     "hl_shade_adjoint", "hl_batch_plan_create", "hl_batch_execute", "hl_batch_plan_view_grid",
     "hl_batch_plan_destroy", "hl_probe_fp32_peak", "hl_bin_froxels_noalloc", "hl_shade_fragments",
     "hl_write_gbuffer", "hl_shade_shadowed", "hl_shade_ex", "hl_shade_reflections", "hl_set_pair_log",
+    "hl_inject_binning_stall",
 ]
 
 _lock = threading.Lock()
@@ -186,6 +187,8 @@ def _bind(l):
     l.hl_shade.restype = i32
     l.hl_shade_stats.argtypes = [vp, vp, vp, P(GBuffer), vp, u32, P(LightGrid), vp, vp]
     l.hl_shade_stats.restype = i32
+    l.hl_inject_binning_stall.argtypes = [vp, u32, u32]
+    l.hl_inject_binning_stall.restype = i32
     l.hl_set_pair_log.argtypes = [vp, vp, u32, vp]
     l.hl_set_pair_log.restype = i32
     l.hl_shade_adjoint.argtypes = [vp, vp, vp, P(GBuffer), vp, u32, P(LightGrid), vp, C.c_uint64, vp, vp, vp]
@@ -360,6 +363,11 @@ class Context:
     def shade_stats(self, camera, globals_, gbuffer: GBuffer, lights, n_lights, grid: LightGrid, counts, stream=None):
         self._check(self._l.hl_shade_stats(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer), _ptr(lights),
                                            n_lights, C.byref(grid), _ptr(counts), _stream(stream)), "hl_shade_stats")
+
+    def inject_binning_stall(self, item: int, spins: int):
+        """The next bin_froxels on this context runs with work item ``item`` withholding
+        its running total; the others give up after ``spins`` polls (HL_ERR_TIMEOUT)."""
+        self._check(self._l.hl_inject_binning_stall(self._h, item, spins), "hl_inject_binning_stall")
 
     def set_pair_log(self, pairs=None, count=None):
         """Record the (pixel, light) pairs later shading launches light into ``pairs``

@@ -153,6 +153,18 @@ hl_status hl_bin_froxels(hl_ctx* ctx, const void* camera, const void* lights, ui
                          const hl_froxel_params* params, const hl_froxel_lists* out,
                          void* stream);
 
+/* Failure injection for the device-side wait of hl_bin_froxels (no reference
+ * counterpart). The single-launch binning splits the grid into work items (a froxel
+ * column, or a group of its slices) and finds where each item's lists start by
+ * polling the running totals that earlier items publish; each poll loop is bounded
+ * (about 0.1 s), after which the kernel reports HL_ERR_TIMEOUT through hl_sync_status
+ * and finishes instead of hanging. After this call, the context's next hl_bin_froxels
+ * runs with work item `item` withholding its total and the other items giving up after
+ * `spins` polls (1..2^20), so a test can trip the bound: the call reports
+ * HL_ERR_TIMEOUT, its lists are not valid, and the context stays usable (the next call
+ * bins normally). */
+hl_status hl_inject_binning_stall(hl_ctx* ctx, uint32_t item, uint32_t spins);
+
 /* Froxel clustering for callers that cannot allocate device memory. No counterpart in
  * the reference. hl_bin_froxels takes its scratch space from the context, which grows
  * it with cudaMalloc; a caller whose frame runs inside a CUDA stream capture (where

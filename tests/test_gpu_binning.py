@@ -163,3 +163,25 @@ def test_froxel_binning_replays_in_a_cuda_graph(ctx):
         o2, i2, _ = gpu_bin_froxels(ctx, w.camera.record, w.lights, other)  # a direct call in between
         o2w, i2w = oracle.bin_froxels(w.camera.record, w.lights, other, capacity=1 << 24)
         np.testing.assert_array_equal(o2, o2w)
+
+
+def test_froxel_bounded_wait_times_out_and_the_context_recovers(ctx):
+    """Failure detection of the single-launch binning: every work item finds where its
+    lists start by polling the running totals earlier items publish, and each poll
+    loop is bounded. With one item withholding its total (hl_inject_binning_stall),
+    the later items give up after the given number of polls: the call reports
+    HL_ERR_TIMEOUT through hl_sync_status instead of hanging, and the next call on the
+    same context bins normally, bit-exact."""
+    w = S.workload(1)
+    p = L.froxel_params(*w.froxel_grid, w.gbuffer.width, w.gbuffer.height, w.camera.far)
+    off_w, idx_w = oracle.bin_froxels(w.camera.record, w.lights, p, capacity=1 << 26)
+    cap = int(off_w[-1]) + 16
+    ctx.inject_binning_stall(item=5, spins=1024)
+    gpu_bin_froxels(ctx, w.camera.record, w.lights, p, capacity=cap, expect_status=N.HL_ERR_TIMEOUT)
+    for _ in range(2):
+        off, idx, _ = gpu_bin_froxels(ctx, w.camera.record, w.lights, p, capacity=cap)
+        np.testing.assert_array_equal(off, off_w)
+        np.testing.assert_array_equal(idx, idx_w)
+    with pytest.raises(N.HelioError) as e:
+        ctx.inject_binning_stall(item=0, spins=0)
+    assert e.value.status == N.HL_ERR_INVALID_ARGUMENT
