@@ -255,7 +255,7 @@ def _shadow_desc(shadows):
 def shade_forced(camera_rec, globals_rec, gb, lights, grid, lit_pairs, shadows=None, rows=None):
     """``shade`` (f64) with another evaluation's branch decisions: ``lit_pairs`` (K, 2)
     are the (y * W + x, light) pairs that evaluation lit (as hl_set_pair_log records
-    them). Those pairs are evaluated as lit whatever the f64 cuts decide, every other
+    them), or their forced_csr. Those pairs are evaluated as lit whatever the f64 cuts decide, every other
     listed pair contributes nothing, so the radiance is comparable at every pixel,
     including those where f32 and f64 fall on different sides of a cut. Returns
     (radiance, flips, unlisted): per pixel the number of listed pairs whose f64 decision
@@ -267,7 +267,7 @@ def shade_forced(camera_rec, globals_rec, gb, lights, grid, lit_pairs, shadows=N
     arrs, ptrs, pitch = _planes(gb)
     kind, lists, counts, params = _grid_args(grid)
     lts = np.ascontiguousarray(lights)
-    off, fls = forced_csr(lit_pairs, W * H)
+    off, fls = lit_pairs if isinstance(lit_pairs, tuple) else forced_csr(lit_pairs, W * H)
     if fls.size == 0:
         fls = np.zeros(1, np.uint32)
     desc, keep = _shadow_desc(shadows) if shadows is not None else (None, None)

@@ -229,3 +229,111 @@ def test_autograd_wrapper_matches_finite_differences(ctx):
         hh = float(pl_p[plane][y, x, comp]) - float(pl_m[plane][y, x, comp])
         fd = (f(lt, pl_p) - f(lt, pl_m)) / hh
         assert abs(fd - g_p[y, x, q]) <= 1e-3 * max(abs(fd), abs(g_p[y, x, q])) + 1e-6, ((y, x, q), fd, g_p[y, x, q])
+
+
+def test_autograd_matches_finite_differences_at_the_differentiation_workload():
+    """The differentiation workload at its own shape: 1920x1080 FP32 G-buffer, 256 point
+    lights, target rendered by the FP64 oracle with the lights moved by N(0, 0.5^2) per
+    axis and intensities scaled by U[0.8, 1.2], loss = sum((radiance - target)^2).
+    Gradients from DeferredShade.backward (hl_shade_adjoint) against FP64 central
+    differences (h = 1e-3) on 32 random parameters (16 light, 16 pixel). The FP64
+    forward holds the kernel's own branch decisions at the cuts of pbr_direct_light
+    (recorded with hl_set_pair_log), as the adjoint does, and evaluates only the rows a
+    parameter reaches. A parameter whose differences at h and h/2 disagree sits at a
+    kink of a clamp (range falloff, NdL, spot cone) and is replaced by another."""
+    import torch
+
+    from helio_gb300 import autograd as AG
+
+    w = S.workload(4)
+    cam, gb, lt, glb = w.camera, w.gbuffer, w.lights, w.globals_
+    W, H = gb.width, gb.height
+    p_np = L.froxel_params(*w.froxel_grid, W, H, cam.far)
+    moved = S.perturbed_lights(lt, 4500)
+    off_t, idx_t = oracle.bin_froxels(cam.record, moved, p_np, capacity=1 << 26)
+    tgt = np.nan_to_num(oracle.shade(cam.record, glb, gb, moved, ("froxels", idx_t, off_t, p_np)))[..., :3]
+
+    with N.Context(0) as ctx:
+        df = FR.upload(cam.record, glb, lt, gb)
+        normal = torch.from_numpy(gb.planes[1][..., :3].copy()).cuda()
+        depth = torch.from_numpy(gb.planes[2].copy()).cuda()
+        scene = AG.ShadeScene(ctx, df.camera, df.globals_, df.lights, normal, depth,
+                              N.froxel_params_from_numpy(p_np), capacity=1 << 24)
+        pp_np = np.concatenate([gb.planes[0], gb.planes[1][..., 3:4]], -1)
+        lp = AG.light_params_of(lt).cuda().requires_grad_(True)
+        pp = torch.from_numpy(pp_np.copy()).cuda().requires_grad_(True)
+        pairs_d = torch.zeros((W * H * 4, 2), dtype=torch.int32, device="cuda")
+        count = torch.zeros(1, dtype=torch.int32, device="cuda")
+        ctx.set_pair_log(pairs_d, count)
+        rad = AG.shade(lp, pp, scene)
+        ctx.set_pair_log(None)
+        loss = ((rad[..., :3] - torch.from_numpy(tgt.astype(np.float32)).cuda()) ** 2).sum()
+        loss.backward()
+        ctx.sync_status()
+        n = int(count.item())
+        assert n <= pairs_d.shape[0]
+        pairs = pairs_d[:n].cpu().numpy().view(np.uint32)
+        g_l = lp.grad.double().cpu().numpy()
+        g_p = pp.grad.double().cpu().numpy()
+
+    off, idx = oracle.bin_froxels(cam.record, lt, p_np, capacity=1 << 26)
+    grid = ("froxels", idx, off, p_np)
+    csr = oracle.forced_csr(pairs, W * H)
+    pix_of = pairs[:, 0].astype(np.int64)
+
+    def loss_rows(lights, planes, r0, r1):
+        r, _, unlisted = oracle.shade_forced(cam.record, glb, S.GBuffer(S.LAYOUT_F32, W, H, planes), lights, grid, csr,
+                                             rows=(r0, r1))
+        assert unlisted.sum() == 0
+        r = np.nan_to_num(r[r0:r1])[..., :3]
+        return float(((r - tgt[r0:r1]) ** 2).sum())
+
+    fields = [("position_range", 0), ("position_range", 1), ("position_range", 2), ("color_intensity", 3),
+              ("color_intensity", 0), ("color_intensity", 1), ("color_intensity", 2)]
+
+    def fd_light(li, q, h):
+        field, comp = fields[q]
+        ys = pix_of[pairs[:, 1] == li] // W
+        r0, r1 = int(ys.min()), int(ys.max()) + 1
+        v = float(lt[field][li, comp])
+        lp_, lm_ = lt.copy(), lt.copy()
+        lp_[field][li, comp] = np.float32(v + h)
+        lm_[field][li, comp] = np.float32(v - h)
+        hh = float(lp_[field][li, comp]) - float(lm_[field][li, comp])
+        return (loss_rows(lp_, gb.planes, r0, r1) - loss_rows(lm_, gb.planes, r0, r1)) / hh
+
+    def fd_pixel(y, x, q, h):
+        plane, comp = (0, q) if q < 4 else (1, 3)
+        v = float(gb.planes[plane][y, x, comp])
+        pl_p = [p.copy() for p in gb.planes]
+        pl_m = [p.copy() for p in gb.planes]
+        pl_p[plane][y, x, comp] = np.float32(v + h)
+        pl_m[plane][y, x, comp] = np.float32(v - h)
+        hh = float(pl_p[plane][y, x, comp]) - float(pl_m[plane][y, x, comp])
+        return (loss_rows(lt, pl_p, y, y + 1) - loss_rows(lt, pl_m, y, y + 1)) / hh
+
+    rng = np.random.default_rng(4)
+    h = 1e-3
+    lit_lights = np.unique(pairs[:, 1])
+    cand_l = [int(f) for f in rng.permutation(np.flatnonzero(np.abs(g_l).ravel() > 1e-3 * np.abs(g_l).max()))
+              if f // 7 in set(lit_lights.tolist())]
+    cand_p = rng.permutation(np.flatnonzero(np.abs(g_p).ravel() > 1e-3 * np.abs(g_p).max()))
+    checked = {"light": 0, "pixel": 0}
+    kinks = 0
+    for kind, cands in (("light", cand_l), ("pixel", cand_p)):
+        for flat in cands:
+            if checked[kind] == 16:
+                break
+            if kind == "light":
+                li, q = divmod(int(flat), 7)
+                fd, fd2, g = fd_light(li, q, h), fd_light(li, q, h / 2), g_l[li, q]
+            else:
+                y, x, q = np.unravel_index(int(flat), g_p.shape)
+                fd, fd2, g = fd_pixel(y, x, q, h), fd_pixel(y, x, q, h / 2), g_p[y, x, q]
+            if abs(fd - fd2) > 1e-4 * max(abs(fd), abs(fd2), 1e-12):
+                kinks += 1
+                continue
+            assert abs(fd - g) <= 1e-3 * max(abs(fd), abs(g)) + 1e-7, (kind, int(flat), fd, g)
+            checked[kind] += 1
+    assert checked == {"light": 16, "pixel": 16}, (checked, kinks)
+    assert kinks <= 16, kinks
