@@ -257,6 +257,34 @@ __device__ __noinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>
     __syncwarp();
 }
 
+// Light-space projection view of shadow debug mode 11 (deferred_lighting.wgsl:1066-1080):
+// the pixel's world position in f32 as the shader forms it (uv = frag / size, ndc,
+// inv_view_proj v / w), projected by the first shadow matrix; orange inside its
+// frustum (depth in red), dark blue outside. Correctly rounded operations in the
+// shader's order.
+__device__ __noinline__ float4 shadow_projection_view(const float* ivp, const float* m0, uint32_t x, uint32_t y,
+                                                      float W, float H, float depth) {
+    const float ux = xdiv(xadd(float(x), 0.5f), W), uy = xdiv(xadd(float(y), 0.5f), H);
+    const float nx = xsub(xmul(ux, 2.0f), 1.0f), ny = xsub(1.0f, xmul(uy, 2.0f));
+    const float hw = xmat_row(ivp, 3, nx, ny, depth, 1.0f);
+    const float wx = xdiv(xmat_row(ivp, 0, nx, ny, depth, 1.0f), hw);
+    const float wy = xdiv(xmat_row(ivp, 1, nx, ny, depth, 1.0f), hw);
+    const float wz = xdiv(xmat_row(ivp, 2, nx, ny, depth, 1.0f), hw);
+    float m[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) m[k] = __ldg(m0 + k);
+    const float lw = xmat_row(m, 3, wx, wy, wz, 1.0f);
+    if (lw > 0.001f) {
+        const float n0 = xdiv(xmat_row(m, 0, wx, wy, wz, 1.0f), lw);
+        const float n1 = xdiv(xmat_row(m, 1, wx, wy, wz, 1.0f), lw);
+        const float n2 = xdiv(xmat_row(m, 2, wx, wy, wz, 1.0f), lw);
+        const float u = xadd(xmul(n0, 0.5f), 0.5f), v = xadd(xmul(-n1, 0.5f), 0.5f);
+        if (u >= 0.0f && v >= 0.0f && u <= 1.0f && v <= 1.0f && n2 >= 0.0f && n2 <= 1.0f)
+            return make_float4(n2, xmul(n2, 0.3f), 0.0f, 1.0f);
+    }
+    return make_float4(0.0f, 0.0f, 0.2f, 1.0f);
+}
+
 // TW x TH = 512 (froxel grid) or 256 (tile grid) pixels, 256 threads.
 // One tile (bx, by) of one view; tabz: the view's slice boundaries (froxel grid).
 // PREFETCH: the kernel's grid is this view's tiles (bx, by); before the walk the CTA asks
@@ -581,7 +609,11 @@ __device__ __forceinline__ void shade_tile(
     const uint32_t debug_mode = glb->debug_mode;
     bool rc_ok = false;  // radiance-cascade GI bound and enabled
     if (EXT) rc_ok = sv->rc != nullptr && glb->has_rc_gi != 0u;
-    if (!STATS && t == 0 && ((glb->has_rc_gi != 0u && !rc_ok) || debug_mode == 10u || debug_mode == 11u))
+    const uint32_t lcount = glb->light_count;
+    bool shadows_bound = false;
+    if (EXT) shadows_bound = sv->dyn != nullptr;
+    // the light-space projection view (mode 11) needs the shadow matrices
+    if (!STATS && t == 0 && ((glb->has_rc_gi != 0u && !rc_ok) || (debug_mode == 11u && lcount > 0u && !shadows_bound)))
         raise_status(status, HL_ERR_NOT_SUPPORTED);
 #pragma unroll
     for (int k = 0; k < PPT; ++k) {
@@ -651,6 +683,39 @@ __device__ __forceinline__ void shade_tile(
         } else if (debug_mode == 5u) {
             c = make_float4(fma_(nxo, 0.5f, 0.5f), fma_(ny, 0.5f, 0.5f), fma_(nzo, 0.5f, 0.5f),
                             1.0f);
+        } else if (debug_mode == 10u) {
+            // shadow factor heatmap (deferred_lighting.wgsl:1049-1064): the mean shadow
+            // factor of the first light_count lights, 1 for a light without shadow maps
+            const uint32_t nl = min(lcount, n_lights);
+            float sum = 0.0f;
+            if (EXT && shadows_bound) {
+                // the pixel's world position rounded to f32, as the pair's shadow factor takes it
+                float wx = s.px[F_PX][i] + s.px[F_PLX][i], wy = s.px[F_PY][i] + s.px[F_PLY][i],
+                      wz = s.px[F_PZ][i] + s.px[F_PLZ][i];
+                if (!PRECISE) {
+                    float hx, hy, hz, lx, ly, lz;
+                    reconstruct<true, false>(cam->inv_view_proj, x, y, W, H, fabsf(s.px[F_DEPTH][i]), hx, hy, hz, lx,
+                                             ly, lz);
+                    wx = hx + lx;
+                    wy = hy + ly;
+                    wz = hz + lz;
+                }
+                const float4 csm = __ldg(reinterpret_cast<const float4*>(sv->csm));
+                for (uint32_t li = 0; li < nl; ++li) {
+                    const float4* gl = reinterpret_cast<const float4*>(lights + li);
+                    const float4 la = __ldg(gl + 0), lb = __ldg(gl + 1);
+                    const uint4 ld = __ldg(reinterpret_cast<const uint4*>(gl + 3));
+                    sum = xadd(sum, shadow_factor(*sv, li, la, lb, ld.x, ld.y, wx, wy, wz, nxo, ny, nzo,
+                                                  float(x) + 0.5f, float(y) + 0.5f, camx, camy, camz, csm));
+                }
+            } else {
+                for (uint32_t li = 0; li < nl; ++li) sum = xadd(sum, 1.0f);
+            }
+            sum = xadd(sum, float(lcount - nl));  // lights beyond the buffer: lit
+            const float sf = xdiv(sum, xmax(float(lcount), 1.0f));
+            c = make_float4(sf, sf, sf, 1.0f);
+        } else if (EXT && debug_mode == 11u && lcount > 0u && shadows_bound) {
+            c = shadow_projection_view(cam->inv_view_proj, sv->mats, x, y, W, H, fabsf(s.px[F_DEPTH][i]));
         }
         unsigned char* row = out.data + out.pitch * y;
         if (TARGET == HL_TARGET_RGBA32F) {

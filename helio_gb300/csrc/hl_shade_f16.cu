@@ -518,8 +518,9 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
 
     // ---- 5. output -----------------------------------------------------------------------
     __syncthreads();
-    const uint32_t debug_mode = glb->debug_mode;
-    if (t == 0 && (glb->has_rc_gi != 0u || debug_mode == 10u || debug_mode == 11u))
+    const uint32_t debug_mode = glb->debug_mode, lcount = glb->light_count;
+    // without shadow maps bound, the light-space projection view (mode 11) has no matrix
+    if (t == 0 && (glb->has_rc_gi != 0u || (debug_mode == 11u && lcount > 0u)))
         raise_status(status, HL_ERR_NOT_SUPPORTED);
     const float amb = glb->ambient_intensity;
     const float skr = glb->ambient_color[0] * amb, skg = glb->ambient_color[1] * amb,
@@ -549,6 +550,11 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
             c = make_float4(ar, ag, ab, 1.0f);
         } else if (debug_mode == 5u) {
             c = make_float4(fma_(rn.x, 0.5f, 0.5f), fma_(ny, 0.5f, 0.5f), fma_(rn.z, 0.5f, 0.5f), 1.0f);
+        } else if (debug_mode == 10u) {
+            // shadow factor heatmap (deferred_lighting.wgsl:1049-1064): without shadow maps
+            // every light's factor is 1, so the mean is 1 (0 with no light)
+            const float sf = lcount > 0u ? 1.0f : 0.0f;
+            c = make_float4(sf, sf, sf, 1.0f);
         }
         unsigned char* row = out.data + out.pitch * y;
         if (TARGET == HL_TARGET_RGBA32F) {

@@ -717,6 +717,50 @@ void shade_impl(const void* camera, const void* globals, const GBufferDesc& g, c
                 o[0] = double(s.albedo.x); o[1] = double(s.albedo.y); o[2] = double(s.albedo.z); o[3] = double(s.alpha);
             } else if (dm == 5) {
                 o[0] = double(N.x * T(0.5) + T(0.5)); o[1] = double(N.y * T(0.5) + T(0.5)); o[2] = double(N.z * T(0.5) + T(0.5)); o[3] = 1.0;
+            } else if (dm == 10) {
+                // shadow factor heatmap (deferred_lighting.wgsl:1049-1064): the mean of
+                // shadow_factor over the first light_count lights (1 without shadow maps)
+                const uint32_t nl = gl.light_count < n_lights ? gl.light_count : n_lights;
+                float sum = 0.0f;
+                for (uint32_t i = 0; i < nl; ++i) {
+                    float sf = 1.0f;
+                    if (shadows) {
+                        const RawLight& l = L[i];
+                        sf = float(shadow_oracle::shadow_factor<T>(*shadows, i, l.pos, l.dir, l.shadow_index, l.type,
+                                                                   P.x, P.y, P.z, N.x, N.y, N.z, float(x) + 0.5f,
+                                                                   float(y) + 0.5f, c.pos.x, c.pos.y, c.pos.z,
+                                                                   gl.csm_splits, shadow_bounds));
+                    }
+                    sum = sum + sf;
+                }
+                sum = sum + float(gl.light_count - nl);  // lights beyond the buffer: lit
+                const float cnt = float(gl.light_count);
+                const float sf = sum / (cnt < 1.0f ? 1.0f : cnt);
+                o[0] = o[1] = o[2] = double(sf);
+                o[3] = 1.0;
+            } else if (dm == 11 && gl.light_count > 0u && shadows) {
+                // light-space projection by the first shadow matrix (:1066-1080), in f32
+                // with the shader's operations in order (uv = frag / size, ndc, M v / w)
+                const float fw = float(W), fh = float(H);
+                const float ux = (float(x) + 0.5f) / fw, uy = (float(y) + 0.5f) / fh;
+                const float nx = ux * 2.0f - 1.0f, ny = 1.0f - uy * 2.0f;
+                float ivp[16], h[4], lc[4];
+                const RawCamera* rc = static_cast<const RawCamera*>(camera);
+                for (int k = 0; k < 16; ++k) ivp[k] = rc->inv_view_proj[k];
+                mat4_mul<float>(ivp, nx, ny, float(s.depth), 1.0f, h);
+                const float wx = h[0] / h[3], wy = h[1] / h[3], wz = h[2] / h[3];
+                mat4_mul<float>(shadows->mats, wx, wy, wz, 1.0f, lc);
+                float r[4] = {0.0f, 0.0f, 0.2f, 1.0f};
+                if (lc[3] > 0.001f) {
+                    const float n0 = lc[0] / lc[3], n1 = lc[1] / lc[3], n2 = lc[2] / lc[3];
+                    const float u = n0 * 0.5f + 0.5f, v = -n1 * 0.5f + 0.5f;
+                    if (u >= 0.0f && v >= 0.0f && u <= 1.0f && v <= 1.0f && n2 >= 0.0f && n2 <= 1.0f) {
+                        r[0] = n2;
+                        r[1] = n2 * 0.3f;
+                        r[2] = 0.0f;
+                    }
+                }
+                for (int k = 0; k < 4; ++k) o[k] = double(r[k]);
             } else {
                 o[0] = double(color.x); o[1] = double(color.y); o[2] = double(color.z); o[3] = double(s.alpha);
             }

@@ -245,3 +245,55 @@ def test_rc_gi_off_or_unbound(ctx):
         ctx.shade_ex(dfo.camera, dfo.globals_, dfo.gbuffer, dfo.lights, dfo.n_lights, dgrid, N.target_struct(out),
                      rc=small)
     assert e.value.status == N.HL_ERR_SIZE
+
+
+@pytest.mark.parametrize("layout", [S.LAYOUT_F32, S.LAYOUT_REFERENCE, S.LAYOUT_F16])
+def test_shadow_debug_modes(ctx, layout):
+    """Debug mode 10 (the mean shadow factor of the first light_count lights) and mode
+    11 (the light-space projection by the first shadow matrix) of fs_main
+    (deferred_lighting.wgsl:1049-1080), with shadow maps bound. Mode 11 is computed in
+    f32 with the shader's operations in order: bit-exact against the f32 restatement.
+    Mode 10 sums per-light shadow factors: exact except where a shadow tap flips."""
+    cam, gb, sc, dyn, sta, glb0 = _setup(layout, "medium")
+    W, H = gb.width, gb.height
+    ogrid, dgrid, keep = _froxel_grid(cam, sc.lights, W, H)
+    dsh, maps = _device_shadows(sc, dyn, sta)
+    shadows = dict(dynamic=dyn, static=sta, matrices=sc.matrices, config=sc.config, max_lights=sc.max_lights)
+    for mode in (10, 11):
+        glb = L.make_globals(L.tile_grid(W, H)[0], len(sc.lights), debug_mode=mode)
+        df = FR.upload(cam.record, glb, sc.lights, gb)
+        img = _shade_shadowed(ctx, df, dgrid, maps)
+        ref, _, _ = oracle.shade_shadowed(cam.record, glb, gb, sc.lights, ogrid, shadows)
+        m = ~np.isnan(ref[..., 0])
+        if mode == 11:
+            assert np.array_equal(img[m], ref[m])
+            inside = img[m][:, 2] == 0.0
+            assert inside.any() and not inside.all(), "the first shadow frustum should cover part of the view"
+        else:
+            assert np.all(img[m][:, 3] == 1.0) and np.all(img[m][:, 0] == img[m][:, 1])
+            d = np.abs(img[m][:, 0] - ref[m][:, 0])
+            assert (d > 1e-6).mean() <= 5e-3, (d > 1e-6).mean()
+            assert d.max() <= 1.0 / len(sc.lights) + 1e-6  # at most one light's factor apart
+            assert (ref[m][:, 0] < 1.0).mean() > 0.1, "some pixels should be in shadow"
+
+
+def test_shadow_debug_modes_without_shadow_maps(ctx):
+    """hl_shade binds no shadow maps: every light's shadow factor is 1, so mode 10 is
+    white (black with no light); mode 11 has no shadow matrix to project with and is
+    reported as not supported."""
+    W, H = 160, 96
+    cam = S.default_camera(W, H)
+    gb = S.make_gbuffer(cam, S.LAYOUT_F16, seed=5)
+    lt = mixed_lights(cam, 5, 30, 10)
+    ogrid, dgrid, keep = _froxel_grid(cam, lt, W, H)
+    for n, want in ((len(lt), 1.0), (0, 0.0)):
+        glb = L.make_globals(L.tile_grid(W, H)[0], n, debug_mode=10)
+        df = FR.upload(cam.record, glb, lt, gb)
+        img = gpu_shade(ctx, df, dgrid)
+        m = gb.planes[-1] < 1.0
+        assert np.all(img[m][:, :3] == want) and np.all(img[m][:, 3] == 1.0)
+    glb = L.make_globals(L.tile_grid(W, H)[0], len(lt), debug_mode=11)
+    df = FR.upload(cam.record, glb, lt, gb)
+    with pytest.raises(N.HelioError) as e:
+        gpu_shade(ctx, df, dgrid)
+    assert e.value.status == N.HL_ERR_NOT_SUPPORTED
