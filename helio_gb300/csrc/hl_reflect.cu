@@ -26,6 +26,14 @@ using namespace sm;
 
 constexpr uint32_t kRefThreadsX = 32, kRefThreadsY = 8;
 
+// The reflection captures and their cube-map array (hl_reflection_env).
+struct EnvView {
+    const unsigned char* caps;    // GpuReflectionCapture[count], 112 B each; nullptr: none bound
+    const unsigned char* texels;  // RGBA16F, layer-major, 6 faces, each face's mip chain
+    uint32_t count, size, levels, layers;
+    uint64_t chain;               // texels of one face's mip chain
+};
+
 struct ReflectParams {
     GBufView gb;
     TargetView out;
@@ -38,6 +46,7 @@ struct ReflectParams {
     const unsigned char* lmuv;
     uint64_t lmuv_pitch;
     ExtView rc;  // rc.rc == nullptr: no probes bound
+    EnvView env;
     int* status;
 };
 
@@ -85,6 +94,143 @@ __device__ __forceinline__ void store_target(unsigned char* o, const TargetTexel
     }
 }
 
+// One level of one cube layer sampled as the pass's env sampler does: the face of the
+// direction's major axis (ties to z, then y), the face coordinates of the Vulkan /
+// WebGPU cube-map table, bilinear within the face with the edge texels clamped.
+__device__ __forceinline__ void cube_sample(const EnvView& e, float dx, float dy, float dz, uint32_t layer,
+                                            uint32_t level, float& r, float& g, float& b) {
+    const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+    uint32_t face;
+    float sc, tc, ma;
+    if (az >= ax && az >= ay) {
+        face = dz >= 0.0f ? 4u : 5u;
+        sc = dz >= 0.0f ? dx : -dx;
+        tc = -dy;
+        ma = az;
+    } else if (ay >= ax) {
+        face = dy >= 0.0f ? 2u : 3u;
+        sc = dx;
+        tc = dy >= 0.0f ? dz : -dz;
+        ma = ay;
+    } else {
+        face = dx >= 0.0f ? 0u : 1u;
+        sc = dx >= 0.0f ? -dz : dz;
+        tc = -dy;
+        ma = ax;
+    }
+    const float sf = ma > 0.0f ? 0.5f * (sc / ma + 1.0f) : 0.5f, tf = ma > 0.0f ? 0.5f * (tc / ma + 1.0f) : 0.5f;
+    const uint32_t n = max(1u, e.size >> level);
+    uint64_t off = 0;
+    for (uint32_t m = 0; m < level; ++m) {
+        const uint64_t nm = max(1u, e.size >> m);
+        off += nm * nm;
+    }
+    const unsigned char* base = e.texels + 8ull * ((uint64_t(layer) * 6u + face) * e.chain + off);
+    const float u = sf * float(n) - 0.5f, v = tf * float(n) - 0.5f;
+    const float fu = floorf(u), fv = floorf(v);
+    const float wu = u - fu, wv = v - fv;
+    const int iu = int(fu), iv = int(fv), top = int(n) - 1;
+    const int u0 = min(max(iu, 0), top), u1 = min(max(iu + 1, 0), top);
+    const int v0 = min(max(iv, 0), top), v1 = min(max(iv + 1, 0), top);
+    const float4 t00 = load_h4(base + 8ull * (uint64_t(v0) * n + u0)), t01 = load_h4(base + 8ull * (uint64_t(v0) * n + u1));
+    const float4 t10 = load_h4(base + 8ull * (uint64_t(v1) * n + u0)), t11 = load_h4(base + 8ull * (uint64_t(v1) * n + u1));
+    r = (t00.x * (1.0f - wu) + t01.x * wu) * (1.0f - wv) + (t10.x * (1.0f - wu) + t11.x * wu) * wv;
+    g = (t00.y * (1.0f - wu) + t01.y * wu) * (1.0f - wv) + (t10.y * (1.0f - wu) + t11.y * wu) * wv;
+    b = (t00.z * (1.0f - wu) + t01.z * wu) * (1.0f - wv) + (t10.z * (1.0f - wu) + t11.z * wu) * wv;
+}
+
+// The 16 floats of a column-major mat4 times (x, y, z, w), row r.
+__device__ __forceinline__ float mrow(const float* m, int r, float x, float y, float z, float w) {
+    return m[r] * x + m[4 + r] * y + m[8 + r] * z + m[12 + r] * w;
+}
+
+// sample_reflection_environment (deferred_lighting.wgsl:646-694) with capture_weight
+// (:618-638), parallax_box (:596-616) and parallax_sphere (:575-588).
+__device__ __noinline__ float3 reflection_environment(const EnvView& e, uint32_t count, float Px, float Py, float Pz,
+                                                      float Rx, float Ry, float Rz, float lod, int* status) {
+    // the env sampler's nearest level: ceil(lod + 0.5) - 1, within the chain
+    const int lvl = int(ceilf(lod + 0.5f)) - 1;
+    const uint32_t level = uint32_t(min(max(lvl, 0), int(e.levels) - 1));
+    float ar = 0.0f, ag = 0.0f, ab = 0.0f, acc = 0.0f;
+    const uint32_t n = min(min(count, 64u), e.count);
+    for (uint32_t i = 0; i < n; ++i) {
+        if (acc >= 0.999f) break;
+        const float* c = reinterpret_cast<const float*>(e.caps + 112ull * i);
+        const float4 pr = __ldg(reinterpret_cast<const float4*>(c));
+        const float4 et = __ldg(reinterpret_cast<const float4*>(c + 4));
+        float m[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) m[k] = __ldg(c + 8 + k);
+        const int layer = __ldg(reinterpret_cast<const int*>(c + 24));
+        const uint32_t shape = __ldg(reinterpret_cast<const uint32_t*>(c + 25));
+        const float brightness = __ldg(c + 27);
+        if (layer < 0) continue;  // no cubemap resident
+        if (uint32_t(layer) >= e.layers) {
+            raise_status(status, HL_ERR_DEVICE_BOUNDS);
+            continue;
+        }
+        float w;
+        if (shape == 1u) {  // box: the distance inside the nearest pair of faces over the transition
+            const float lx = mrow(m, 0, Px, Py, Pz, 1.0f), ly = mrow(m, 1, Px, Py, Pz, 1.0f),
+                        lz = mrow(m, 2, Px, Py, Pz, 1.0f);
+            const float gx = et.x - fabsf(lx), gy = et.y - fabsf(ly), gz = et.z - fabsf(lz);
+            w = (gx < 0.0f || gy < 0.0f || gz < 0.0f)
+                    ? 0.0f
+                    : fminf(fmaxf(fminf(fminf(gx, gy), gz) / fmaxf(et.w, 1e-4f), 0.0f), 1.0f);
+        } else {  // sphere: fade over the outer 10 % of the radius
+            const float ox = Px - pr.x, oy = Py - pr.y, oz = Pz - pr.z;
+            const float dist = sqrtf(ox * ox + oy * oy + oz * oz);
+            w = dist > pr.w ? 0.0f : fminf(fmaxf((pr.w - dist) / fmaxf(pr.w * 0.1f, 1e-4f), 0.0f), 1.0f);
+        }
+        if (w <= 0.0f) continue;
+        float dx = Rx, dy = Ry, dz = Rz;
+        if (shape == 1u) {
+            const float plx = mrow(m, 0, Px, Py, Pz, 1.0f), ply = mrow(m, 1, Px, Py, Pz, 1.0f),
+                        plz = mrow(m, 2, Px, Py, Pz, 1.0f);
+            const float rlx = mrow(m, 0, Rx, Ry, Rz, 0.0f), rly = mrow(m, 1, Rx, Ry, Rz, 0.0f),
+                        rlz = mrow(m, 2, Rx, Ry, Rz, 0.0f);
+            const float ix = 1.0f / rlx, iy = 1.0f / rly, iz = 1.0f / rlz;
+            const float tx = fmaxf((-et.x - plx) * ix, (et.x - plx) * ix);
+            const float ty = fmaxf((-et.y - ply) * iy, (et.y - ply) * iy);
+            const float tz = fmaxf((-et.z - plz) * iz, (et.z - plz) * iz);
+            const float t = fminf(fminf(tx, ty), tz);
+            if (t > 0.0f && t < 3.402823e38f) {
+                dx = (Px + Rx * t) - pr.x;
+                dy = (Py + Ry * t) - pr.y;
+                dz = (Pz + Rz * t) - pr.z;
+            }
+        } else {
+            const float ox = Px - pr.x, oy = Py - pr.y, oz = Pz - pr.z;
+            const float bb = ox * Rx + oy * Ry + oz * Rz;
+            const float cc = (ox * ox + oy * oy + oz * oz) - pr.w * pr.w;
+            const float disc = bb * bb - cc;
+            if (disc >= 0.0f) {
+                const float t = -bb + sqrtf(disc);
+                if (t > 0.0f) {
+                    dx = (Px + Rx * t) - pr.x;
+                    dy = (Py + Ry * t) - pr.y;
+                    dz = (Pz + Rz * t) - pr.z;
+                }
+            }
+        }
+        float sr, sg, sb;
+        cube_sample(e, dx, dy, dz, uint32_t(layer), level, sr, sg, sb);
+        const float contrib = w * (1.0f - acc);
+        ar += sr * brightness * contrib;
+        ag += sg * brightness * contrib;
+        ab += sb * brightness * contrib;
+        acc += contrib;
+    }
+    if (acc < 0.999f) {  // layer 0 as the skylight, along R
+        float sr, sg, sb;
+        cube_sample(e, Rx, Ry, Rz, 0u, level, sr, sg, sb);
+        ar += sr * (1.0f - acc);
+        ag += sg * (1.0f - acc);
+        ab += sb * (1.0f - acc);
+    }
+    return make_float3(ar, ag, ab);
+}
+
 __device__ __forceinline__ float smoothstep_(float lo, float hi, float x) {
     const float t = fminf(fmaxf((x - lo) / (hi - lo), 0.0f), 1.0f);
     return t * t * (3.0f - 2.0f * t);
@@ -123,7 +269,8 @@ __global__ void __launch_bounds__(kRefThreadsX* kRefThreadsY, 3)
     const float rough = t.rough;
     const bool want_rc = rc_on && rough > 0.6f;
     const bool use_ssr = refl_on && ssr.w > 0.0f, use_pl = refl_on && pl.w > 0.0f;
-    if (!use_ssr && !use_pl && !want_rc) return;  // nothing to add: the target keeps its bits
+    const bool use_env = p.env.caps != nullptr && refl_on && __ldg(&glb->enable_env_reflections) != 0u;
+    if (!use_ssr && !use_pl && !want_rc && !use_env) return;  // nothing to add: the target keeps its bits
 
     // N, F0 (:1287-1295); lightmap sentinel (:1300-1303)
     const float nn = sqrtf(t.nx * t.nx + t.ny * t.ny + t.nz * t.nz);
@@ -154,6 +301,20 @@ __global__ void __launch_bounds__(kRefThreadsX* kRefThreadsY, 3)
     for (int k = 0; k < 3; ++k) F[k] = f0[k] + (fmaxf(1.0f - rough, f0[k]) - f0[k]) * p5;  // pbr_eval.wgsl:63-66
 
     float spec[3] = {0.0f, 0.0f, 0.0f};  // the environment term under the black fallback cube
+    if (use_env) {
+        // R = reflect(-V, N) (:1311); spec = env (F0 env_brdf.x + env_brdf.y) (:1313-1318)
+        const float Rx = 2.0f * nv * Nx - Vx, Ry = 2.0f * nv * Ny - Vy, Rz = 2.0f * nv * Nz - Vz;
+        const float3 env = reflection_environment(p.env, __ldg(&glb->reflection_capture_count), Px + Plx, Py + Ply,
+                                                  Pz + Plz, Rx, Ry, Rz, rough * 8.0f, p.status);
+        // env_brdf_approx (pbr_eval.wgsl:70-76)
+        const float r0 = rough * -1.0f + 1.0f, r1 = rough * -0.0275f + 0.0425f, r2 = rough * -0.572f + 1.04f,
+                    r3 = rough * 0.022f - 0.04f;
+        const float a004 = fminf(r0 * r0, exp2f(-9.28f * ndv)) * r0 + r1;
+        const float bx = -1.04f * a004 + r2, by = 1.04f * a004 + r3;
+        spec[0] = env.x * (f0[0] * bx + by);
+        spec[1] = env.y * (f0[1] * bx + by);
+        spec[2] = env.z * (f0[2] * bx + by);
+    }
     if (use_ssr) {
         const float s[3] = {ssr.x, ssr.y, ssr.z};
 #pragma unroll
@@ -249,6 +410,28 @@ extern "C" hl_status hl_shade_reflections(hl_ctx* ctx, const void* camera, const
                             rc->height, (unsigned long long)rc->pitch, need_w, need_h);
             p.rc.rc = static_cast<const unsigned char*>(rc->texels);
             p.rc.rc_pitch = rc->pitch;
+        }
+        if (const hl_reflection_env* env = inputs->env) {
+            if (!env->captures || !env->texels)
+                return fail(ctx, HL_ERR_INVALID_ARGUMENT, "reflection env: captures or texels NULL");
+            if (!aligned(env->captures, 16) || !aligned(env->texels, 8))
+                return fail(ctx, HL_ERR_LAYOUT, "reflection env: captures need 16-byte, texels 8-byte alignment");
+            if (env->face_size == 0 || env->face_size > 16384 || env->mip_levels == 0 || env->mip_levels > 15 ||
+                env->layers == 0 || env->layers > 65536)
+                return fail(ctx, HL_ERR_SIZE, "reflection env: face %u, %u levels, %u layers", env->face_size,
+                            env->mip_levels, env->layers);
+            uint64_t chain = 0;
+            for (uint32_t m = 0; m < env->mip_levels; ++m) {
+                const uint64_t n = std::max<uint64_t>(1, env->face_size >> m);
+                chain += n * n;
+            }
+            p.env.caps = static_cast<const unsigned char*>(env->captures);
+            p.env.texels = static_cast<const unsigned char*>(env->texels);
+            p.env.count = env->count;
+            p.env.size = env->face_size;
+            p.env.levels = env->mip_levels;
+            p.env.layers = env->layers;
+            p.env.chain = chain;
         }
     }
     p.camera = static_cast<const hl::GpuCamera*>(camera);

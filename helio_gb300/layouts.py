@@ -279,6 +279,24 @@ SHADOW_MAPS = np.dtype(
 )
 # hl_rc_cascade (include/helio_gb300.h): the radiance-cascade probe texture rc_cascade0
 RC_CASCADE = np.dtype([("texels", "<u8"), ("pitch", "<u8"), ("width", "<u4"), ("height", "<u4")])
+
+# GpuReflectionCapture (libhelio/src/reflection.rs:64-80): the captures the reflection
+# draw blends (deferred_lighting.wgsl:189-198)
+REFLECTION_CAPTURE = np.dtype(
+    [
+        ("position_radius", "<f4", (4,)),
+        ("extents_transition", "<f4", (4,)),
+        ("world_to_local", "<f4", (16,)),  # column major
+        ("cubemap_index", "<i4"),
+        ("shape", "<u4"),  # 0 sphere, 1 box
+        ("mobility", "<u4"),
+        ("brightness", "<f4"),
+    ]
+)
+CAPTURE_SPHERE, CAPTURE_BOX = 0, 1
+# hl_reflection_env: captures and their cube-map array (texels RGBA16F)
+REFLECTION_ENV = np.dtype([("captures", "<u8"), ("count", "<u4"), ("face_size", "<u4"), ("mip_levels", "<u4"),
+                           ("layers", "<u4"), ("texels", "<u8")])
 RC_PROBE_DIM, RC_DIR_DIM = 16, 4  # deferred_lighting.wgsl:824-825
 
 SHADOW_ATLAS_SIZE = 1024  # the shader's ATLAS_SIZE (deferred_lighting.wgsl:235)
@@ -330,6 +348,8 @@ EXPECTED_SIZES = {
     "SHADOW_CONFIG": 80,
     "SHADOW_MAPS": 48,
     "RC_CASCADE": 24,
+    "REFLECTION_CAPTURE": 112,
+    "REFLECTION_ENV": 32,
 }
 
 for _name, _size in EXPECTED_SIZES.items():

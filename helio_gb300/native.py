@@ -113,12 +113,18 @@ class ShadeBindings(C.Structure):
     _fields_ = [("shadows", C.POINTER(ShadowMaps)), ("rc", C.POINTER(RcCascade))]
 
 
+class ReflectionEnv(C.Structure):
+    """hl_reflection_env: reflection captures and their pre-filtered cube-map array."""
+    _fields_ = [("captures", C.c_void_p), ("count", C.c_uint32), ("face_size", C.c_uint32),
+                ("mip_levels", C.c_uint32), ("layers", C.c_uint32), ("texels", C.c_void_p)]
+
+
 class ReflectionInputs(C.Structure):
-    """hl_reflection_inputs: SSR and planar hit images (RGBA16F), lightmap UVs (RG16F) and
-    radiance-cascade probes, each optional (NULL)."""
+    """hl_reflection_inputs: SSR and planar hit images (RGBA16F), lightmap UVs (RG16F),
+    radiance-cascade probes and the capture environment, each optional (NULL)."""
     _fields_ = [("ssr", C.c_void_p), ("ssr_pitch", C.c_uint64), ("planar", C.c_void_p),
                 ("planar_pitch", C.c_uint64), ("lightmap_uv", C.c_void_p), ("lightmap_uv_pitch", C.c_uint64),
-                ("rc", C.POINTER(RcCascade))]
+                ("rc", C.POINTER(RcCascade)), ("env", C.POINTER(ReflectionEnv))]
 
 
 class GBufferTargets(C.Structure):
@@ -347,15 +353,17 @@ class Context:
                     "hl_shade_ex")
 
     def shade_reflections(self, camera, globals_, gbuffer: GBuffer, target: Target, ssr=None, planar=None,
-                          lightmap_uv=None, rc: "RcCascade" = None, stream=None):
+                          lightmap_uv=None, rc: "RcCascade" = None, env: "ReflectionEnv" = None, stream=None):
         """The reflection draw (fs_reflection) added over ``target``; ``ssr`` / ``planar``:
-        device float16 tensors (H, W, 4), ``lightmap_uv``: (H, W, 2), each optional."""
+        device float16 tensors (H, W, 4), ``lightmap_uv``: (H, W, 2), ``env``: captures
+        and cube array (reflection_env_struct), each optional."""
         inp = ReflectionInputs()
         for name, t in (("ssr", ssr), ("planar", planar), ("lightmap_uv", lightmap_uv)):
             if t is not None:
                 setattr(inp, name, _ptr(t))
                 setattr(inp, name + "_pitch", int(t.stride(0) * t.element_size()))
         inp.rc = C.pointer(rc) if rc is not None else None
+        inp.env = C.pointer(env) if env is not None else None
         self._check(self._l.hl_shade_reflections(self._h, _ptr(camera), _ptr(globals_), C.byref(gbuffer),
                                                  C.byref(inp), C.byref(target), _stream(stream)),
                     "hl_shade_reflections")
@@ -499,6 +507,13 @@ def shadow_maps_struct(dynamic, static, matrices, config, max_shadow_lights: int
     m.layers, m.size = int(dynamic.shape[0]), int(dynamic.shape[1])
     m.max_shadow_lights = max_shadow_lights
     return m
+
+
+def reflection_env_struct(captures, n_captures: int, texels, face_size: int, mip_levels: int,
+                          layers: int) -> ReflectionEnv:
+    """hl_reflection_env over device tensors: ``captures`` (n x 112 bytes), ``texels``
+    (RGBA16F cube array, layer-major, 6 faces, each face's mip chain)."""
+    return ReflectionEnv(_ptr(captures), n_captures, face_size, mip_levels, layers, _ptr(texels))
 
 
 def rc_cascade_struct(texels) -> RcCascade:

@@ -759,3 +759,34 @@ def reflection_images(width: int, height: int, seed: int):
     lm[k == 0] = -1.0
     lm[k == 1] = -2.0
     return ssr.astype(np.float16), planar.astype(np.float16), lm.astype(np.float16)
+
+
+def reflection_env(seed: int, face_size: int = 16, mip_levels: int = 5, layers: int = 5, n_captures: int = 6):
+    """Reflection captures and their cube-map array for the reflection draw's
+    environment term: a dict with ``captures`` (REFLECTION_CAPTURE records: spheres and
+    oriented boxes of radius / half-extent 10-35 placed in front of the default camera,
+    cubemap layers 1.., one capture without a cubemap), ``texels`` (float16 RGBA cube
+    array, layer-major, 6 faces, each face's mip chain; radiance in [0, 3), alpha 1),
+    ``face_size``, ``mip_levels`` and ``layers`` (layer 0 is the skylight)."""
+    rng = np.random.default_rng(seed)
+    chain = sum(max(1, face_size >> m) ** 2 for m in range(mip_levels))
+    texels = np.ones((layers * 6 * chain, 4), np.float32)
+    texels[:, :3] = rng.uniform(0.0, 3.0, (layers * 6 * chain, 3))
+    caps = np.zeros(n_captures, L.REFLECTION_CAPTURE)
+    for i in range(n_captures):
+        centre = np.array([rng.uniform(-25, 25), rng.uniform(-12, 12), rng.uniform(-90, -10)])
+        box = i % 2 == 1
+        caps[i]["position_radius"] = (*centre, rng.uniform(10.0, 35.0))
+        caps[i]["cubemap_index"] = 1 + i % (layers - 1) if i != n_captures - 1 else -1
+        caps[i]["shape"] = L.CAPTURE_BOX if box else L.CAPTURE_SPHERE
+        caps[i]["brightness"] = rng.uniform(0.5, 2.0)
+        m = np.eye(4)
+        if box:
+            a = rng.uniform(0.0, 2.0 * math.pi)
+            rot = np.array([[math.cos(a), 0.0, math.sin(a)], [0.0, 1.0, 0.0], [-math.sin(a), 0.0, math.cos(a)]])
+            m[:3, :3] = rot.T
+            m[:3, 3] = -rot.T @ centre
+            caps[i]["extents_transition"] = (*rng.uniform(8.0, 30.0, 3), rng.uniform(0.5, 4.0))
+        caps[i]["world_to_local"] = m.T.reshape(16).astype(np.float32)  # column major
+    return dict(captures=caps, texels=texels.astype(np.float16), face_size=face_size, mip_levels=mip_levels,
+                layers=layers)

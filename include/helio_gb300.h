@@ -338,6 +338,29 @@ hl_status hl_shade_ex(hl_ctx* ctx, const void* camera, const void* globals, cons
  *               no-lightmap sentinel (-1, -1) (gbuffer.wgsl:245)
  *   rc          the radiance-cascade probes for the rough-specular fallback.
  * Pitches in bytes; ssr, planar and the rc texels 8-byte aligned, lightmap_uv 4. */
+/* Reflection captures and the pre-filtered cube-map array they sample: the pass's
+ * reflection_captures and env_cube bindings (deferred_lighting.wgsl:163-198).
+ *   captures : device GpuReflectionCapture[count] (112 B: position_radius, extents_transition,
+ *              world_to_local (column major), cubemap_index (i32, -1: none), shape (0 sphere,
+ *              1 box), mobility, brightness; libhelio/src/reflection.rs:64-80), in the order
+ *              the scene uploads them; globals.reflection_capture_count (at most 64) of them
+ *              are read
+ *   texels   : device RGBA16F, 8-byte aligned: layer-major, each layer 6 faces (+x, -x, +y, -y,
+ *              +z, -z), each face its mip chain from level 0, level m a row-major square of
+ *              max(1, face_size >> m) texels. Layer 0 is the skylight.
+ * Sampling follows the pass's env sampler (linear within a level, nearest level, clamp to
+ * edge): the face of the direction's major axis, bilinear within that face with its edge
+ * texels clamped (not blended across faces), level round(lod) clamped to the chain. */
+#define HL_SIZEOF_REFLECTION_CAPTURE 112u
+typedef struct hl_reflection_env {
+    const void* captures;
+    uint32_t count;        /* entries in captures                         */
+    uint32_t face_size;    /* texels per side of level 0, 1..16384        */
+    uint32_t mip_levels;   /* levels per face, 1..15                      */
+    uint32_t layers;       /* cube layers, >= 1                           */
+    const void* texels;
+} hl_reflection_env;
+
 typedef struct hl_reflection_inputs {
     const void* ssr;
     uint64_t ssr_pitch;
@@ -346,13 +369,19 @@ typedef struct hl_reflection_inputs {
     const void* lightmap_uv;
     uint64_t lightmap_uv_pitch;
     const hl_rc_cascade* rc;
+    const hl_reflection_env* env; /* NULL: the pass's black fallback cube, no captures */
 } hl_reflection_inputs;
 
 /* The indirect specular of fs_reflection (deferred_lighting.wgsl:1265-1341), added to
  * `radiance` as the pass's additive second draw does (colour One + One, alpha kept;
  * deferred-light/src/lib.rs:448-489): for every pixel with depth < 1,
- *   spec = 0 (the environment term under the pass's fallback environment: no capture
- *          cubemaps are bound, so env_cube is the black fallback cube, lib.rs:542)
+ *   spec = env (F0 env_brdf.x + env_brdf.y)      when enable_env_reflections, else 0
+ *          with env = sample_reflection_environment(P, R, 8 roughness) (:646-694): the
+ *          captures covering P blended front to back by capture_weight, each sampled
+ *          along its sphere or box parallax direction times its brightness, the
+ *          skylight (layer 0, along R) filling the remaining coverage; 0 when
+ *          enable_reflections == 0 or inputs->env is NULL (the black fallback cube,
+ *          lib.rs:542); env_brdf = env_brdf_approx(NdV, roughness) (pbr_eval.wgsl:70-76)
  *   spec = mix(spec, ssr.rgb F_ibl, ssr.a)       when enable_reflections and ssr.a > 0
  *   spec = mix(spec, planar.rgb F_ibl, planar.a) when enable_reflections and planar.a > 0
  *   spec = mix(spec, rc_specular, smoothstep(0.6, 0.9, r) 0.4)  when has_rc_gi, r > 0.6

@@ -68,7 +68,7 @@ def _bind(l):
     l.oracle_shade_forced_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, vp, u32p,
                                           u32p, f64p, u32p, u32, u32, vp]
     l.oracle_reflections_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, C.c_uint64, vp, C.c_uint64, vp,
-                                         C.c_uint64, vp, f64p, vp]
+                                         C.c_uint64, vp, vp, f64p, vp]
     l.oracle_shade_adjoint_f64.argtypes = [vp, vp, u32, u32, u32, vp, u64p, vp, u32, u32, u32p, u32p, vp, f64p, f64p, f64p]
     frag_args = [vp, vp, vp, u32, vp, u32, u32p, vp, u32, u32, u32p, u32p, vp, f64p]
     l.oracle_shade_fragments_f64.argtypes = frag_args
@@ -293,11 +293,12 @@ def _rc_desc(rc):
     return rcd, rct
 
 
-def reflections(camera_rec, globals_rec, gb, base, ssr=None, planar=None, lightmap_uv=None, rc=None):
+def reflections(camera_rec, globals_rec, gb, base, ssr=None, planar=None, lightmap_uv=None, rc=None, env=None):
     """fs_reflection (f64) blended over ``base`` (H, W, 4), the lit target: returns
     (result (H, W, 4) float64, unsupported flag). ``ssr`` / ``planar``: (H, W, 4) float16
-    hit images, ``lightmap_uv``: (H, W, 2) float16, ``rc``: the probe texture; each None
-    for the pass's fallback."""
+    hit images, ``lightmap_uv``: (H, W, 2) float16, ``rc``: the probe texture, ``env``:
+    dict(captures=REFLECTION_CAPTURE array, texels=float16 cube array, face_size,
+    mip_levels, layers); each None for the pass's fallback."""
     W, H = gb.width, gb.height
     out = np.array(base, np.float64, copy=True, order="C")
     assert out.shape == (H, W, 4)
@@ -312,10 +313,20 @@ def reflections(camera_rec, globals_rec, gb, base, ssr=None, planar=None, lightm
         arrs.append(a)
         imgs += [_ptr(a), a.strides[0]]
     rcd, rct = _rc_desc(rc)
+    envd = None
+    if env is not None:
+        from helio_gb300 import layouts as L
+
+        caps = np.ascontiguousarray(env["captures"])
+        tex = np.ascontiguousarray(env["texels"], np.float16)
+        envd = np.zeros(1, L.REFLECTION_ENV)
+        envd["captures"], envd["count"], envd["texels"] = caps.ctypes.data, len(caps), tex.ctypes.data
+        envd["face_size"], envd["mip_levels"], envd["layers"] = env["face_size"], env["mip_levels"], env["layers"]
+        arrs += [caps, tex]
     flag = np.zeros(1, np.int32)
     lib().oracle_reflections_f64(_ptr(np.ascontiguousarray(camera_rec)), _ptr(np.ascontiguousarray(globals_rec)),
                                  gb.layout, W, H, ptrs, pitch, *imgs, _ptr(rcd) if rcd is not None else None,
-                                 _ptr(out), _ptr(flag))
+                                 _ptr(envd) if envd is not None else None, _ptr(out), _ptr(flag))
     return out, bool(flag[0])
 
 

@@ -789,7 +789,22 @@ void shade_impl(const void* camera, const void* globals, const GBufferDesc& g, c
 
 // ---- the reflection draw (fs_reflection, deferred_lighting.wgsl:1265-1341) ----
 
-struct ReflectImages {  // hl_reflection_inputs with host pointers; rc: null = unbound
+inline void half4(const unsigned char* p, double* o) {
+    for (int i = 0; i < 4; ++i) {
+        uint16_t v;
+        std::memcpy(&v, p + 2 * i, 2);
+        o[i] = half_to_double(v);
+    }
+}
+
+struct EnvDesc {  // hl_reflection_env with host pointers
+    const void* captures;
+    uint32_t count, face_size, mip_levels, layers;
+    const void* texels;
+};
+static_assert(sizeof(EnvDesc) == 32, "hl_reflection_env is 32 bytes");
+
+struct ReflectImages {  // hl_reflection_inputs with host pointers; rc, env: null = unbound
     const unsigned char* ssr;
     uint64_t ssr_pitch;
     const unsigned char* planar;
@@ -797,14 +812,128 @@ struct ReflectImages {  // hl_reflection_inputs with host pointers; rc: null = u
     const unsigned char* lmuv;
     uint64_t lmuv_pitch;
     const rc_oracle::RcDesc* rc;
+    const EnvDesc* env;
 };
 
-inline void half4(const unsigned char* p, double* o) {
-    for (int i = 0; i < 4; ++i) {
-        uint16_t v;
-        std::memcpy(&v, p + 2 * i, 2);
-        o[i] = half_to_double(v);
+// One level of one cube layer as the pass's env sampler reads it (linear within the
+// level, clamp to edge): the face of the direction's major axis (ties to z, then y),
+// the Vulkan / WebGPU face coordinates, bilinear within the face.
+template <class T>
+void cube_sample(const EnvDesc& e, T dx, T dy, T dz, uint32_t layer, uint32_t level, T out[3]) {
+    const T ax = std::fabs(dx), ay = std::fabs(dy), az = std::fabs(dz);
+    uint32_t face;
+    T sc, tc, ma;
+    if (az >= ax && az >= ay) {
+        face = dz >= T(0) ? 4u : 5u;
+        sc = dz >= T(0) ? dx : -dx;
+        tc = -dy;
+        ma = az;
+    } else if (ay >= ax) {
+        face = dy >= T(0) ? 2u : 3u;
+        sc = dx;
+        tc = dy >= T(0) ? dz : -dz;
+        ma = ay;
+    } else {
+        face = dx >= T(0) ? 0u : 1u;
+        sc = dx >= T(0) ? -dz : dz;
+        tc = -dy;
+        ma = ax;
     }
+    const T s = ma > T(0) ? T(0.5) * (sc / ma + T(1)) : T(0.5), t = ma > T(0) ? T(0.5) * (tc / ma + T(1)) : T(0.5);
+    uint64_t chain = 0, off = 0;
+    for (uint32_t m = 0; m < e.mip_levels; ++m) {
+        const uint64_t nm = std::max<uint64_t>(1, e.face_size >> m);
+        if (m < level) off += nm * nm;
+        chain += nm * nm;
+    }
+    const uint32_t n = std::max<uint32_t>(1u, e.face_size >> level);
+    const unsigned char* base =
+        static_cast<const unsigned char*>(e.texels) + 8ull * ((uint64_t(layer) * 6u + face) * chain + off);
+    const T u = s * T(n) - T(0.5), v = t * T(n) - T(0.5);
+    const T fu = std::floor(u), fv = std::floor(v);
+    const T wu = u - fu, wv = v - fv;
+    const int64_t iu = int64_t(fu), iv = int64_t(fv), top = int64_t(n) - 1;
+    auto cl = [&](int64_t k) { return k < 0 ? 0 : (k > top ? top : k); };
+    double t00[4], t01[4], t10[4], t11[4];
+    half4(base + 8ull * (uint64_t(cl(iv)) * n + cl(iu)), t00);
+    half4(base + 8ull * (uint64_t(cl(iv)) * n + cl(iu + 1)), t01);
+    half4(base + 8ull * (uint64_t(cl(iv + 1)) * n + cl(iu)), t10);
+    half4(base + 8ull * (uint64_t(cl(iv + 1)) * n + cl(iu + 1)), t11);
+    for (int k = 0; k < 3; ++k)
+        out[k] = (T(t00[k]) * (T(1) - wu) + T(t01[k]) * wu) * (T(1) - wv) + (T(t10[k]) * (T(1) - wu) + T(t11[k]) * wu) * wv;
+}
+
+// sample_reflection_environment (deferred_lighting.wgsl:646-694) with capture_weight
+// (:618-638), parallax_box (:596-616) and parallax_sphere (:575-588).
+template <class T>
+void reflection_environment(const EnvDesc& e, uint32_t count, V3<T> P, V3<T> R, T lod, T out[3], int* bounds) {
+    const int64_t lvl = int64_t(std::ceil(lod + T(0.5))) - 1;
+    const uint32_t level = uint32_t(std::min<int64_t>(std::max<int64_t>(lvl, 0), int64_t(e.mip_levels) - 1));
+    T acc_c[3] = {0, 0, 0}, acc = 0;
+    const uint32_t n = std::min(std::min(count, 64u), e.count);
+    for (uint32_t i = 0; i < n; ++i) {
+        if (acc >= T(0.999)) break;
+        const unsigned char* cp = static_cast<const unsigned char*>(e.captures) + 112ull * i;
+        float pr[4], et[4], m[16], brightness;
+        int32_t layer;
+        uint32_t shape;
+        std::memcpy(pr, cp, 16);
+        std::memcpy(et, cp + 16, 16);
+        std::memcpy(m, cp + 32, 64);
+        std::memcpy(&layer, cp + 96, 4);
+        std::memcpy(&shape, cp + 100, 4);
+        std::memcpy(&brightness, cp + 108, 4);
+        if (layer < 0) continue;
+        if (uint32_t(layer) >= e.layers) {
+            *bounds = 1;
+            continue;
+        }
+        auto row = [&](int r, T x, T y, T z, T w) { return T(m[r]) * x + T(m[4 + r]) * y + T(m[8 + r]) * z + T(m[12 + r]) * w; };
+        T w;
+        if (shape == 1u) {
+            const T gx = T(et[0]) - std::fabs(row(0, P.x, P.y, P.z, T(1)));
+            const T gy = T(et[1]) - std::fabs(row(1, P.x, P.y, P.z, T(1)));
+            const T gz = T(et[2]) - std::fabs(row(2, P.x, P.y, P.z, T(1)));
+            w = (gx < T(0) || gy < T(0) || gz < T(0))
+                    ? T(0) : clampt(tmin(tmin(gx, gy), gz) / tmax(T(et[3]), T(1e-4)), T(0), T(1));
+        } else {
+            const V3<T> o = P - v3<T>(pr[0], pr[1], pr[2]);
+            const T dist = tsqrt(dot(o, o));
+            w = dist > T(pr[3]) ? T(0) : clampt((T(pr[3]) - dist) / tmax(T(pr[3]) * T(0.1), T(1e-4)), T(0), T(1));
+        }
+        if (w <= T(0)) continue;
+        V3<T> dir = R;
+        if (shape == 1u) {
+            const T pl[3] = {row(0, P.x, P.y, P.z, T(1)), row(1, P.x, P.y, P.z, T(1)), row(2, P.x, P.y, P.z, T(1))};
+            const T rl[3] = {row(0, R.x, R.y, R.z, T(0)), row(1, R.x, R.y, R.z, T(0)), row(2, R.x, R.y, R.z, T(0))};
+            T t = std::numeric_limits<T>::infinity();
+            for (int k = 0; k < 3; ++k) {
+                const T inv = T(1) / rl[k];
+                t = tmin(t, tmax((-T(et[k]) - pl[k]) * inv, (T(et[k]) - pl[k]) * inv));
+            }
+            if (t > T(0) && t < T(3.402823e38)) dir = (P + R * t) - v3<T>(pr[0], pr[1], pr[2]);
+        } else {
+            const V3<T> o = P - v3<T>(pr[0], pr[1], pr[2]);
+            const T b = dot(o, R);
+            const T c = dot(o, o) - T(pr[3]) * T(pr[3]);
+            const T disc = b * b - c;
+            if (disc >= T(0)) {
+                const T t = -b + tsqrt(disc);
+                if (t > T(0)) dir = (P + R * t) - v3<T>(pr[0], pr[1], pr[2]);
+            }
+        }
+        T smp[3];
+        cube_sample<T>(e, dir.x, dir.y, dir.z, uint32_t(layer), level, smp);
+        const T contrib = w * (T(1) - acc);
+        for (int k = 0; k < 3; ++k) acc_c[k] += smp[k] * T(brightness) * contrib;
+        acc += contrib;
+    }
+    if (acc < T(0.999)) {
+        T sky[3];
+        cube_sample<T>(e, R.x, R.y, R.z, 0u, level, sky);
+        for (int k = 0; k < 3; ++k) acc_c[k] += sky[k] * (T(1) - acc);
+    }
+    for (int k = 0; k < 3; ++k) out[k] = acc_c[k];
 }
 
 // out_rgba holds the lit target (fs_main's output) and receives the blended result:
@@ -857,7 +986,18 @@ void reflect_impl(const void* camera, const void* globals, const GBufferDesc& g,
             for (int k = 0; k < 3; ++k) F[k] = F0[k] + (tmax(T(1) - rough, F0[k]) - F0[k]) * p5;
             const T nv = dot(N, V);
             const V3<T> R = v3<T>(T(2) * nv * N.x - V.x, T(2) * nv * N.y - V.y, T(2) * nv * N.z - V.z);
-            T spec[3] = {0, 0, 0};  // environment term: the black fallback cube (lib.rs:542)
+            T spec[3] = {0, 0, 0};  // environment term: the black fallback cube (lib.rs:542) ...
+            if (im.env && gl.enable_env_reflections != 0u && gl.enable_reflections != 0u) {
+                // ... or the captures' (:1313-1318)
+                T env[3];
+                int env_bounds = 0;  // layer indices beyond the array: skipped (the kernel reports them)
+                reflection_environment<T>(*im.env, gl.reflection_capture_count, P, R, rough * T(8), env, &env_bounds);
+                const T r0 = rough * T(-1) + T(1), r1 = rough * T(-0.0275) + T(0.0425);
+                const T r2 = rough * T(-0.572) + T(1.04), r3 = rough * T(0.022) + T(-0.04);
+                const T a004 = tmin(r0 * r0, T(std::exp2(T(-9.28) * NdV))) * r0 + r1;
+                const T bx = T(-1.04) * a004 + r2, by = T(1.04) * a004 + r3;
+                for (int k = 0; k < 3; ++k) spec[k] = env[k] * (F0[k] * bx + by);
+            }
             if (gl.enable_reflections != 0u && T(ssr[3]) > T(0))
                 for (int k = 0; k < 3; ++k) spec[k] = mixt(spec[k], T(ssr[k]) * F[k], T(ssr[3]));
             if (gl.enable_reflections != 0u && im.planar) {
@@ -1309,11 +1449,11 @@ void oracle_shade_ex_f64(const void* cam, const void* globals, uint32_t layout, 
 void oracle_reflections_f64(const void* cam, const void* globals, uint32_t layout, uint32_t W, uint32_t H,
                             const void* const* planes, const uint64_t* pitch, const void* ssr, uint64_t ssr_pitch,
                             const void* planar, uint64_t planar_pitch, const void* lmuv, uint64_t lmuv_pitch,
-                            const void* rc, double* out_rgba, int* unsupported) {
+                            const void* rc, const void* env, double* out_rgba, int* unsupported) {
     GBufferDesc g = make_gbuf(layout, W, H, planes, pitch);
     ReflectImages im{static_cast<const unsigned char*>(ssr), ssr_pitch, static_cast<const unsigned char*>(planar),
                      planar_pitch, static_cast<const unsigned char*>(lmuv), lmuv_pitch,
-                     static_cast<const rc_oracle::RcDesc*>(rc)};
+                     static_cast<const rc_oracle::RcDesc*>(rc), static_cast<const EnvDesc*>(env)};
     *unsupported = 0;
     reflect_impl<double>(cam, globals, g, im, out_rgba, unsupported);
 }

@@ -128,6 +128,17 @@ pub struct hl_shade_bindings {
 
 #[repr(C)]
 #[derive(Clone, Copy)]
+pub struct hl_reflection_env {
+    pub captures: *const c_void,
+    pub count: u32,
+    pub face_size: u32,
+    pub mip_levels: u32,
+    pub layers: u32,
+    pub texels: *const c_void,
+}
+
+#[repr(C)]
+#[derive(Clone, Copy)]
 pub struct hl_reflection_inputs {
     pub ssr: *const c_void,
     pub ssr_pitch: u64,
@@ -136,6 +147,7 @@ pub struct hl_reflection_inputs {
     pub lightmap_uv: *const c_void,
     pub lightmap_uv_pitch: u64,
     pub rc: *const hl_rc_cascade,
+    pub env: *const hl_reflection_env,
 }
 
 #[repr(C)]

@@ -65,7 +65,8 @@ struct Globals {
 static_assert(sizeof(Camera) == HL_SIZEOF_GPU_CAMERA, "camera record");
 static_assert(sizeof(Light) == HL_SIZEOF_GPU_LIGHT, "light record");
 static_assert(sizeof(Globals) == HL_SIZEOF_DEFERRED_GLOBALS, "globals record");
-static_assert(sizeof(hl_reflection_inputs) == 56, "hl_reflection_inputs: 3 x (pointer, pitch) + rc pointer");
+static_assert(sizeof(hl_reflection_inputs) == 64, "hl_reflection_inputs: 3 x (pointer, pitch) + rc, env pointers");
+static_assert(sizeof(hl_reflection_env) == 32, "hl_reflection_env: captures, 4 sizes, texels");
 
 // 4x4 inverse by Gauss-Jordan (column-major in and out).
 void invert(const double* m, double* out) {

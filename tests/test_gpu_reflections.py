@@ -119,3 +119,62 @@ def test_reflection_argument_errors(ctx):
         ctx.shade_reflections(df.camera, df.globals_, df.gbuffer, N.target_struct(out),
                               rc=N.rc_cascade_struct(probes[:512]))
     assert e.value.status == N.HL_ERR_SIZE
+
+
+@pytest.mark.parametrize("layout", [S.LAYOUT_REFERENCE, S.LAYOUT_F32, S.LAYOUT_F16])
+@pytest.mark.parametrize("fmt", [N.TARGET_RGBA32F, N.TARGET_RGBA16F])
+def test_environment_term_matches_oracle(ctx, layout, fmt):
+    """The environment term (sample_reflection_environment, deferred_lighting.wgsl:646-694)
+    with sphere and box captures over a cube-map array with mip chains, with SSR and
+    planar hits blended over it. A pixel whose reflection direction lies within f32
+    rounding of a cube face edge may sample the other face (the faces are filtered
+    separately): such pixels must be rare."""
+    import torch
+
+    cam, gb, glb, base = _frame(layout, seed=41)
+    glb["enable_reflections"] = 1
+    glb["enable_env_reflections"] = 1
+    env = S.reflection_env(41)
+    glb["reflection_capture_count"] = len(env["captures"])
+    ssr, planar, lm = S.reflection_images(gb.width, gb.height, 41)
+    dcap = torch.from_numpy(env["captures"].view(np.uint8).copy()).cuda()
+    dtex = torch.from_numpy(env["texels"]).cuda()
+    es = N.reflection_env_struct(dcap, len(env["captures"]), dtex, env["face_size"], env["mip_levels"],
+                                 env["layers"])
+    df = FR.upload(cam.record, glb, np.zeros(0, L.GPU_LIGHT), gb)
+    dt = torch.float32 if fmt == N.TARGET_RGBA32F else torch.float16
+    out = torch.from_numpy(base).to(dt).cuda()
+    dssr, dpl, dlm = (torch.from_numpy(a).cuda() for a in (ssr, planar, lm))
+    ctx.shade_reflections(df.camera, df.globals_, df.gbuffer, N.target_struct(out, fmt), ssr=dssr, planar=dpl,
+                          lightmap_uv=dlm, env=es)
+    ctx.sync_status()
+    img = out.float().cpu().numpy().astype(np.float64)
+    start = base.astype(np.float64) if fmt == N.TARGET_RGBA32F else base.astype(np.float16).astype(np.float64)
+    ref, flag = oracle.reflections(cam.record, glb, gb, start, ssr=ssr, planar=planar, lightmap_uv=lm, env=env)
+    assert not flag
+    m = gb.planes[-1] < 1.0
+    added = np.abs(ref[m][:, :3] - start[m][:, :3])
+    assert (added > 0).any(-1).mean() > 0.9  # the environment lights almost every pixel
+    err = (np.abs(img - ref) / np.maximum(np.abs(ref), 1e-3))[m].max(-1)
+    bad = err > TOL[fmt]
+    assert bad.sum() <= max(2, 2e-4 * m.sum()), (int(bad.sum()), float(err.max()))
+    np.testing.assert_array_equal(img[..., 3], start[..., 3])  # alpha kept
+
+
+def test_environment_rejects_bad_inputs(ctx):
+    import torch
+
+    cam, gb, glb, base = _frame(S.LAYOUT_F32, W=64, H=32)
+    env = S.reflection_env(2)
+    df = FR.upload(cam.record, glb, np.zeros(0, L.GPU_LIGHT), gb)
+    out = torch.from_numpy(base).cuda()
+    dcap = torch.from_numpy(env["captures"].view(np.uint8).copy()).cuda()
+    dtex = torch.from_numpy(env["texels"]).cuda()
+    for kw, status in ((dict(face_size=0), N.HL_ERR_SIZE), (dict(mip_levels=16), N.HL_ERR_SIZE),
+                       (dict(layers=0), N.HL_ERR_SIZE)):
+        args = dict(face_size=env["face_size"], mip_levels=env["mip_levels"], layers=env["layers"])
+        args.update(kw)
+        es = N.reflection_env_struct(dcap, len(env["captures"]), dtex, **args)
+        with pytest.raises(N.HelioError) as e:
+            ctx.shade_reflections(df.camera, df.globals_, df.gbuffer, N.target_struct(out), env=es)
+        assert e.value.status == status

@@ -21,11 +21,13 @@ PAIRS = [
     ("hl_batch_config", N.BatchConfig), ("hl_fragment_params", N.FragmentParams), ("hl_texture", N.Texture),
     ("hl_shadow_maps", N.ShadowMaps), ("hl_rc_cascade", N.RcCascade), ("hl_shade_bindings", N.ShadeBindings),
     ("hl_reflection_inputs", N.ReflectionInputs), ("hl_gbuffer_targets", N.GBufferTargets),
+    ("hl_reflection_env", N.ReflectionEnv),
 ]
 # (C struct, numpy record dtype) for the records the oracle and the tests build
 DTYPES = [
     ("hl_froxel_params", L.FROXEL_PARAMS), ("hl_fragment", L.FRAGMENT), ("hl_surface", L.SURFACE),
     ("hl_texture", L.TEXTURE), ("hl_shadow_maps", L.SHADOW_MAPS), ("hl_rc_cascade", L.RC_CASCADE),
+    ("hl_reflection_env", L.REFLECTION_ENV),
 ]
 
 

@@ -160,3 +160,65 @@ def test_rc_specular_only_on_rough_pixels():
     # has_rc_gi without probes: the pixels that need them are reported
     _, unsupported = oracle.reflections(cam.record, g, gb, base)
     assert unsupported
+
+
+def _env_scene(layout=S.LAYOUT_F32, W=64, H=40, seed=8):
+    cam = S.default_camera(W, H)
+    gb = S.make_gbuffer(cam, layout, seed=seed)
+    glb = L.make_globals(L.tile_grid(W, H)[0], 0)
+    glb["enable_reflections"] = 1
+    glb["enable_env_reflections"] = 1
+    return cam, gb, glb
+
+
+def test_environment_term_of_a_uniform_sky_is_the_split_sum():
+    """Layer 0 only (no capture) holding one colour c at every texel: the environment
+    sample is c at any direction and level, so the draw adds
+    c (F0 env_brdf.x + env_brdf.y) ao (env_brdf_approx, pbr_eval.wgsl:70-76)."""
+    cam, gb, glb = _env_scene()
+    env = S.reflection_env(3, face_size=8, mip_levels=4, layers=1, n_captures=0)
+    c = np.array([0.75, 1.5, 2.25])
+    env["texels"][:, :3] = c.astype(np.float16)
+    glb["reflection_capture_count"] = 0
+    base = np.zeros((gb.height, gb.width, 4))
+    out, flag = oracle.reflections(cam.record, glb, gb, base, env=env)
+    assert not flag
+    metal, dep = gb.planes[1][..., 3].astype(np.float64), gb.planes[2]
+    # the three channels differ only through F0 and c: check their ratios
+    m = dep < 1.0
+    got = out[m][:, :3]
+    assert np.all(got >= 0.0) and (got > 0).any(-1).mean() > 0.99
+    ratio = got / c
+    # for metallic == 0 every channel shares F0 = 0.04: the three ratios agree
+    die = metal[m] == 0.0
+    np.testing.assert_allclose(ratio[die][:, 0], ratio[die][:, 1], rtol=1e-12)
+    np.testing.assert_allclose(ratio[die][:, 1], ratio[die][:, 2], rtol=1e-12)
+
+
+def test_environment_capture_weight_and_brightness():
+    """One sphere capture of uniform colour c1 (brightness b) well inside which every
+    point lies, over a sky of colour c0: weight 1 everywhere inside the inner 90 % of
+    the radius, so the sample is c1 b there; outside the sphere it is the sky c0."""
+    cam, gb, glb = _env_scene(W=48, H=32)
+    env = S.reflection_env(4, face_size=4, mip_levels=3, layers=2, n_captures=1)
+    face = 6 * sum(max(1, 4 >> m) ** 2 for m in range(3))
+    env["texels"][:face, :3] = np.float16(0.5)   # layer 0, the sky
+    env["texels"][face:, :3] = np.float16(2.0)   # layer 1
+    caps = env["captures"]
+    caps[0]["position_radius"] = (0.0, 0.0, -10.0, 12.0)
+    caps[0]["shape"] = L.CAPTURE_SPHERE
+    caps[0]["cubemap_index"] = 1
+    caps[0]["brightness"] = 1.25
+    glb["reflection_capture_count"] = 1
+    base = np.zeros((gb.height, gb.width, 4))
+    out, _ = oracle.reflections(cam.record, glb, gb, base, env=env)
+    env0 = dict(env, captures=caps[:0])
+    glb0 = glb.copy()
+    glb0["reflection_capture_count"] = 0
+    sky, _ = oracle.reflections(cam.record, glb0, gb, base, env=env0)
+    # world positions of the pixels (depth linear in NDC is not needed: use the ratio)
+    m = gb.planes[2] < 1.0
+    ratio = out[m][:, 0] / np.maximum(sky[m][:, 0], 1e-30)
+    # inside: 2.0 * 1.25 / 0.5 = 5 times the sky; outside: 1; the fade band in between
+    assert np.isclose(ratio, 5.0).any() and np.isclose(ratio, 1.0).any()
+    assert np.all((ratio > 1.0 - 1e-9) & (ratio < 5.0 + 1e-9))

@@ -76,7 +76,7 @@ def test_every_entry_point_is_bound_with_its_arity():
 
 def test_repr_c_structs_list_the_header_fields_in_order():
     for name in ["hl_froxel_params", "hl_froxel_lists", "hl_gbuffer", "hl_light_grid", "hl_target", "hl_shadow_maps",
-                 "hl_rc_cascade", "hl_shade_bindings", "hl_reflection_inputs", "hl_fragment_params", "hl_surface",
+                 "hl_rc_cascade", "hl_shade_bindings", "hl_reflection_inputs", "hl_reflection_env", "hl_fragment_params", "hl_surface",
                  "hl_texture", "hl_gbuffer_targets", "hl_view", "hl_batch_config"]:
         assert rust_struct_fields(name) == header_struct_fields(name), name
 
