@@ -26,6 +26,7 @@
 #include "hl_common.cuh"
 #include "hl_host.h"
 #include "hl_internal.h"
+#include "hl_bin_item.cuh"
 
 using namespace hl_host;
 
@@ -45,6 +46,13 @@ struct hl_batch_plan {
     cudaStream_t capture_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    // the persistent form (FP16 G-buffers): binning and shading items in one launch
+    bool persistent = false;
+    uint32_t total_bin = 0, grid_ctas = 0;
+    uint2* tiles = nullptr;                 // shading work list: (view, tile), heaviest views first
+    unsigned long long* chain = nullptr;    // one word per binning item
+    hl::BinChainState* state = nullptr;     // ticket counter and epoch
+    uint32_t* view_done = nullptr;          // binning items finished per view, over all launches
 };
 
 namespace {
@@ -70,6 +78,10 @@ void free_plan(hl_batch_plan* p) {
     cudaFree(p->counts);
     cudaFree(p->offsets);
     cudaFree(p->indices);
+    cudaFree(p->tiles);
+    cudaFree(p->chain);
+    cudaFree(p->state);
+    cudaFree(p->view_done);
     delete p;
 }
 
@@ -84,6 +96,23 @@ hl_froxel_params params_for(const HostView& v, const uint32_t* g) {
     p.slice_far = v.far_plane;
     p.reserved = 0;
     return p;
+}
+
+// One execution of a plan's work: the persistent form (candidate tables, then one launch
+// of binning and shading items) or six launches (light preparation, froxel counts,
+// scans, fills, candidate tables, shading).
+cudaError_t record_plan(hl_batch_plan* p, const void* lights, const void* globals, cudaStream_t st) {
+    if (p->persistent) {
+        cudaError_t e = hl::launch_prep_cand_batched(p->d_shade, p->n_views, lights, p->n_lights, true, st);
+        if (e != cudaSuccess) return e;
+        return hl::launch_batch_persistent(p->target_format, p->d_bin, p->d_shade, p->n_views, p->tiles, p->total_bin,
+                                           p->total_tiles, p->grid_ctas, globals, lights, p->n_lights, p->chain,
+                                           p->state, p->view_done, p->d_status, st);
+    }
+    cudaError_t e = hl::launch_bin_froxels_batched(p->d_bin, p->n_views, p->total_cols, lights, p->n_lights, p->d_status, st);
+    if (e != cudaSuccess) return e;
+    return hl::launch_shade_batched(p->layout, p->target_format, p->d_shade, p->n_views, p->total_tiles, globals,
+                                    lights, p->n_lights, p->d_status, st);
 }
 
 // Builds a plan over `views` with grids `grid` (3 per view): buffers, descriptors,
@@ -183,6 +212,52 @@ hl_status build_plan(hl_ctx* ctx, const std::vector<HostView>& views, const std:
         free_plan(p);
         return cuda_fail(ctx, e, "batch froxel index buffer");
     }
+    // the persistent form: binning items per view (slice groups only when the batch has
+    // too few columns to fill the GPU) and the shading work list, heaviest views first
+    std::vector<uint2> work;
+    if (layout == HL_GBUF_F16) {
+        int sms = 1;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess || sms <= 0) sms = 1;
+        uint64_t items = 0;
+        for (uint32_t v = 0; v < V; ++v) {
+            bd[v].groups = p->total_cols >= 2u * uint32_t(sms) ? 1u : hl::bin::item_groups(bd[v].p, 2u * uint32_t(sms));
+            bd[v].item_start = uint32_t(items);
+            items += uint64_t(bd[v].p.grid_x) * bd[v].p.grid_y * bd[v].groups;
+        }
+        std::vector<uint32_t> order(V);
+        for (uint32_t v = 0; v < V; ++v) order[v] = v;
+        // list entries per froxel column: the mean length of a view's pixel lists, up to the slice count
+        std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+            const double ca = double(totals[a]) / (double(bd[a].p.grid_x) * bd[a].p.grid_y);
+            const double cb = double(totals[b]) / (double(bd[b].p.grid_x) * bd[b].p.grid_y);
+            return ca > cb;
+        });
+        for (uint32_t v : order) {
+            const uint32_t nt = sd[v].tiles_x * ((views[v].gb.height + 15) / 16);
+            for (uint32_t t = 0; t < nt; ++t) work.push_back(make_uint2(v, t));
+        }
+        if (items + work.size() > 0x7FFFFFFFull) {
+            free_plan(p);
+            return fail(ctx, HL_ERR_SIZE, "batch has %llu work items", (unsigned long long)(items + work.size()));
+        }
+        p->persistent = true;
+        p->total_bin = uint32_t(items);
+        p->grid_ctas = std::min<uint32_t>(hl::batch_persistent_grid(p->device), uint32_t(items + work.size()));
+        e = cudaMalloc(&p->tiles, sizeof(uint2) * std::max<size_t>(work.size(), 1));
+        if (e == cudaSuccess) e = cudaMalloc(&p->chain, sizeof(unsigned long long) * std::max<uint64_t>(items, 1));
+        if (e == cudaSuccess) e = cudaMalloc(&p->state, sizeof(hl::BinChainState));
+        if (e == cudaSuccess) e = cudaMalloc(&p->view_done, sizeof(uint32_t) * V);
+        if (e == cudaSuccess) e = cudaMemsetAsync(p->chain, 0, sizeof(unsigned long long) * std::max<uint64_t>(items, 1), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(p->state, 0, sizeof(hl::BinChainState), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(p->view_done, 0, sizeof(uint32_t) * V, st);
+        if (e == cudaSuccess && !work.empty())
+            e = cudaMemcpyAsync(p->tiles, work.data(), sizeof(uint2) * work.size(), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // `work` is a host temporary
+        if (e != cudaSuccess) {
+            free_plan(p);
+            return cuda_fail(ctx, e, "batch plan work list");
+        }
+    }
     for (uint32_t v = 0; v < V; ++v) {
         bd[v].indices = p->indices + i_base[v];
         bd[v].capacity = uint32_t(i_base[v + 1] - i_base[v]);
@@ -201,18 +276,11 @@ hl_status build_plan(hl_ctx* ctx, const std::vector<HostView>& views, const std:
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(p->d_shade, sd.data(), sizeof(hl::ShadeViewDesc) * V, cudaMemcpyHostToDevice, st);
     // one uncaptured run (sets kernel attributes and checks the launches), then the graph
-    if (e == cudaSuccess)
-        e = hl::launch_bin_froxels_batched(p->d_bin, V, p->total_cols, lights, n_lights, p->d_status, st);
-    if (e == cudaSuccess)
-        e = hl::launch_shade_batched(layout, target, p->d_shade, V, p->total_tiles, globals, lights, n_lights,
-                                     p->d_status, st);
+    if (e == cudaSuccess) e = record_plan(p, lights, globals, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        cudaError_t e1 = hl::launch_bin_froxels_batched(p->d_bin, V, p->total_cols, lights, n_lights, p->d_status, st);
-        if (e1 == cudaSuccess)
-            e1 = hl::launch_shade_batched(layout, target, p->d_shade, V, p->total_tiles, globals, lights, n_lights,
-                                          p->d_status, st);
+        cudaError_t e1 = record_plan(p, lights, globals, st);
         e = cudaStreamEndCapture(st, &p->graph);
         if (e == cudaSuccess) e = e1;
     }

@@ -188,6 +188,8 @@ struct BinViewDesc {
     hl_froxel_params p;
     uint32_t capacity;
     uint32_t col_start;         // first column of this view in the batch's column range
+    uint32_t groups;            // slice groups per column of the persistent launch's binning items
+    uint32_t item_start;        // first binning item of this view in the persistent launch
     SliceTable tab;
 };
 

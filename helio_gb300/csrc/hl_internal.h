@@ -122,6 +122,21 @@ cudaError_t launch_shade_f16_batched(uint32_t target_format, const ShadeViewDesc
                                      uint32_t total_tiles, const void* globals, const void* lights, uint32_t n,
                                      int* status, cudaStream_t stream);
 
+// Batched views of an FP16 G-buffer in one persistent launch: froxel binning items of
+// every view, then the (view, tile) shading items `tiles` (x: view, y: tile), taken by
+// ticket from `state`; `chain` holds one word per binning item, `view_done` one counter
+// per view (all zeroed when allocated). grid: batch_persistent_grid (resident CTAs).
+size_t batch_persistent_smem();
+uint32_t batch_persistent_grid(int device);
+cudaError_t launch_batch_persistent(uint32_t target_format, const BinViewDesc* bd, const ShadeViewDesc* sd,
+                                    uint32_t n_views, const uint2* tiles, uint32_t total_bin, uint32_t total_tiles,
+                                    uint32_t grid, const void* globals, const void* lights, uint32_t n,
+                                    unsigned long long* chain, BinChainState* state, uint32_t* view_done,
+                                    int* status, cudaStream_t stream);
+// The views' candidate-test light tables of a batch (one launch).
+cudaError_t launch_prep_cand_batched(const ShadeViewDesc* descs, uint32_t n_views, const void* lights, uint32_t n,
+                                     bool relative, cudaStream_t stream);
+
 // Adjoint of shading. partials: grid_size * n_lights * 8 floats of scratch.
 uint32_t adjoint_grid_size(int device, uint32_t width, uint32_t height);
 cudaError_t launch_shade_adjoint(uint32_t layout, uint32_t grid_kind, const void* camera, const void* globals,

@@ -881,6 +881,14 @@ cudaError_t dispatch_grid(uint32_t grid_kind, uint32_t target, const void* camer
 
 }  // namespace
 
+cudaError_t launch_prep_cand_batched(const ShadeViewDesc* descs, uint32_t n_views, const void* lights, uint32_t n,
+                                     bool relative, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    prep_cand_batched_kernel<<<dim3((n + 255) / 256, n_views), 256, 0, stream>>>(
+        descs, static_cast<const GpuLight*>(lights), n, relative ? 1u : 0u);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_prep_cand(const void* camera, const void* lights, uint32_t n, bool relative, float4* cand,
                              cudaStream_t stream) {
     return launch_pdl(prep_cand_kernel, dim3((n + 255) / 256), dim3(256), 0, stream,

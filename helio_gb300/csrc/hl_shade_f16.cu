@@ -22,6 +22,9 @@
 //     The pairs left in the warps' queues at the end are evaluated together, 32 per
 //     warp, and each warp then adds its own in order;
 //  5. threads compose hemisphere ambient and store their pixels.
+#include <algorithm>
+
+#include "hl_bin_item.cuh"
 #include "hl_common.cuh"
 #include "hl_internal.h"
 #include "hl_precise.cuh"
@@ -222,9 +225,16 @@ __device__ __noinline__ void flush32(f16k::Smem& s, const uint32_t* queue, uint3
     __syncwarp();
 }
 
+// A load of the froxel lists: through the read-only path, or (COHERENT) from L2 when
+// the lists were written earlier in the same launch (the persistent batched launch).
+template <bool COHERENT>
+__device__ __forceinline__ uint32_t list_ld(const uint32_t* p) {
+    return COHERENT ? __ldcg(p) : __ldg(p);
+}
+
 // Lights the 32x16 tile (bx, by) of one view. prefetch_next: the tile index (row-major
 // over tiles_x tiles per row) whose G-buffer to ask L2 for, or ~0u.
-template <uint32_t TARGET>
+template <uint32_t TARGET, bool COHERENT = false>
 __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* __restrict__ cam,
                                                const DeferredGlobals* __restrict__ glb, const GBufView& gb,
                                                const GpuLight* __restrict__ lights, uint32_t n_lights,
@@ -420,8 +430,8 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
             px = rp.x; py = rp.y; pz = rp.z;
             nx = rn.x; ny = rn.y; nz = rn.z;
             f = s.w.walk.fidx[i];
-            lb = __ldg(grid.counts + f);
-            le = __ldg(grid.counts + f + 1);
+            lb = list_ld<COHERENT>(grid.counts + f);
+            le = list_ld<COHERENT>(grid.counts + f + 1);
             if (!(lb <= le && le <= grid.lists_capacity)) {
                 raise_status(status, HL_ERR_DEVICE_BOUNDS);
                 le = lb;
@@ -450,7 +460,7 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
                 const float b1z = o2f(__reduce_max_sync(0xffffffffu, mine ? f2o(pz) : int(0x80000000)));
                 const uint32_t j = __shfl_sync(0xffffffffu, lb, leader) + c0 + lane;
                 const uint32_t je = __shfl_sync(0xffffffffu, le, leader);
-                const uint32_t lj = j < je ? __ldg(grid.lists + j) : 0xffffffffu;
+                const uint32_t lj = j < je ? list_ld<COHERENT>(grid.lists + j) : 0xffffffffu;
                 const bool ok = lj < n_lights;
                 if (j < je && !ok) raise_status(status, HL_ERR_DEVICE_BOUNDS);
                 const float4 c = ok ? __ldg(cand + lj) : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
@@ -473,7 +483,7 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
                 if (smask) {
                     const uint32_t bit = __ffs(smask) - 1;
                     smask &= smask - 1;
-                    li = __ldg(grid.lists + cb + bit);
+                    li = list_ld<COHERENT>(grid.lists + cb + bit);
                     const float4 a = __ldg(cand + li);
                     pass = a.w < 0.0f || candidate(px, py, pz, 0.0f, 0.0f, 0.0f, nx, ny, nz, a.x, a.y, a.z, a.w,
                                                    slack, true);
@@ -610,6 +620,112 @@ __global__ void __launch_bounds__(f16k::kThreads, 3) shade_f16_batched_kernel(co
                            v.tiles_x, ~0u);
 }
 
+// ---- batched views in one persistent launch ------------------------------------------
+//
+// CTAs take work items by ticket from a device counter: first the froxel binning items
+// of every view (bin::bin_item, a slice group of one froxel column), then the (view,
+// 32x16 tile) shading items in the plan's order (views with the longest lists first).
+// A shading item waits until every binning item of its view has finished: that view's
+// counter reaches its item count times the launch's epoch. The wait polls with a bound
+// (~0.5 s), after which the item reports HL_ERR_TIMEOUT and is skipped instead of
+// hanging; it can only wait on items with smaller tickets, which CTAs already running
+// hold. Lists written in this launch are read from L2 (COHERENT). The last CTA to
+// finish advances the ticket base and the epoch, so a graph replays the launch.
+constexpr uint32_t kViewWaitSpins = 1u << 21;
+
+// The two kinds of work item, out of line so that each keeps its own register
+// allocation inside the persistent kernel.
+__device__ __noinline__ void persistent_bin_item(unsigned char* smem, const BinViewDesc& v, const GpuLight* lights,
+                                                 uint32_t n_lights, uint32_t item, uint32_t epoch,
+                                                 unsigned long long* chain, int* status) {
+    const hl_froxel_params p = v.p;
+    bin::bin_item(*reinterpret_cast<bin::ItemSmem*>(smem), static_cast<const GpuCamera*>(v.camera), lights, n_lights,
+                  p, v.tab.z, item, v.groups, epoch, chain + v.item_start, v.offsets, v.indices, v.capacity, status,
+                  bin::StallTest{~0u, bin::kLookbackSpins});
+}
+
+template <uint32_t TARGET>
+__device__ __noinline__ void persistent_tile(unsigned char* smem, const ShadeViewDesc& v,
+                                             const DeferredGlobals* glb, const GpuLight* lights, uint32_t n_lights,
+                                             uint32_t tile, int* status) {
+    const GBufView gb = v.gb;
+    const GridView grid = v.grid;
+    const TargetView out = v.out;
+    shade_tile_f16<TARGET, true>(*reinterpret_cast<f16k::Smem*>(smem), static_cast<const GpuCamera*>(v.camera), glb,
+                                 gb, lights, n_lights, grid, v.tabz, out, status, v.cand, PairLog{nullptr, nullptr, 0},
+                                 tile % v.tiles_x, tile / v.tiles_x, v.tiles_x, ~0u);
+}
+
+template <uint32_t TARGET>
+__global__ void __launch_bounds__(f16k::kThreads, 3) batch_persistent_kernel(
+    const BinViewDesc* __restrict__ bd, const ShadeViewDesc* __restrict__ sd, uint32_t n_views,
+    const uint2* __restrict__ tiles, uint32_t total_bin, uint32_t total_tiles, const DeferredGlobals* __restrict__ glb,
+    const GpuLight* __restrict__ lights, uint32_t n_lights, unsigned long long* __restrict__ chain,
+    BinChainState* __restrict__ state, uint32_t* __restrict__ view_done, int* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint32_t s_ticket, s_ok;
+    __shared__ unsigned long long s_base;
+    __shared__ uint32_t s_epoch;
+    const uint32_t t = threadIdx.x;
+    if (t == 0) {
+        // every CTA of the previous launch has finished before this one starts (stream
+        // order), so base and epoch are that launch's final values
+        s_base = *reinterpret_cast<volatile unsigned long long*>(&state->base);
+        s_epoch = *reinterpret_cast<volatile uint32_t*>(&state->epoch) + 1u;
+    }
+    const uint32_t total = total_bin + total_tiles;
+    for (;;) {
+        __syncthreads();
+        if (t == 0) s_ticket = uint32_t(atomicAdd(&state->ticket, 1ull) - s_base);
+        __syncthreads();
+        const uint32_t tk = s_ticket, epoch = s_epoch;
+        if (tk >= total) break;
+        if (tk < total_bin) {
+            uint32_t lo = 0, hi = n_views;  // the view whose items hold tk
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) / 2;
+                if (__ldg(&bd[mid].item_start) <= tk) lo = mid; else hi = mid;
+            }
+            persistent_bin_item(smem_raw, bd[lo], lights, n_lights, tk - bd[lo].item_start, epoch, chain, status);
+            if (t == 0) {
+                __threadfence();
+                atomicAdd(&view_done[lo], 1u);
+            }
+        } else {
+            const uint2 it = __ldg(&tiles[tk - total_bin]);
+            const ShadeViewDesc& v = sd[it.x];
+            if (t == 0) {
+                const BinViewDesc& b = bd[it.x];
+                const uint32_t items = b.p.grid_x * b.p.grid_y * b.groups;
+                const uint32_t want = items * epoch;  // the view's items of this launch have finished
+                uint32_t ok = 1, spins = 0;
+                while (*reinterpret_cast<volatile uint32_t*>(&view_done[it.x]) < want) {
+                    if (++spins > kViewWaitSpins) {
+                        raise_status(status, HL_ERR_TIMEOUT);
+                        ok = 0;
+                        break;
+                    }
+                    __nanosleep(256);
+                }
+                __threadfence();
+                s_ok = ok;
+            }
+            __syncthreads();
+            if (s_ok) persistent_tile<TARGET>(smem_raw, v, glb, lights, n_lights, it.y, status);
+        }
+    }
+    // the last CTA to finish advances the ticket base and the epoch for the next launch
+    if (t == 0) {
+        __threadfence();
+        if (atomicAdd(&state->done, 1u) == gridDim.x - 1u) {
+            state->done = 0u;
+            state->base += total + gridDim.x;  // every CTA drew one ticket past the end
+            state->epoch = s_epoch;
+            __threadfence();
+        }
+    }
+}
+
 template <class K>
 cudaError_t smem_attr(K kern, int smem) {
     static unsigned long long attr_devices = 0;  // devices on which the smem limit is raised
@@ -642,6 +758,37 @@ cudaError_t launch_target(const void* camera, const void* globals, const GBufVie
 }
 
 }  // namespace
+
+size_t batch_persistent_smem() { return std::max(sizeof(bin::ItemSmem), sizeof(f16k::Smem)); }
+
+cudaError_t launch_batch_persistent(uint32_t target_format, const BinViewDesc* bd, const ShadeViewDesc* sd,
+                                    uint32_t n_views, const uint2* tiles, uint32_t total_bin, uint32_t total_tiles,
+                                    uint32_t grid, const void* globals, const void* lights, uint32_t n,
+                                    unsigned long long* chain, BinChainState* state, uint32_t* view_done,
+                                    int* status, cudaStream_t stream) {
+    const int smem = int(batch_persistent_smem());
+    const bool h = target_format == HL_TARGET_RGBA16F;
+    auto kern = h ? batch_persistent_kernel<HL_TARGET_RGBA16F> : batch_persistent_kernel<HL_TARGET_RGBA32F>;
+    cudaError_t e = h ? smem_attr(batch_persistent_kernel<HL_TARGET_RGBA16F>, smem)
+                      : smem_attr(batch_persistent_kernel<HL_TARGET_RGBA32F>, smem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, f16k::kThreads, smem, stream>>>(bd, sd, n_views, tiles, total_bin, total_tiles,
+                                                  static_cast<const DeferredGlobals*>(globals),
+                                                  static_cast<const GpuLight*>(lights), n, chain, state, view_done,
+                                                  status);
+    return cudaGetLastError();
+}
+
+uint32_t batch_persistent_grid(int device) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms <= 0) sms = 1;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_persistent_kernel<HL_TARGET_RGBA32F>,
+                                                      f16k::kThreads, batch_persistent_smem()) != cudaSuccess ||
+        per_sm <= 0)
+        per_sm = 1;
+    return uint32_t(sms) * uint32_t(per_sm);
+}
 
 cudaError_t launch_shade_f16_batched(uint32_t target_format, const ShadeViewDesc* descs, uint32_t n_views,
                                      uint32_t total_tiles, const void* globals, const void* lights, uint32_t n,
