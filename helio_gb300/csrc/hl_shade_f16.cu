@@ -783,6 +783,10 @@ uint32_t batch_persistent_grid(int device) {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms <= 0) sms = 1;
     int per_sm = 0;
+    // the shared-memory limit first: the occupancy query respects the kernel's attribute
+    if (smem_attr(batch_persistent_kernel<HL_TARGET_RGBA32F>, int(batch_persistent_smem())) != cudaSuccess ||
+        smem_attr(batch_persistent_kernel<HL_TARGET_RGBA16F>, int(batch_persistent_smem())) != cudaSuccess)
+        cudaGetLastError();
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_persistent_kernel<HL_TARGET_RGBA32F>,
                                                       f16k::kThreads, batch_persistent_smem()) != cudaSuccess ||
         per_sm <= 0)
