@@ -14,7 +14,10 @@
 // The array lives on every GPU that loads this library until the process exits. Its
 // device address is looked up once per device with cudaGetSymbolAddress, on the first
 // call made on that device (with the device current); that first call should come before
-// any stream capture. Every call shares the array: the kernels write every scratch word
+// any stream capture. The cached address belongs to the device's primary context: a
+// cudaDeviceReset destroys that context and the address with it, so a process that
+// resets a device must not call this entry point on that device again (the next call
+// would launch on a stale address). Every call shares the array: the kernels write every scratch word
 // they read within the call, so nothing has to start at zero, but calls that overlap on
 // the GPU (on different streams, or from different host threads) race on the array and
 // must be serialised by the caller.
@@ -46,7 +49,10 @@ hl_status scratch_address(void** out) {
     if (!g_scratch_ptr[dev]) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) return HL_ERR_CUDA;
+        if (e != cudaSuccess || !p) {
+            (void)cudaGetLastError();  // the lookup's error is not left for the caller's next check
+            return HL_ERR_CUDA;
+        }
         g_scratch_ptr[dev] = p;
     }
     *out = g_scratch_ptr[dev];

@@ -175,7 +175,9 @@ hl_status hl_inject_binning_stall(hl_ctx* ctx, uint32_t item, uint32_t spins);
  * HL_NOALLOC_MAX_FROXELS counts (320 KiB, held by every GPU that loads the library
  * until the process exits). Larger requests return HL_ERR_SIZE.
  *   - The first call on a device looks the array's address up (cudaGetSymbolAddress,
- *     with that device current); make that first call before any stream capture.
+ *     with that device current); make that first call before any stream capture. The
+ *     address is kept for the life of the process: do not call this entry point on a
+ *     device after cudaDeviceReset of that device.
  *   - All calls share the array: calls that overlap on the GPU (different streams or
  *     host threads) race and must be serialised by the caller.
  *   - There is no device status word: a total above `capacity` shows as
@@ -629,8 +631,10 @@ hl_status hl_batch_plan_destroy(hl_batch_plan* plan);
  * Diagnostics (no reference counterpart)
  * -------------------------------------------------------------------------------*/
 
-/* Measures the device's FP32 FMA throughput with a register-resident FFMA loop
- * (best of 5 timed launches); the denominator of the FP32 roofline. Synchronous. */
+/* Measurement only, not part of the rendering interface: measures the device's FP32
+ * FMA throughput with a register-resident FFMA loop (best of 5 timed launches), the
+ * denominator of the FP32 roofline a benchmark reports. Synchronous; occupies the whole
+ * GPU for a few milliseconds, so never call it from a frame. */
 hl_status hl_probe_fp32_peak(hl_ctx* ctx, double* tflops);
 
 #ifdef __cplusplus

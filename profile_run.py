@@ -1,15 +1,16 @@
 """A few frames of one workload through the C ABI, for profiler captures.
 
-    python -m helio_gb300.profile_run --workload 1 --frames 3            # bin + shade
-    python -m helio_gb300.profile_run --workload 4 --frames 3 --adjoint  # + adjoint
-    python -m helio_gb300.profile_run --batched --frames 3              # 98-view plan
-    python -m helio_gb300.profile_run --workload 1 --frames 3 --fragments  # + fragment loop
-    python -m helio_gb300.profile_run --gbuffer-write --frames 3        # G-buffer pass only
-    python -m helio_gb300.profile_run --workload 1 --shadows --atlas 256 --frames 3  # + shadow term
-    python -m helio_gb300.profile_run --workload 1 --rc --frames 3      # + radiance-cascade GI
+    python profile_run.py --workload 1 --frames 3            # bin + shade
+    python profile_run.py --workload 4 --frames 3 --adjoint  # + adjoint
+    python profile_run.py --batched --frames 3              # 98-view plan
+    python profile_run.py --workload 1 --frames 3 --fragments  # + fragment loop
+    python profile_run.py --gbuffer-write --frames 3        # G-buffer pass only
+    python profile_run.py --workload 1 --shadows --atlas 256 --frames 3  # + shadow term
+    python profile_run.py --workload 1 --rc --frames 3      # + radiance-cascade GI
 
-Every frame launches the same kernels as one bench step (froxel binning: 4 launches,
-shading: 1, adjoint: 2), so ``ncu -k <kernel> -s <n> -c 1`` can pick one warm launch.
+Every frame launches the same kernels as one bench step (froxel binning: 1 launch,
+candidate light table: 1, shading: 1, adjoint: 2), so ``ncu -k <kernel> -s <n> -c 1``
+can pick one warm launch.
 Prints one line with the device time of the last frame.
 """
 from __future__ import annotations
@@ -38,10 +39,10 @@ def main(argv=None):
 
     import torch
 
-    from . import frame as FR
-    from . import layouts as L
-    from . import native as N
-    from . import synthetic as S
+    from helio_gb300 import frame as FR
+    from helio_gb300 import layouts as L
+    from helio_gb300 import native as N
+    from helio_gb300 import synthetic as S
 
     ctx = N.Context(0)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

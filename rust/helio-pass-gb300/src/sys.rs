@@ -268,5 +268,6 @@ extern "C" {
     pub fn hl_batch_execute(ctx: *mut hl_ctx, plan: *mut hl_batch_plan, stream: *mut c_void) -> hl_status;
     pub fn hl_batch_plan_view_grid(plan: *const hl_batch_plan, view: u32, grid_xyz: *mut u32) -> hl_status;
     pub fn hl_batch_plan_destroy(plan: *mut hl_batch_plan) -> hl_status;
+    /// Measurement only (the FP32 roofline denominator of a benchmark); never call it from a frame.
     pub fn hl_probe_fp32_peak(ctx: *mut hl_ctx, tflops: *mut f64) -> hl_status;
 }

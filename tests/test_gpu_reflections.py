@@ -121,6 +121,33 @@ def test_reflection_argument_errors(ctx):
     assert e.value.status == N.HL_ERR_SIZE
 
 
+def test_rc_globals_without_probes_report_and_keep_the_other_pixels(ctx):
+    """has_rc_gi set with no probe texture bound: the draw reports HL_ERR_NOT_SUPPORTED,
+    leaves the pixels that need the radiance-cascade fallback (roughness > 0.6) as they
+    were, and still lights every other pixel as the oracle does."""
+    import torch
+
+    cam, gb, glb, base = _frame(S.LAYOUT_REFERENCE, rc=True)
+    ssr, planar, lm = S.reflection_images(gb.width, gb.height, 14)
+    df = FR.upload(cam.record, glb, np.zeros(0, L.GPU_LIGHT), gb)
+    out = torch.from_numpy(base).cuda()
+    dssr, dpl, dlm = (torch.from_numpy(a).cuda() for a in (ssr, planar, lm))
+    ctx.shade_reflections(df.camera, df.globals_, df.gbuffer, N.target_struct(out), ssr=dssr, planar=dpl,
+                          lightmap_uv=dlm)
+    with pytest.raises(N.HelioError) as e:
+        ctx.sync_status()
+    assert e.value.status == N.HL_ERR_NOT_SUPPORTED
+    img = out.cpu().numpy().astype(np.float64)
+    start = base.astype(np.float64)
+    ref, unsupported = oracle.reflections(cam.record, glb, gb, start, ssr=ssr, planar=planar, lightmap_uv=lm)
+    assert unsupported
+    rough = gb.planes[2][..., 1].astype(np.float32) / np.float32(255.0) > 0.6  # ORM green, unorm8
+    assert 0.1 < rough.mean() < 0.9
+    np.testing.assert_array_equal(img[rough], start[rough])
+    _check(img, ref, start, N.TARGET_RGBA32F)
+    assert (np.abs(img - start)[~rough].max(-1) > 0).mean() > 0.3  # the smooth pixels were lit
+
+
 @pytest.mark.parametrize("layout", [S.LAYOUT_REFERENCE, S.LAYOUT_F32, S.LAYOUT_F16])
 @pytest.mark.parametrize("fmt", [N.TARGET_RGBA32F, N.TARGET_RGBA16F])
 def test_environment_term_matches_oracle(ctx, layout, fmt):

@@ -69,3 +69,63 @@ def test_noalloc_rejects_sizes_beyond_its_limit(built_library):
         N.bin_froxels_noalloc(16, 16, 8, big, 16, 16, 16)
     assert e.value.status == N.HL_ERR_SIZE
     del cam
+
+
+def test_noalloc_replays_in_a_cuda_graph_after_warm_up(ctx):
+    """The use the entry point exists for: one warm-up call on the device (the scratch
+    address is looked up there), then the call recorded inside a stream capture, where
+    nothing may allocate. Every replay gives the lists of the oracle."""
+    import torch
+
+    import oracle
+
+    w = S.workload(0, 0.5)
+    W, H = w.gbuffer.width, w.gbuffer.height
+    p_np = L.froxel_params(*w.froxel_grid, W, H, w.camera.far)
+    off_w, idx_w = oracle.bin_froxels(w.camera.record, w.lights, p_np, capacity=1 << 24)
+    p = N.froxel_params_from_numpy(p_np)
+    cap = int(off_w[-1]) + 64
+    off, idx = _buffers(p_np, cap)
+    df = FR.upload_workload(w)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        N.bin_froxels_noalloc(df.camera, df.lights, df.n_lights, p, off, idx, cap, s.cuda_stream)  # warm-up
+    s.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        N.bin_froxels_noalloc(df.camera, df.lights, df.n_lights, p, off, idx, cap, s.cuda_stream)
+    for _ in range(3):
+        off.fill_(-1)
+        idx.fill_(-1)
+        g.replay()
+        got_off, got_idx = _host(off, idx)
+        np.testing.assert_array_equal(got_off, off_w)
+        np.testing.assert_array_equal(got_idx, idx_w)
+
+
+def test_noalloc_overflow_shows_in_the_total_and_keeps_the_prefix(ctx):
+    """With no device status word, a total above the capacity shows as
+    offsets[F] > capacity: the offsets are all written, and the entries below the
+    capacity are the true lists' first entries, nothing is written beyond it."""
+    import torch
+
+    import oracle
+
+    w = S.workload(1, 0.5)
+    W, H = w.gbuffer.width, w.gbuffer.height
+    p_np = L.froxel_params(*w.froxel_grid, W, H, w.camera.far)
+    off_w, idx_w = oracle.bin_froxels(w.camera.record, w.lights, p_np, capacity=1 << 24)
+    total = int(off_w[-1])
+    cap = total // 3
+    assert cap > 0
+    off, idx_full = _buffers(p_np, cap + 256)
+    idx = idx_full[:cap]
+    df = FR.upload_workload(w)
+    N.bin_froxels_noalloc(df.camera, df.lights, df.n_lights, N.froxel_params_from_numpy(p_np), off, idx, cap)
+    torch.cuda.synchronize()
+    got_off = off.cpu().numpy().view(np.uint32)
+    got = idx_full.cpu().numpy().view(np.uint32)
+    assert got_off[-1] == total > cap
+    np.testing.assert_array_equal(got_off, off_w)
+    np.testing.assert_array_equal(got[:cap], idx_w[:cap])
+    assert (got[cap:] == 0xFFFFFFFF).all()  # the guard words past the capacity are untouched
