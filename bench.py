@@ -325,7 +325,7 @@ def run_ours(args, world, rank, local):
                 "frac": round(frac_fp32, 4), "traffic": traffic,
                 "peak_source": "hl_probe_fp32_peak FFMA loop, of measured"}
     roof.update({
-        "kernel": "shade_kernel<F16 G-buffer, froxel grid, 32x16 tile>",
+        "kernel": "shade_f16_kernel<RGBA32F> (FP16 G-buffer, froxel grid, 32x16 tile)",
         "kernel_ms": round(t_shade * 1e3, 4),
         "algorithmic_bytes": int(bytes_alg),
         "algorithmic_flops": int(flops),
@@ -335,15 +335,8 @@ def run_ours(args, world, rank, local):
         "pairs": {"listed": int(c[0]), "in_range": int(c[1]), "full": int(c[2]), "lit_pixels": lit},
     })
 
-    # ---------------- the reference's 16x16 tile culling on the same frame ----------------
-    tiles = N.load().hl_tile_count(W, H)
-    t_lists = torch.zeros(tiles * 64, dtype=torch.int32, device=dev)
-    t_counts = torch.zeros(tiles, dtype=torch.int32, device=dev)
-    t_tiles = _median_ms(lambda: ctx.bin_tiles_ref(df.camera, df.lights, df.n_lights, W, H, t_lists, t_counts, sh),
-                         stream, flush, 50)
-    ctx.sync_status(sh)
-    ref_tiles = {"tiles": int(tiles), "at_cap_64": int((t_counts == 64).sum().item()),
-                 "bin_tiles_ref_ms": round(t_tiles, 4)}
+    # ---------------- the reference's 16x16 tile culling and tile-list frames ----------------
+    ref_tiles = ref_tiles_form(ctx, dev, stream, flush, w, df, target)
 
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
@@ -357,7 +350,7 @@ def run_ours(args, world, rank, local):
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_t * 1e3 / args.steps, 4),
                 "pipelining": "3 streams x 2 buffer sets: upload k+1 / kernels k / download k-1",
                 "result_matches_device_run": e2e_check},
-        "gpu_launches": 4 * args.steps,
+        "gpu_launches": 3 * args.steps,  # froxel binning, candidate light table, shading
         "ref_tiles": ref_tiles,
         "roofline": roof,
         "clocks": clk,
@@ -376,11 +369,14 @@ def run_ours(args, world, rank, local):
                                 "kind": "port",
                                 "sample": "5 full 1920x1080 frames, froxel binning + f32 shading, OpenMP over rows"}
         off_o, idx_o = oracle.bin_froxels(w.camera.record, w.lights, p_np, capacity=1 << 22)
-        ref, pc = oracle.shade(w.camera.record, w.globals_, w.gbuffer, w.lights, ("froxels", idx_o, off_o, p_np),
-                               pair_counts=True)
-        img = target.cpu().numpy()
-        full_k = counts.cpu().numpy().view(np.uint32)[..., 2]
-        e = metrics.radiance_error(img, ref, full_k, pc[..., 2])
+        # the FP64 oracle with the timed kernel's branch decisions at the cuts of
+        # pbr_direct_light, recorded by one more launch of the same kernel
+        img, pairs = logged_shade(ctx, dev, sh, df, grid, tgt, target, W * H * 4)
+        ref, flips, unlisted = oracle.shade_forced(w.camera.record, w.globals_, w.gbuffer, w.lights,
+                                                   ("froxels", idx_o, off_o, p_np), pairs)
+        e = metrics.radiance_error(img, ref, flip_pixels=flips)
+        e["unlisted_lit_pairs"] = int(unlisted.sum())
+        e["lit_pairs"] = int(len(pairs))
         off_g = offsets.cpu().numpy().view(np.uint32)
         line["error_vs_fp64_oracle"] = {k: (round(v, 9) if isinstance(v, float) else v) for k, v in e.items()}
         line["error_vs_fp64_oracle"]["lists_bit_exact"] = bool(np.array_equal(off_g, off_o))
@@ -389,6 +385,82 @@ def run_ours(args, world, rank, local):
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
+
+
+def logged_shade(ctx, dev, sh, df, grid, tgt, target, capacity):
+    """One hl_shade launch with the lit-pair record on: (image as float64, (K, 2) uint32
+    (y * W + x, light) pairs the kernel lit)."""
+    import torch
+
+    while True:
+        pairs = torch.zeros((capacity, 2), dtype=torch.int32, device=dev)
+        count = torch.zeros(1, dtype=torch.int32, device=dev)
+        ctx.set_pair_log(pairs, count)
+        ctx.shade(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, tgt, sh)
+        ctx.set_pair_log(None)
+        ctx.sync_status(sh)
+        n = int(count.item())
+        if n <= capacity:
+            return target.double().cpu().numpy(), pairs[:n].cpu().numpy().view(np.uint32)
+        capacity = n
+
+
+def ref_tiles_form(ctx, dev, stream, flush, w1, df1, target1):
+    """The reference's observable frame: its 16x16 tile culling (at most 64 lights per
+    tile, light_cull.wgsl:123-180) and the shading over those tile lists, on w1 and on
+    w2 (3840x2160, 4096 clumped lights), beside the froxel path ("exact": every light in
+    range). Reports the tiles at the 64-light cap, the tile culling and tile-frame times,
+    the froxel binning time, and how far the tile frame's radiance is from the exact one."""
+    import torch
+
+    from helio_gb300 import frame as FR
+    from helio_gb300 import layouts as L
+    from helio_gb300 import metrics
+    from helio_gb300 import native as N
+    from helio_gb300 import synthetic as S
+
+    sh = stream.cuda_stream
+    out = {}
+    for name, wi in (("w1", 1), ("w2", 2)):
+        w = w1 if wi == 1 else S.workload(2)
+        df = df1 if wi == 1 else FR.upload_workload(w, dev)
+        W, H = w.gbuffer.width, w.gbuffer.height
+        tiles = N.load().hl_tile_count(W, H)
+        t_lists = torch.zeros(tiles * 64, dtype=torch.int32, device=dev)
+        t_counts = torch.zeros(tiles, dtype=torch.int32, device=dev)
+        t_bin = _median_ms(lambda: ctx.bin_tiles_ref(df.camera, df.lights, df.n_lights, W, H, t_lists, t_counts, sh),
+                           stream, flush, 30)
+        tg = N.tile_grid_struct(t_lists, t_counts)
+        rad_t = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
+        tt = N.target_struct(rad_t)
+
+        def tile_frame():
+            ctx.bin_tiles_ref(df.camera, df.lights, df.n_lights, W, H, t_lists, t_counts, sh)
+            ctx.shade(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, tg, tt, sh)
+
+        t_frame = _median_ms(tile_frame, stream, flush, 30)
+        fp = N.froxel_params_from_numpy(L.froxel_params(*w.froxel_grid, W, H, w.camera.far))
+        F = fp.grid_x * fp.grid_y * fp.grid_z
+        cap = F * 256
+        off = torch.zeros(F + 1, dtype=torch.int32, device=dev)
+        idx = torch.zeros(cap, dtype=torch.int32, device=dev)
+        t_fbin = _median_ms(lambda: ctx.bin_froxels(df.camera, df.lights, df.n_lights, fp, off, idx, cap, sh),
+                            stream, flush, 30)
+        rad_x = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
+        ctx.shade(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, N.froxel_grid_struct(idx, off, fp, cap),
+                  N.target_struct(rad_x), sh)
+        ctx.sync_status(sh)
+        d = metrics.radiance_error(rad_t.cpu().numpy(), rad_x.cpu().numpy())
+        out[name] = {
+            "tiles": int(tiles), "at_cap_64": int((t_counts == 64).sum().item()),
+            "max_tile_count": int(t_counts.max().item()),
+            "bin_tiles_ref_ms": round(t_bin, 4), "tile_frame_ms": round(t_frame, 4),
+            "bin_froxels_ms": round(t_fbin, 4), "froxel_grid": list(w.froxel_grid),
+            "tile_vs_exact": {"max_rel": float(f"{d['max']:.3e}"), "p9999": float(f"{d['p9999']:.3e}"),
+                              "mean_rel": float(f"{d['mean']:.3e}"), "pixels_over_2e-3": d["n_over_2e3"]},
+        }
+        del t_lists, rad_t, rad_x, off, idx
+    return out
 
 
 def _median_ms(fn, stream, flush, reps, warm=3):
@@ -487,13 +559,10 @@ def run_forms(ctx, dev, stream, flush, with_oracle=True):
         from helio_gb300 import metrics
 
         fwd()
-        st = torch.zeros((H, W, 3), dtype=torch.int32, device=dev)
-        ctx.shade_stats(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, st, sh)
-        ctx.sync_status(sh)
-        ref, pc = oracle.shade(w.camera.record, w.globals_, w.gbuffer, w.lights, ("froxels", idx_h, off_h, p_np),
-                               pair_counts=True)
-        e = metrics.radiance_error(rad.double().cpu().numpy(), ref, st.cpu().numpy().view(np.uint32)[..., 2],
-                                   pc[..., 2])
+        img, pairs = logged_shade(ctx, dev, sh, df, grid, N.target_struct(rad), rad, W * H * 4)
+        ref, flips, _ = oracle.shade_forced(w.camera.record, w.globals_, w.gbuffer, w.lights,
+                                            ("froxels", idx_h, off_h, p_np), pairs)
+        e = metrics.radiance_error(img, ref, flip_pixels=flips)
         forms["adjoint"]["forward_error_vs_fp64_oracle"] = {
             "max": float(f"{e['max']:.3e}"), "p9999": float(f"{e['p9999']:.3e}"), "n": e["n"], "flips": e["flips"],
             "n_over_1e5": e["n_over_1e5"]}
@@ -545,19 +614,29 @@ def run_forms(ctx, dev, stream, flush, with_oracle=True):
         batch_err = {}
         for vi in (0, 40, 97):  # a 128^2 face, a 512^2 face, the 1280x720 viewport
             f, p, o, ix, c, _ = per[vi]
+            plan_img = outs[vi].cpu().numpy().astype(np.float64)
+            # the single-view path gives the plan's image bit for bit; its lit pairs are the plan's
+            one = torch.zeros_like(outs[vi])
+            img1, pairs = logged_shade(ctx, dev, sh, f, N.froxel_grid_struct(ix, o, p, c), N.target_struct(one), one,
+                                       f.width * f.height * 4)
             off_h = o.cpu().numpy().view(np.uint32)
             idx_h = ix.cpu().numpy().view(np.uint32)[: int(off_h[-1])]
             pn = L.froxel_params(p.grid_x, p.grid_y, p.grid_z, p.width, p.height, p.slice_far, p.slice_near)
-            ref = oracle.shade(views[vi].camera.record, glb, views[vi].gbuffer, lights, ("froxels", idx_h, off_h, pn))
-            e = metrics.radiance_error(outs[vi].cpu().numpy().astype(np.float64), ref)
+            ref, flips, _ = oracle.shade_forced(views[vi].camera.record, glb, views[vi].gbuffer, lights,
+                                                ("froxels", idx_h, off_h, pn), pairs)
+            e = metrics.radiance_error(plan_img, ref, flip_pixels=flips)
             batch_err[f"view{vi}_{f.width}x{f.height}"] = {"max": float(f"{e['max']:.3e}"),
-                                                          "p9999": float(f"{e['p9999']:.3e}")}
+                                                          "p9999": float(f"{e['p9999']:.3e}"), "flips": e["flips"],
+                                                          "plan_equals_single_view": bool(np.array_equal(plan_img,
+                                                                                                         img1))}
     forms["batched"] = {
         "workload": "w3: 16 probes x 6 cube faces (128^2/256^2/512^2) + 1920x1080 + 1280x720, FP16 G-buffers, "
                     "2048 lights",
         "views": len(frames), "pixels": px, "batched_ms": round(t_b, 4), "per_view_launches_ms": round(t_v, 4),
         "speedup": round(t_v / t_b, 2), "batched_mpix_s": round(px / (t_b / 1e3) / 1e6, 1),
-        "launches": {"batched": 6, "per_view": 4 * len(frames)}, "autotune_s": round(tune_s, 2),
+        "launches": {"batched": 2, "per_view": 3 * len(frames)}, "autotune_s": round(tune_s, 2),
+        "batched_form": "one persistent launch: froxel binning items of every view, then (view, tile) shading "
+                        "items by device ticket (after one launch writing the views' candidate light tables)",
         "grids": sorted({(f.width, f.height) + plan.view_grid(i) for i, f in enumerate(frames)}),
         "hbm_frac": round(px * (18 + 16) / (t_b / 1e3) / 1e9 / measured_peaks()[0], 4),
         "error_vs_fp64_oracle": batch_err,
