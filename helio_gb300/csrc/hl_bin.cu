@@ -23,6 +23,9 @@ namespace {
 using namespace bin;
 constexpr int kBinWarps = bin::kWarps;
 constexpr int kBinThreads = bin::kThreads;
+// CTAs of the single-launch binning: 16 warps, two resident per SM
+constexpr int kItemWarps = 16;
+constexpr int kItemMinBlocks = 2;
 
 __global__ void __launch_bounds__(256) prep_bin_lights_kernel(const GpuCamera* __restrict__ cam,
                                                               const GpuLight* __restrict__ lights, uint32_t n,
@@ -208,12 +211,13 @@ __global__ void __launch_bounds__(kBinThreads) bin_froxels_kernel(const GpuCamer
 // view space as it gathers them, so no separate preparation launch). The ticket base
 // and the epoch live on the device and the last CTA of a launch advances them, so a
 // launch recorded in a CUDA graph can be replayed.
-__global__ void __launch_bounds__(kBinThreads, 3) bin_froxels_items_kernel(
+template <int NW>
+__global__ void __launch_bounds__(NW * 32, kItemMinBlocks) bin_froxels_items_kernel(
     const GpuCamera* __restrict__ cam, const GpuLight* __restrict__ lights, uint32_t n, hl_froxel_params p,
     const __grid_constant__ SliceTable tab, uint32_t groups, uint32_t* __restrict__ offsets,
     uint32_t* __restrict__ indices, uint32_t capacity, int* __restrict__ status,
     unsigned long long* __restrict__ chain, BinChainState* __restrict__ state, StallTest test) {
-    __shared__ ItemSmem sm;
+    __shared__ ItemSmemT<NW> sm;
     __shared__ uint32_t s_item, s_epoch;
     const uint32_t items = p.grid_x * p.grid_y * groups;
     if (threadIdx.x == 0) {
@@ -230,7 +234,7 @@ __global__ void __launch_bounds__(kBinThreads, 3) bin_froxels_items_kernel(
         return;
     }
     pdl_launch_dependents();  // the shading launch's light table and pixel set-up may start
-    bin_item(sm, cam, lights, n, p, tab.z, item, groups, epoch, chain, offsets, indices, capacity, status, test);
+    bin_item<NW>(sm, cam, lights, n, p, tab.z, item, groups, epoch, chain, offsets, indices, capacity, status, test);
     // the last CTA to finish advances the ticket base and the epoch for the next launch
     if (threadIdx.x == 0) {
         __threadfence();
@@ -385,7 +389,9 @@ cudaError_t launch_bin_froxels_batched(const BinViewDesc* descs, uint32_t n_view
 uint32_t bin_item_groups(int device, const hl_froxel_params& p) {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) sms = 1;
-    return item_groups(p, 2u * uint32_t(sms > 0 ? sms : 1));
+    // each item gathers all the lights for its column: split columns into slice groups
+    // only when there are too few columns to give every other SM one
+    return item_groups(p, uint32_t(sms > 1 ? sms : 2) / 2u);
 }
 
 cudaError_t launch_bin_froxels_items(const void* camera, const void* lights, uint32_t n, const hl_froxel_params& p,
@@ -396,7 +402,7 @@ cudaError_t launch_bin_froxels_items(const void* camera, const void* lights, uin
     const StallTest test{stall_item, stall_item == ~0u ? kLookbackSpins : stall_spins};
     // launched plainly: it starts after its predecessor has finished, so two binning
     // launches of one context (sharing ticket and chain) never overlap
-    bin_froxels_items_kernel<<<items, kBinThreads, 0, stream>>>(
+    bin_froxels_items_kernel<kItemWarps><<<items, kItemWarps * 32, 0, stream>>>(
         static_cast<const GpuCamera*>(camera), static_cast<const GpuLight*>(lights), n, p, tab, groups, offsets,
         indices, capacity, status, chain, state, test);
     return cudaGetLastError();

@@ -53,6 +53,53 @@ __device__ __forceinline__ bool sphere_in_planes(const Planes& p, float cx, floa
     return true;
 }
 
+// The three rows of the camera's view matrix that map a point to view space, held in
+// registers by code that transforms many lights (column-major: element (r, c) at
+// m[4 c + r]; row r is m[r], m[4 + r], m[8 + r], m[12 + r]).
+struct ViewRows {
+    float m[3][4];
+};
+
+__device__ __forceinline__ ViewRows load_view_rows(const GpuCamera* __restrict__ cam) {
+    ViewRows v;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) v.m[r][c] = __ldg(&cam->view[4 * c + r]);
+    return v;
+}
+
+// xmat_row over ViewRows: the same operations in the same order.
+__device__ __forceinline__ float view_row(const ViewRows& v, int r, float x, float y, float z, float w) {
+    return xadd(xadd(xadd(xmul(v.m[r][0], x), xmul(v.m[r][1], y)), xmul(v.m[r][2], z)), xmul(v.m[r][3], w));
+}
+
+// The centre, culling radius and type of a light's BinLight (prep_light's first half):
+// all a column test needs.
+__device__ __forceinline__ void prep_light_centre(const ViewRows& v, float4 pr, uint32_t type, BinLight& b) {
+    b.cx = view_row(v, 0, pr.x, pr.y, pr.z, 1.0f);
+    b.cy = view_row(v, 1, pr.x, pr.y, pr.z, 1.0f);
+    b.cz = view_row(v, 2, pr.x, pr.y, pr.z, 1.0f);
+    b.r = xadd(pr.w, xmul(xadd(pr.w, 1.0f), 1.0f / 1024.0f));  // froxel margin
+    b.type = type;
+}
+
+// The cone fields (prep_light's second half) of a light whose centre is set: the axis
+// and sine only where the cone test applies (light_meets_froxel reads them only then).
+__device__ __forceinline__ void prep_light_cone(const ViewRows& v, float4 dir, float inner, BinLight& b) {
+    b.cos_o = dir.w;
+    b.cone = (b.type == 2u) && (0.0f < dir.w) && (dir.w < inner);
+    b.pad = 0;
+    if (b.cone) {
+        const f3 a = xnormalize(mk3(view_row(v, 0, dir.x, dir.y, dir.z, 0.0f), view_row(v, 1, dir.x, dir.y, dir.z, 0.0f),
+                                    view_row(v, 2, dir.x, dir.y, dir.z, 0.0f)));
+        b.ax = a.x;
+        b.ay = a.y;
+        b.az = a.z;
+        b.sin_o = xsqrt(xmax(xsub(1.0f, xmul(dir.w, dir.w)), 0.0f));
+    }
+}
+
 // One light in the camera's view space, with its culling radius (widened for froxels).
 __device__ __forceinline__ BinLight prep_light(const GpuCamera* __restrict__ cam, const GpuLight& l,
                                                uint32_t froxel_margin) {
@@ -170,16 +217,18 @@ constexpr uint32_t kFlagAggregate = 1u, kFlagPrefix = 2u;
 constexpr uint32_t kChainValueMax = (1u << 30) - 1u;
 constexpr uint32_t kLookbackSpins = 1u << 20;  // ~0.1 s of polling before HL_ERR_TIMEOUT
 
-struct ItemSmem {
+template <int NW>
+struct ItemSmemT {
     uint32_t idx[kItemCap];           // the round's column list: light indices
     BinLight bl[kItemCap];            // and their view-space records
     uint32_t mask[kItemMaskCap];      // ballot of chunk c of slice s0 + k at [k * chunks + c]
-    uint32_t warp_tot[kGatherU * kWarps];
+    uint32_t warp_tot[kGatherU * NW];
     uint32_t slice_run[kMaxSlices];   // entries per slice of the item
     uint32_t slice_dst[kMaxSlices];   // first entry of each slice
     uint32_t stop[2];                 // first light index not kept by a full round (by step parity)
     uint32_t excl, total;
 };
+using ItemSmem = ItemSmemT<kWarps>;  // the 256-thread CTAs of the persistent batched launch
 
 // Parameters of a failure-injection test: item `stall` never publishes its chain word,
 // and the look-back gives up after `spins` polls. stall = ~0u: none.
@@ -199,12 +248,16 @@ __device__ __forceinline__ void st_chain(unsigned long long* p, uint32_t epoch, 
 
 // Appends to sm.idx / sm.bl, in light-index order, the lights from `base` on that may
 // touch the column (directional, or a sphere not outside its four planes), until the
-// lights run out or the round is full. A step tests kGatherU x 256 lights, their loads
-// in flight together; when a step overflows the round, the round ends at the first
-// light that did not fit and `base` resumes there.
-__device__ __forceinline__ uint32_t gather_item_round(ItemSmem& sm, const GpuCamera* __restrict__ cam,
+// lights run out or the round is full. A step tests kGatherU x NT lights on their
+// view-space centres alone, their loads in flight together; when a step overflows the
+// round, the round ends at the first light that did not fit and `base` resumes there.
+// The kept lights' cone fields are computed at the end of the round, once per kept
+// light (most lights miss a given column).
+template <int NW>
+__device__ __forceinline__ uint32_t gather_item_round(ItemSmemT<NW>& sm, const ViewRows& vr,
                                                       const GpuLight* __restrict__ lights, const ColumnGeom& g,
                                                       uint32_t n, uint32_t& base) {
+    constexpr uint32_t NT = NW * 32;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t len = 0, step = 0;
     if (threadIdx.x == 0) sm.stop[0] = 0xffffffffu;
@@ -215,17 +268,18 @@ __device__ __forceinline__ uint32_t gather_item_round(ItemSmem& sm, const GpuCam
         uint32_t mask[kGatherU];
 #pragma unroll
         for (uint32_t u = 0; u < kGatherU; ++u) {
-            const uint32_t i = base + u * kThreads + threadIdx.x;
+            const uint32_t i = base + u * NT + threadIdx.x;
             pass[u] = false;
             if (i < n) {
-                rec[u] = prep_light(cam, lights[i], 1u);
+                const float4 pr = __ldg(reinterpret_cast<const float4*>(lights[i].position_range));
+                prep_light_centre(vr, pr, __ldg(&lights[i].light_type), rec[u]);
                 pass[u] = (rec[u].type == 0u) || sphere_in_planes(g.planes, rec[u].cx, rec[u].cy, rec[u].cz, rec[u].r);
             }
         }
 #pragma unroll
         for (uint32_t u = 0; u < kGatherU; ++u) {
             mask[u] = __ballot_sync(0xffffffffu, pass[u]);
-            if (lane == 0) sm.warp_tot[u * kWarps + warp] = __popc(mask[u]);
+            if (lane == 0) sm.warp_tot[u * NW + warp] = __popc(mask[u]);
         }
         __syncthreads();
         if (threadIdx.x == 0) sm.stop[(step + 1) & 1u] = 0xffffffffu;  // read by the last step before this barrier
@@ -234,18 +288,23 @@ __device__ __forceinline__ uint32_t gather_item_round(ItemSmem& sm, const GpuCam
         for (uint32_t u = 0; u < kGatherU; ++u) {
             uint32_t before = 0, total = 0;
 #pragma unroll
-            for (int w = 0; w < kWarps; ++w) {
-                const uint32_t t = sm.warp_tot[u * kWarps + w];
+            for (int w = 0; w < NW; ++w) {
+                const uint32_t t = sm.warp_tot[u * NW + w];
                 before += (uint32_t(w) < warp) ? t : 0u;
                 total += t;
             }
             if (pass[u]) {
                 const uint32_t pos = run + before + __popc(mask[u] & lanemask_lt());
                 if (pos < kItemCap) {
-                    sm.idx[pos] = base + u * kThreads + threadIdx.x;
-                    sm.bl[pos] = rec[u];
+                    sm.idx[pos] = base + u * NT + threadIdx.x;
+                    BinLight& d = sm.bl[pos];
+                    d.cx = rec[u].cx;
+                    d.cy = rec[u].cy;
+                    d.cz = rec[u].cz;
+                    d.r = rec[u].r;
+                    d.type = rec[u].type;
                 } else {
-                    atomicMin(&sm.stop[step & 1u], base + u * kThreads + threadIdx.x);
+                    atomicMin(&sm.stop[step & 1u], base + u * NT + threadIdx.x);
                 }
             }
             run += total;
@@ -258,8 +317,17 @@ __device__ __forceinline__ uint32_t gather_item_round(ItemSmem& sm, const GpuCam
             break;
         }
         len = run;
-        base += kGatherU * kThreads;
+        base += kGatherU * NT;
         ++step;
+    }
+    for (uint32_t j = threadIdx.x; j < len; j += NT) {
+        BinLight& d = sm.bl[j];
+        if (d.type == 2u) {
+            const GpuLight& l = lights[sm.idx[j]];
+            prep_light_cone(vr, __ldg(reinterpret_cast<const float4*>(l.direction_outer)), __ldg(&l.inner_angle), d);
+        } else {
+            d.cone = 0u;
+        }
     }
     __syncthreads();
     return len;
@@ -268,13 +336,13 @@ __device__ __forceinline__ uint32_t gather_item_round(ItemSmem& sm, const GpuCam
 // Tests a gathered round against the item's slice boxes: counts into sm.slice_run, and
 // with FILL writes the lists from sm.slice_dst. With MASKS the count keeps each chunk's
 // ballot and the fill replays them instead of testing again.
-template <bool FILL>
-__device__ __forceinline__ void test_item_slices(ItemSmem& sm, const ColumnGeom& g, const float* __restrict__ tabz,
+template <int NW, bool FILL>
+__device__ __forceinline__ void test_item_slices(ItemSmemT<NW>& sm, const ColumnGeom& g, const float* __restrict__ tabz,
                                                  uint32_t gz, float zlast, uint32_t s0, uint32_t s1, uint32_t len,
                                                  uint32_t* __restrict__ indices, uint32_t capacity, bool masks) {
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t chunks = (len + 31) / 32;
-    for (uint32_t s = s0 + warp; s < s1; s += kWarps) {
+    for (uint32_t s = s0 + warp; s < s1; s += NW) {
         const uint32_t k = s - s0;
         uint32_t run = sm.slice_run[k];
         const uint32_t dst0 = FILL ? sm.slice_dst[k] : 0u;
@@ -311,7 +379,8 @@ __device__ __forceinline__ void test_item_slices(ItemSmem& sm, const ColumnGeom&
 // Bins item `item` of a view: froxel column item / groups, slices [s0, s1) of the
 // group item % groups (groups of ceil(grid_z / groups) slices). Items of a view are in
 // froxel order, so the item chain's prefix is the first entry of the item's froxels.
-__device__ __forceinline__ void bin_item(ItemSmem& sm, const GpuCamera* __restrict__ cam,
+template <int NW>
+__device__ __forceinline__ void bin_item(ItemSmemT<NW>& sm, const GpuCamera* __restrict__ cam,
                                          const GpuLight* __restrict__ lights, uint32_t n, const hl_froxel_params& p,
                                          const float* __restrict__ tabz, uint32_t item, uint32_t groups,
                                          uint32_t epoch, unsigned long long* __restrict__ chain,
@@ -324,6 +393,7 @@ __device__ __forceinline__ void bin_item(ItemSmem& sm, const GpuCamera* __restri
     const uint32_t ns = s1 - s0;
     const uint32_t items = p.grid_x * p.grid_y * groups;
     const ColumnGeom g = column_geom(cam, p, col % p.grid_x, col / p.grid_x);
+    const ViewRows vr = load_view_rows(cam);
     const float zlast = xmax(tabz[p.grid_z], cam->forward_far[3]);
     for (uint32_t k = threadIdx.x; k < ns; k += blockDim.x) sm.slice_run[k] = 0;
 
@@ -331,11 +401,11 @@ __device__ __forceinline__ void bin_item(ItemSmem& sm, const GpuCamera* __restri
     uint32_t base = 0, len = 0;
     bool one_round = true, masks = false;
     for (bool first = true;; first = false) {
-        len = gather_item_round(sm, cam, lights, g, n, base);
+        len = gather_item_round<NW>(sm, vr, lights, g, n, base);
         if (!first) one_round = false;
         // an item gathered in one round keeps its chunk ballots when they fit
         masks = one_round && base >= n && ns * ((len + 31) / 32) <= kItemMaskCap;
-        test_item_slices<false>(sm, g, tabz, p.grid_z, zlast, s0, s1, len, indices, capacity, masks);
+        test_item_slices<NW, false>(sm, g, tabz, p.grid_z, zlast, s0, s1, len, indices, capacity, masks);
         if (base >= n) break;
     }
     __syncthreads();
@@ -398,20 +468,20 @@ __device__ __forceinline__ void bin_item(ItemSmem& sm, const GpuCamera* __restri
 
     // ---- 3. fill (from the round still in shared memory when there was only one) ----
     if (one_round) {
-        test_item_slices<true>(sm, g, tabz, p.grid_z, zlast, s0, s1, len, indices, capacity, masks);
+        test_item_slices<NW, true>(sm, g, tabz, p.grid_z, zlast, s0, s1, len, indices, capacity, masks);
     } else {
         base = 0;
         for (;;) {
-            len = gather_item_round(sm, cam, lights, g, n, base);
-            test_item_slices<true>(sm, g, tabz, p.grid_z, zlast, s0, s1, len, indices, capacity, false);
+            len = gather_item_round<NW>(sm, vr, lights, g, n, base);
+            test_item_slices<NW, true>(sm, g, tabz, p.grid_z, zlast, s0, s1, len, indices, capacity, false);
             if (base >= n) break;
         }
     }
     __syncthreads();
 }
 
-// Slice groups per column for a grid: enough items for `min_items` (two per SM),
-// at most one group per slice.
+// Slice groups per column for a grid: enough items for `min_items`, at most one group
+// per slice.
 __host__ __device__ inline uint32_t item_groups(const hl_froxel_params& p, uint32_t min_items) {
     const uint32_t cols = p.grid_x * p.grid_y;
     uint32_t g = (min_items + cols - 1) / cols;

@@ -18,7 +18,7 @@ from helio_gb300 import metrics
 from helio_gb300 import native as N
 from helio_gb300 import synthetic as S
 
-from gpu_util import gpu_bin_froxels, gpu_bin_tiles, gpu_shade, gpu_shade_logged
+from gpu_util import assert_tile_lists_equal, gpu_bin_froxels, gpu_bin_tiles, gpu_shade, gpu_shade_logged
 from scenes import mixed_lights
 
 pytestmark = pytest.mark.gpu
@@ -69,6 +69,19 @@ def _check(ctx, cam_rec, glb, lights, gb, grid_shape, kind, tol, counts=False):
 def test_shade_workloads(ctx, wi, kind):
     w = S.workload(wi)
     _check(ctx, w.camera.record, w.globals_, w.lights, w.gbuffer, w.froxel_grid, kind, TOL[w.gbuffer.layout])
+
+
+def test_shade_tiles_truncated_at_the_cap(ctx):
+    """The reference's tile lists keep at most 64 lights per 16x16 tile
+    (light_cull.wgsl:123-180). With 4096 clumped lights on a 960x540 view most tiles
+    overflow: the GPU tile culling keeps the same first 64 lights as the oracle, and
+    the shading over those truncated lists matches the oracle over the same lists."""
+    w = S.workload(2, 0.25)
+    W, H = w.gbuffer.width, w.gbuffer.height
+    lists, counts = oracle.bin_tiles_ref(w.camera.record, w.lights, W, H)
+    assert (counts == 64).mean() > 0.5
+    assert_tile_lists_equal(gpu_bin_tiles(ctx, w.camera.record, w.lights, W, H), (lists, counts))
+    _check(ctx, w.camera.record, w.globals_, w.lights, w.gbuffer, w.froxel_grid, "tiles", TOL[S.LAYOUT_F32])
 
 
 def test_shade_4k_clumped(ctx):
