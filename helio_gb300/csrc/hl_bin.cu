@@ -227,6 +227,14 @@ __global__ void __launch_bounds__(NW * 32, kItemMinBlocks) bin_froxels_items_ker
         s_epoch = *reinterpret_cast<volatile uint32_t*>(&state->epoch) + 1u;
         s_item = uint32_t(atomicAdd(&state->ticket, 1ull) - base);
     }
+    // while the ticket is drawn: the camera and the lights of the first gather step
+    // (one 128-byte line each, every item reads them) on their way to this SM's L1
+    if (threadIdx.x < 3) prefetch_l1(reinterpret_cast<const unsigned char*>(cam) + 128 * threadIdx.x);
+#pragma unroll
+    for (uint32_t u = 0; u < kGatherU; ++u) {
+        const uint32_t i = u * NW * 32 + threadIdx.x;
+        if (i < n) prefetch_l1(lights + i);
+    }
     __syncthreads();
     const uint32_t item = s_item, epoch = s_epoch;
     if (item >= items) {  // launches overlapping on one context: refused

@@ -15,6 +15,12 @@ namespace bin {
 constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
 
+// Asks for the 128-byte line at p in this SM's L1 (no register written, no fault on
+// any address the caller may read).
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -132,25 +138,57 @@ struct ColumnGeom {
 
 __device__ __forceinline__ uint32_t ceil_div_u64(uint64_t a, uint64_t b) { return uint32_t((a + b - 1) / b); }
 
-__device__ __forceinline__ ColumnGeom column_geom(const GpuCamera* cam, const hl_froxel_params& p, uint32_t fx,
-                                                  uint32_t fy) {
+// The NDC rectangle of froxel column (fx, fy): its pixel edges, as the reference forms
+// a tile's (light_cull.wgsl:140-147).
+struct ColumnRect {
+    float left, right, top, bottom;
+};
+
+__device__ __forceinline__ ColumnRect column_rect(const hl_froxel_params& p, uint32_t fx, uint32_t fy) {
     const uint32_t px0 = ceil_div_u64(uint64_t(fx) * p.width, p.grid_x);
     const uint32_t px1 = ceil_div_u64(uint64_t(fx + 1) * p.width, p.grid_x);
     const uint32_t py0 = ceil_div_u64(uint64_t(fy) * p.height, p.grid_y);
     const uint32_t py1 = ceil_div_u64(uint64_t(fy + 1) * p.height, p.grid_y);
     const float fw = float(p.width), fh = float(p.height);
-    const float left = xsub(xmul(xdiv(float(px0), fw), 2.0f), 1.0f);
-    const float right = xsub(xmul(xdiv(float(px1), fw), 2.0f), 1.0f);
-    const float top = xsub(1.0f, xmul(xdiv(float(py0), fh), 2.0f));
-    const float bottom = xsub(1.0f, xmul(xdiv(float(py1), fh), 2.0f));
+    ColumnRect r;
+    r.left = xsub(xmul(xdiv(float(px0), fw), 2.0f), 1.0f);
+    r.right = xsub(xmul(xdiv(float(px1), fw), 2.0f), 1.0f);
+    r.top = xsub(1.0f, xmul(xdiv(float(py0), fh), 2.0f));
+    r.bottom = xsub(1.0f, xmul(xdiv(float(py1), fh), 2.0f));
+    return r;
+}
+
+__device__ __forceinline__ ColumnGeom column_geom(const GpuCamera* cam, const hl_froxel_params& p, uint32_t fx,
+                                                  uint32_t fy) {
+    const ColumnRect c = column_rect(p, fx, fy);
     const float p00 = cam->proj[0], p11 = cam->proj[5];
     ColumnGeom g;
-    g.planes = rect_planes(p00, p11, left, right, top, bottom);
-    g.kx0 = xdiv(left, p00);
-    g.kx1 = xdiv(right, p00);
-    g.ky_bot = xdiv(bottom, p11);
-    g.ky_top = xdiv(top, p11);
+    g.planes = rect_planes(p00, p11, c.left, c.right, c.top, c.bottom);
+    g.kx0 = xdiv(c.left, p00);
+    g.kx1 = xdiv(c.right, p00);
+    g.ky_bot = xdiv(c.bottom, p11);
+    g.ky_top = xdiv(c.top, p11);
     return g;
+}
+
+// One fifth of column_geom, by the same operations: part 0-3 the plane rect_planes puts
+// at that index, part 4 the slopes. Five lanes build a column's geometry side by side.
+__device__ __forceinline__ void column_geom_part(const GpuCamera* cam, const hl_froxel_params& p, uint32_t fx,
+                                                 uint32_t fy, uint32_t part, ColumnGeom& g) {
+    const ColumnRect c = column_rect(p, fx, fy);
+    const float p00 = __ldg(&cam->proj[0]), p11 = __ldg(&cam->proj[5]);
+    switch (part) {
+        case 0: g.planes.n[0] = plane_from_ndc_edge(p00, p11, c.left, c.bottom, c.left, c.top); break;
+        case 1: g.planes.n[1] = plane_from_ndc_edge(p00, p11, c.right, c.top, c.right, c.bottom); break;
+        case 2: g.planes.n[2] = plane_from_ndc_edge(p00, p11, c.left, c.top, c.right, c.top); break;
+        case 3: g.planes.n[3] = plane_from_ndc_edge(p00, p11, c.right, c.bottom, c.left, c.bottom); break;
+        default:
+            g.kx0 = xdiv(c.left, p00);
+            g.kx1 = xdiv(c.right, p00);
+            g.ky_bot = xdiv(c.bottom, p11);
+            g.ky_top = xdiv(c.top, p11);
+            break;
+    }
 }
 
 struct Box {
@@ -216,6 +254,7 @@ constexpr uint32_t kItemMaskCap = 1024; // (slice, 32-light chunk) ballots kept 
 constexpr uint32_t kFlagAggregate = 1u, kFlagPrefix = 2u;
 constexpr uint32_t kChainValueMax = (1u << 30) - 1u;
 constexpr uint32_t kLookbackSpins = 1u << 20;  // ~0.1 s of polling before HL_ERR_TIMEOUT
+constexpr uint32_t kLookbackWords = 4;         // chain words per lane in one look-back read
 
 template <int NW>
 struct ItemSmemT {
@@ -227,6 +266,7 @@ struct ItemSmemT {
     uint32_t slice_dst[kMaxSlices];   // first entry of each slice
     uint32_t stop[2];                 // first light index not kept by a full round (by step parity)
     uint32_t excl, total;
+    ColumnGeom geom;                  // the item's column
 };
 using ItemSmem = ItemSmemT<kWarps>;  // the 256-thread CTAs of the persistent batched launch
 
@@ -240,8 +280,9 @@ __device__ __forceinline__ unsigned long long ld_chain(const unsigned long long*
     return *reinterpret_cast<const volatile unsigned long long*>(p);
 }
 
+// A chain word carries its whole message (state and value) in one 8-byte store, and
+// the items that read it read nothing else this item wrote: no fence is needed.
 __device__ __forceinline__ void st_chain(unsigned long long* p, uint32_t epoch, uint32_t state, uint32_t value) {
-    __threadfence();
     *reinterpret_cast<volatile unsigned long long*>(p) =
         (static_cast<unsigned long long>(epoch) << 32) | (state << 30) | min(value, kChainValueMax);
 }
@@ -392,10 +433,12 @@ __device__ __forceinline__ void bin_item(ItemSmemT<NW>& sm, const GpuCamera* __r
     const uint32_t s0 = min(grp * spg, p.grid_z), s1 = min(s0 + spg, p.grid_z);
     const uint32_t ns = s1 - s0;
     const uint32_t items = p.grid_x * p.grid_y * groups;
-    const ColumnGeom g = column_geom(cam, p, col % p.grid_x, col / p.grid_x);
+    if (warp == 0 && lane < 5) column_geom_part(cam, p, col % p.grid_x, col / p.grid_x, lane, sm.geom);
     const ViewRows vr = load_view_rows(cam);
     const float zlast = xmax(tabz[p.grid_z], cam->forward_far[3]);
     for (uint32_t k = threadIdx.x; k < ns; k += blockDim.x) sm.slice_run[k] = 0;
+    __syncthreads();
+    const ColumnGeom g = sm.geom;
 
     // ---- 1. count ----
     uint32_t base = 0, len = 0;
@@ -413,31 +456,60 @@ __device__ __forceinline__ void bin_item(ItemSmemT<NW>& sm, const GpuCamera* __r
     // ---- 2. chained scan over the items ----
     if (warp == 0) {
         const bool publish = item != test.stall;
-        if (lane == 0) {
-            uint32_t acc = 0;
-            for (uint32_t k = 0; k < ns; ++k) {
-                sm.slice_dst[k] = acc;
-                acc += sm.slice_run[k];
+        uint32_t acc = 0;  // exclusive scan of the slice counts, 32 slices at a time
+        for (uint32_t k0 = 0; k0 < ns; k0 += 32) {
+            const uint32_t k = k0 + lane;
+            const uint32_t r = k < ns ? sm.slice_run[k] : 0u;
+            uint32_t v = r;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= uint32_t(o)) v += u;
             }
+            if (k < ns) sm.slice_dst[k] = acc + v - r;
+            acc += __shfl_sync(0xffffffffu, v, 31);
+        }
+        if (lane == 0) {
             sm.total = acc;
             if (publish) st_chain(chain + item, epoch, item == 0 ? kFlagPrefix : kFlagAggregate, acc);
         }
         __syncwarp();
+        // look-back: the warp reads kLookbackWords x 32 predecessors at once (item - 1
+        // down), finds the nearest one holding an inclusive prefix (before item 0: a
+        // prefix of 0) and sums that prefix and the bare totals after it; a window of
+        // totals only is added whole and the walk goes on below it
         uint32_t excl = 0;
-        int32_t pred = int32_t(item) - 1;
+        int32_t hi = int32_t(item) - 1;
         uint32_t spins = 0;
-        while (pred >= 0) {
-            const int32_t c = pred - int32_t(lane);
-            uint32_t st = kFlagPrefix, val = 0;  // before item 0: a prefix of 0
-            if (c >= 0) {
-                const unsigned long long w = ld_chain(chain + c);
-                st = uint32_t(w >> 32) == epoch ? (uint32_t(w) >> 30) : 0u;
-                val = uint32_t(w) & kChainValueMax;
+        while (hi >= 0) {
+            uint32_t st[kLookbackWords], val[kLookbackWords];
+#pragma unroll
+            for (uint32_t k = 0; k < kLookbackWords; ++k) {
+                const int32_t c = hi - int32_t(lane + 32u * k);
+                st[k] = kFlagPrefix;
+                val[k] = 0;
+                if (c >= 0) {
+                    const unsigned long long w = ld_chain(chain + c);
+                    st[k] = uint32_t(w >> 32) == epoch ? (uint32_t(w) >> 30) : 0u;
+                    val[k] = uint32_t(w) & kChainValueMax;
+                }
             }
-            const uint32_t pm = __ballot_sync(0xffffffffu, st == kFlagPrefix);
-            const int stop = pm ? __ffs(pm) - 1 : 31;  // lanes 0..stop are summed
-            const uint32_t upto = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
-            if (__ballot_sync(0xffffffffu, st == 0u) & upto) {
+            // offset (lane + 32 k) of the nearest prefix this lane holds
+            uint32_t near = 0xffffffffu;
+#pragma unroll
+            for (int k = int(kLookbackWords) - 1; k >= 0; --k)
+                if (st[k] == kFlagPrefix) near = lane + 32u * uint32_t(k);
+            near = __reduce_min_sync(0xffffffffu, near);
+            bool missing = false;
+            uint32_t sum = 0;
+#pragma unroll
+            for (uint32_t k = 0; k < kLookbackWords; ++k) {
+                if (lane + 32u * k <= near) {
+                    missing |= st[k] == 0u;
+                    sum += val[k];
+                }
+            }
+            if (__any_sync(0xffffffffu, missing)) {  // a predecessor has not published yet
                 if (++spins > test.spins) {
                     if (lane == 0) raise_status(status, HL_ERR_TIMEOUT);
                     break;
@@ -445,9 +517,9 @@ __device__ __forceinline__ void bin_item(ItemSmemT<NW>& sm, const GpuCamera* __r
                 __nanosleep(64);
                 continue;
             }
-            excl += __reduce_add_sync(0xffffffffu, uint32_t(lane) <= uint32_t(stop) ? val : 0u);
-            if (pm) break;
-            pred -= 32;
+            excl += __reduce_add_sync(0xffffffffu, sum);
+            if (near != 0xffffffffu) break;
+            hi -= int32_t(32u * kLookbackWords);
         }
         if (lane == 0) {
             if (item > 0 && publish) st_chain(chain + item, epoch, kFlagPrefix, excl + sm.total);

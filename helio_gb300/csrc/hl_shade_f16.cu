@@ -726,13 +726,16 @@ __global__ void __launch_bounds__(f16k::kThreads, 3) batch_persistent_kernel(
     }
 }
 
-template <class K>
-cudaError_t smem_attr(K kern, int smem) {
-    static unsigned long long attr_devices = 0;  // devices on which the smem limit is raised
+// Raises KERN's dynamic shared-memory limit once per device. The kernel is a template
+// argument so that every kernel has its own record: instantiations of one kernel
+// template for different targets share a signature but are different functions.
+template <auto KERN>
+cudaError_t smem_attr(int smem) {
+    static unsigned long long attr_devices = 0;  // devices on which KERN's limit is raised
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 64 && !(attr_devices & (1ull << dev))) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaError_t e = cudaFuncSetAttribute(KERN, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
         attr_devices |= 1ull << dev;
     }
@@ -745,7 +748,7 @@ cudaError_t launch_target(const void* camera, const void* globals, const GBufVie
                           float4* cand, const PairLog& log, cudaStream_t stream) {
     auto kern = shade_f16_kernel<TARGET>;
     const int smem = int(sizeof(f16k::Smem));
-    cudaError_t ea = smem_attr(kern, smem);
+    cudaError_t ea = smem_attr<shade_f16_kernel<TARGET>>(smem);
     if (ea != cudaSuccess) return ea;
     if (n > 0) {
         cudaError_t e = launch_prep_cand(camera, lights, n, true, cand, stream);
@@ -769,8 +772,8 @@ cudaError_t launch_batch_persistent(uint32_t target_format, const BinViewDesc* b
     const int smem = int(batch_persistent_smem());
     const bool h = target_format == HL_TARGET_RGBA16F;
     auto kern = h ? batch_persistent_kernel<HL_TARGET_RGBA16F> : batch_persistent_kernel<HL_TARGET_RGBA32F>;
-    cudaError_t e = h ? smem_attr(batch_persistent_kernel<HL_TARGET_RGBA16F>, smem)
-                      : smem_attr(batch_persistent_kernel<HL_TARGET_RGBA32F>, smem);
+    cudaError_t e = h ? smem_attr<batch_persistent_kernel<HL_TARGET_RGBA16F>>(smem)
+                      : smem_attr<batch_persistent_kernel<HL_TARGET_RGBA32F>>(smem);
     if (e != cudaSuccess) return e;
     kern<<<grid, f16k::kThreads, smem, stream>>>(bd, sd, n_views, tiles, total_bin, total_tiles,
                                                   static_cast<const DeferredGlobals*>(globals),
@@ -784,8 +787,8 @@ uint32_t batch_persistent_grid(int device) {
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms <= 0) sms = 1;
     int per_sm = 0;
     // the shared-memory limit first: the occupancy query respects the kernel's attribute
-    if (smem_attr(batch_persistent_kernel<HL_TARGET_RGBA32F>, int(batch_persistent_smem())) != cudaSuccess ||
-        smem_attr(batch_persistent_kernel<HL_TARGET_RGBA16F>, int(batch_persistent_smem())) != cudaSuccess)
+    if (smem_attr<batch_persistent_kernel<HL_TARGET_RGBA32F>>(int(batch_persistent_smem())) != cudaSuccess ||
+        smem_attr<batch_persistent_kernel<HL_TARGET_RGBA16F>>(int(batch_persistent_smem())) != cudaSuccess)
         cudaGetLastError();
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_persistent_kernel<HL_TARGET_RGBA32F>,
                                                       f16k::kThreads, batch_persistent_smem()) != cudaSuccess ||
@@ -800,8 +803,8 @@ cudaError_t launch_shade_f16_batched(uint32_t target_format, const ShadeViewDesc
     const int smem = int(sizeof(f16k::Smem));
     const bool h = target_format == HL_TARGET_RGBA16F;
     auto kern = h ? shade_f16_batched_kernel<HL_TARGET_RGBA16F> : shade_f16_batched_kernel<HL_TARGET_RGBA32F>;
-    cudaError_t e = h ? smem_attr(shade_f16_batched_kernel<HL_TARGET_RGBA16F>, smem)
-                      : smem_attr(shade_f16_batched_kernel<HL_TARGET_RGBA32F>, smem);
+    cudaError_t e = h ? smem_attr<shade_f16_batched_kernel<HL_TARGET_RGBA16F>>(smem)
+                      : smem_attr<shade_f16_batched_kernel<HL_TARGET_RGBA32F>>(smem);
     if (e != cudaSuccess) return e;
     kern<<<total_tiles, f16k::kThreads, smem, stream>>>(descs, n_views, static_cast<const DeferredGlobals*>(globals),
                                                          static_cast<const GpuLight*>(lights), n, status);

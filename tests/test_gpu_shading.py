@@ -125,14 +125,24 @@ def test_shade_debug_modes(ctx):
         np.testing.assert_allclose(img[m], ref[m], rtol=1e-6, atol=1e-6)
 
 
-def test_shade_rgba16f_target(ctx):
-    w = S.workload(0, scale=0.5)
+@pytest.mark.parametrize("wi", [0, 1])  # FP32 G-buffer (shade_kernel), FP16 G-buffer (shade_f16_kernel)
+def test_shade_rgba16f_target(ctx, wi):
+    """The reference's own output format (RGBA16F, like pre_aa): each texel is the
+    RGBA32F result rounded once to half precision, after an RGBA32F launch of the same
+    kernel (both target instantiations launched in one process)."""
+    w = S.workload(wi, scale=0.5)
     df = FR.upload_workload(w)
     ogrid, dgrid, keep = _grids(ctx, w.camera.record, w.lights, w.gbuffer, w.froxel_grid, "froxels")
+    img32, pairs = gpu_shade_logged(ctx, df, dgrid)
     img = gpu_shade(ctx, df, dgrid, target_format=N.TARGET_RGBA16F)
-    ref = oracle.shade(w.camera.record, w.globals_, w.gbuffer, w.lights, ogrid)
+    np.testing.assert_array_equal(img, img32.astype(np.float32).astype(np.float16).astype(np.float64))
+    ref, flips, _ = oracle.shade_forced(w.camera.record, w.globals_, w.gbuffer, w.lights, ogrid, pairs)
     m = ~np.isnan(ref[..., 0])
-    np.testing.assert_allclose(img[m][:, :3], ref[m][:, :3], rtol=2e-3, atol=1e-6)
+    # the kernel's tolerance plus one rounding to half: 2^-11 relative for normal halves,
+    # half of the subnormal spacing (2^-25) below 2^-14
+    r = np.abs(ref[m][:, :3])
+    tol = (TOL[w.gbuffer.layout][1] + 2.0 ** -11) * np.maximum(r, 1e-6 * r.max()) + 2.0 ** -25  # floor as metrics
+    assert (np.abs(img[m][:, :3] - ref[m][:, :3]) <= tol).all()
 
 
 def test_shade_uses_gpu_lists(ctx):
