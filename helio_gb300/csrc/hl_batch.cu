@@ -142,7 +142,10 @@ hl_status build_plan(hl_ctx* ctx, const std::vector<HostView>& views, const std:
         }
         const uint64_t F = uint64_t(fp.grid_x) * fp.grid_y * fp.grid_z;
         f_base[v + 1] = f_base[v] + F;
-        o_base[v + 1] = o_base[v] + F + 1;
+        // every view's offsets and indices start on a 128-byte line of their own: no line
+        // holds two views' lists (the persistent launch reads a view's lists through L1
+        // once that view's binning has finished, while other views are still binned)
+        o_base[v + 1] = o_base[v] + ((F + 1 + 31) & ~31ull);
         std::memset(&bd[v], 0, sizeof bd[v]);
         bd[v].camera = views[v].camera;
         bd[v].p = fp;
@@ -201,7 +204,7 @@ hl_status build_plan(hl_ctx* ctx, const std::vector<HostView>& views, const std:
     std::vector<uint64_t> i_base(V + 1, 0);
     for (uint32_t v = 0; v < V; ++v) {
         const uint64_t cap = std::max<uint64_t>(1024, 2ull * totals[v]);
-        i_base[v + 1] = i_base[v] + cap;
+        i_base[v + 1] = i_base[v] + ((cap + 31) & ~31ull);
     }
     if (i_base[V] > 0xFFFFFFFFull) {
         free_plan(p);

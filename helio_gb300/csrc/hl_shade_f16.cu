@@ -225,11 +225,17 @@ __device__ __noinline__ void flush32(f16k::Smem& s, const uint32_t* queue, uint3
     __syncwarp();
 }
 
-// A load of the froxel lists: through the read-only path, or (COHERENT) from L2 when
-// the lists were written earlier in the same launch (the persistent batched launch).
+// A load of the froxel lists: through the read-only path, or (COHERENT) by a plain
+// L1-cached load (ld.global.ca) when the lists were written earlier in the same launch
+// (the persistent batched launch). The read-only path may not be used for data written
+// during the launch; a plain load may be, once ordered after the writes: a view's
+// shading reads its lists only after thread 0 has seen every binning item of the view
+// finish (the counter the items raise after a fence, read and followed by a fence) and
+// the CTA barrier has passed that on, and no cache line holds two views' lists, so L1
+// never holds a line of them from before they were written.
 template <bool COHERENT>
 __device__ __forceinline__ uint32_t list_ld(const uint32_t* p) {
-    return COHERENT ? __ldcg(p) : __ldg(p);
+    return COHERENT ? __ldca(p) : __ldg(p);
 }
 
 // Lights the 32x16 tile (bx, by) of one view. prefetch_next: the tile index (row-major
