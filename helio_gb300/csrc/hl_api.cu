@@ -66,7 +66,8 @@ hl_status shade_common(hl_ctx* ctx, const void* camera, const void* globals, con
     }
     DeviceGuard dg(ctx->device);
     if (!dg.ok) return fail(ctx, HL_ERR_CUDA, "cudaSetDevice(%d) failed", ctx->device);
-    if ((s = ensure(ctx, ctx->shade_cand, ctx->shade_cand_cap, n_lights > 0 ? n_lights : 1, "shade light table")) !=
+    if ((s = ensure(ctx, ctx->shade_cand, ctx->shade_cand_cap, hl::cand_table_len(n_lights > 0 ? n_lights : 1),
+                    "shade light table")) !=
         HL_OK)
         return s;
     cudaError_t e = hl::launch_shade(gbuffer->layout, grid->kind, stats ? HL_TARGET_RGBA32F : radiance->format, camera,

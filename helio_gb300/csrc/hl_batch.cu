@@ -169,7 +169,7 @@ hl_status build_plan(hl_ctx* ctx, const std::vector<HostView>& views, const std:
     cudaError_t e = cudaMalloc(&p->d_bin, sizeof(hl::BinViewDesc) * V);
     if (e == cudaSuccess) e = cudaMalloc(&p->d_shade, sizeof(hl::ShadeViewDesc) * V);
     if (e == cudaSuccess) e = cudaMalloc(&p->bl, sizeof(hl::BinLight) * size_t(V) * std::max(n_lights, 1u));
-    if (e == cudaSuccess) e = cudaMalloc(&p->cand, sizeof(float4) * size_t(V) * std::max(n_lights, 1u));
+    if (e == cudaSuccess) e = cudaMalloc(&p->cand, sizeof(float4) * size_t(V) * hl::cand_table_len(std::max(n_lights, 1u)));
     if (e == cudaSuccess) e = cudaMalloc(&p->counts, sizeof(uint32_t) * std::max<uint64_t>(f_base[V], 1));
     if (e == cudaSuccess) e = cudaMalloc(&p->offsets, sizeof(uint32_t) * o_base[V]);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->capture_stream, cudaStreamNonBlocking);
@@ -271,7 +271,7 @@ hl_status build_plan(hl_ctx* ctx, const std::vector<HostView>& views, const std:
         g.tiles = 0;
         g.fp = bd[v].p;
         sd[v].grid = g;
-        sd[v].cand = p->cand + size_t(v) * n_lights;
+        sd[v].cand = p->cand + size_t(v) * hl::cand_table_len(n_lights);
         sd[v].tabz = reinterpret_cast<const float*>(reinterpret_cast<const unsigned char*>(p->d_bin + v) +
                                                     offsetof(hl::BinViewDesc, tab));
     }

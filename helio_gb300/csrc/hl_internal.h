@@ -48,7 +48,7 @@ struct ShadeViewDesc {
     GridView grid;
     TargetView out;
     const float* tabz;     // the view's slice boundaries (device memory)
-    float4* cand;          // n_lights entries: the view's candidate-test light table
+    float4* cand;          // cand_table_len(n_lights) entries: the view's candidate-test light table
     uint32_t tiles_x;      // 32x16 tiles per row
     uint32_t tile_start;   // first CTA of this view in the batched launch
 };
@@ -103,6 +103,10 @@ cudaError_t launch_shade(uint32_t layout, uint32_t grid_kind, uint32_t target_fo
                          const GridView& grid, const SliceTable& tab, const TargetView& out, uint32_t* stats,
                          int* status, float4* cand, const PairLog& log, cudaStream_t stream,
                          const ExtView* ext = nullptr);
+
+// Length in float4 of a candidate-test light table of n lights: n candidate records
+// followed by n floats, each light's largest colour channel times its intensity.
+constexpr size_t cand_table_len(uint32_t n) { return size_t(n) + (size_t(n) + 3) / 4; }
 
 // The candidate-test light table of the shading kernels: per light its position
 // (camera-relative when `relative`) and range^2 (1 + 2^-9), or -1 for a directional

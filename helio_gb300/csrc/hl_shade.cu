@@ -775,6 +775,13 @@ __device__ __forceinline__ float4 cand_entry(const GpuCamera* __restrict__ cam, 
     return c;
 }
 
+// The light's largest colour channel times its intensity: with the attenuation it bounds
+// the radiance that pbr_direct_light compares with its 0.002 cut.
+__device__ __forceinline__ float cand_peak(const GpuLight& l) {
+    const float4 c = *reinterpret_cast<const float4*>(l.color_intensity);
+    return fmaxf(fmaxf(c.x, c.y), c.z) * c.w;
+}
+
 // Launched as a dependent of whatever precedes it (the binning, in a frame): it reads
 // only the camera and the lights, and waits for its predecessor before it ends, so the
 // shading kernel that waits for it also waits for the lists.
@@ -783,7 +790,10 @@ __global__ void __launch_bounds__(256) prep_cand_kernel(const GpuCamera* __restr
                                                         uint32_t relative, float4* __restrict__ out) {
     pdl_launch_dependents();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = cand_entry(cam, lights[i], relative != 0u);
+    if (i < n) {
+        out[i] = cand_entry(cam, lights[i], relative != 0u);
+        reinterpret_cast<float*>(out + n)[i] = cand_peak(lights[i]);
+    }
     pdl_wait();
 }
 
@@ -792,7 +802,10 @@ __global__ void __launch_bounds__(256) prep_cand_batched_kernel(const ShadeViewD
                                                                 uint32_t relative) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const ShadeViewDesc& v = d[blockIdx.y];
-    if (i < n) v.cand[i] = cand_entry(static_cast<const GpuCamera*>(v.camera), lights[i], relative != 0u);
+    if (i < n) {
+        v.cand[i] = cand_entry(static_cast<const GpuCamera*>(v.camera), lights[i], relative != 0u);
+        reinterpret_cast<float*>(v.cand + n)[i] = cand_peak(lights[i]);
+    }
 }
 
 template <uint32_t LAYOUT, uint32_t TARGET>

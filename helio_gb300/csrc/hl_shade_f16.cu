@@ -178,6 +178,25 @@ __device__ __forceinline__ float4 eval_pair(const f16k::Smem& s, uint32_t q, uin
     return o;
 }
 
+// The walk's test of a candidate pair (pixel at p, normal n; light record a, peak its
+// largest colour channel times intensity): inside the widened range, in front of the
+// surface (|N.t| within sqrt(slack) of zero is left to the exact NdL cut), and not surely
+// below the radiance cut of pbr_direct_light. The radiance bound takes the falloff with
+// the widened range (no smaller than the true one) plus 2^-20 and 2^-8 to spare, so that
+// no rounding of the fast or the precise evaluation reaches 0.002 on a pair it drops:
+// those pairs would be evaluated only to be cut. Directional lights always pass.
+__device__ __forceinline__ bool walk_test(float px, float py, float pz, float nx, float ny, float nz, const float4& a,
+                                          float peak, float slack) {
+    if (a.w < 0.0f) return true;
+    const float tx = a.x - px, ty = a.y - py, tz = a.z - pz;
+    const float d2 = fma_(tz, tz, fma_(ty, ty, tx * tx));
+    const float ndl = fma_(nz, tz, fma_(ny, ty, nx * tx));
+    if (!(d2 <= a.w) || !(ndl > 0.0f || ndl * ndl <= slack)) return false;
+    const float q = d2 * rcpn_(a.w);
+    const float bound = peak * (fmax_(fma_(-q, q, 1.0f), 0.0f) + (1.0f / 1048576.0f)) * rcpn_(d2 + 0.0001f);
+    return !(bound * (1.0f + 1.0f / 256.0f) < kRadianceCut);
+}
+
 // Records lit pairs for a verifier (hl_set_pair_log); a no-op without a log.
 __device__ __forceinline__ void log_pair(const PairLog& log, bool lit, uint32_t lane, uint32_t x, uint32_t y,
                                          uint32_t W, uint32_t li) {
@@ -345,9 +364,10 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
                 // the depth to a few ulp)
                 const float dv = nrfr * rcpn_(fma_(-depth, frmnr, fr));
                 const float sf = __log2f(dv * slice_inv_near) * slice_scale;
-                uint32_t sl = uint32_t(min(max(int(sf), 0), int(fp.grid_z) - 1));
-                while (sl + 1 < fp.grid_z && s.u.sort.tab[sl + 1] <= dv) ++sl;
-                while (sl > 0 && s.u.sort.tab[sl] > dv) --sl;
+                // (near a slice boundary the rounding of this scale may give the
+                // neighbouring slice: both lists hold every light that reaches the pixel,
+                // a froxel's box being widened by 2^-10 of its far depth)
+                const uint32_t sl = uint32_t(min(max(int(sf), 0), int(fp.grid_z) - 1));
                 const uint32_t fx = s.u.sort.col_of[x - x0];
                 const uint32_t fy = s.u.sort.row_of[y - y0];
                 s.w.walk.fidx[i] = (fy * fp.grid_x + fx) * fp.grid_z + sl;
@@ -491,8 +511,8 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
                     smask &= smask - 1;
                     li = list_ld<COHERENT>(grid.lists + cb + bit);
                     const float4 a = __ldg(cand + li);
-                    pass = a.w < 0.0f || candidate(px, py, pz, 0.0f, 0.0f, 0.0f, nx, ny, nz, a.x, a.y, a.z, a.w,
-                                                   slack, true);
+                    const float peak = __ldg(reinterpret_cast<const float*>(cand + n_lights) + li);
+                    pass = walk_test(px, py, pz, nx, ny, nz, a, peak, slack);
                 }
                 const uint32_t pm = __ballot_sync(0xffffffffu, pass);
                 if (pass) queue[(head + qlen + __popc(pm & lanemask_lt())) & (kQueue - 1)] = (i << 23) | li;
