@@ -49,7 +49,7 @@ struct hl_batch_plan {
     // the persistent form (FP16 G-buffers): binning and shading items in one launch
     bool persistent = false;
     uint32_t total_bin = 0, grid_ctas = 0;
-    uint2* tiles = nullptr;                 // shading work list: (view, tile), heaviest views first
+    uint2* tiles = nullptr;                 // work list: (view, binning item), then (view, tile)
     unsigned long long* chain = nullptr;    // one word per binning item
     hl::BinChainState* state = nullptr;     // ticket counter and epoch
     uint32_t* view_done = nullptr;          // binning items finished per view, over all launches
@@ -221,12 +221,6 @@ hl_status build_plan(hl_ctx* ctx, const std::vector<HostView>& views, const std:
     if (layout == HL_GBUF_F16) {
         int sms = 1;
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess || sms <= 0) sms = 1;
-        uint64_t items = 0;
-        for (uint32_t v = 0; v < V; ++v) {
-            bd[v].groups = p->total_cols >= 2u * uint32_t(sms) ? 1u : hl::bin::item_groups(bd[v].p, 2u * uint32_t(sms));
-            bd[v].item_start = uint32_t(items);
-            items += uint64_t(bd[v].p.grid_x) * bd[v].p.grid_y * bd[v].groups;
-        }
         std::vector<uint32_t> order(V);
         for (uint32_t v = 0; v < V; ++v) order[v] = v;
         // list entries per froxel column: the mean length of a view's pixel lists, up to the slice count
@@ -235,17 +229,27 @@ hl_status build_plan(hl_ctx* ctx, const std::vector<HostView>& views, const std:
             const double cb = double(totals[b]) / (double(bd[b].p.grid_x) * bd[b].p.grid_y);
             return ca > cb;
         });
+        // the views' binning items in the same order as their shading items, so that the
+        // first shading items find their view's lists finished earliest
+        uint64_t items = 0;
+        for (uint32_t v : order) {
+            bd[v].groups = p->total_cols >= 2u * uint32_t(sms) ? 1u : hl::bin::item_groups(bd[v].p, 2u * uint32_t(sms));
+            bd[v].item_start = uint32_t(items);
+            const uint32_t n_items = bd[v].p.grid_x * bd[v].p.grid_y * bd[v].groups;
+            for (uint32_t k = 0; k < n_items; ++k) work.push_back(make_uint2(v, k));
+            items += n_items;
+        }
         for (uint32_t v : order) {
             const uint32_t nt = sd[v].tiles_x * ((views[v].gb.height + 15) / 16);
             for (uint32_t t = 0; t < nt; ++t) work.push_back(make_uint2(v, t));
         }
-        if (items + work.size() > 0x7FFFFFFFull) {
+        if (work.size() > 0x7FFFFFFFull) {
             free_plan(p);
-            return fail(ctx, HL_ERR_SIZE, "batch has %llu work items", (unsigned long long)(items + work.size()));
+            return fail(ctx, HL_ERR_SIZE, "batch has %llu work items", (unsigned long long)work.size());
         }
         p->persistent = true;
         p->total_bin = uint32_t(items);
-        p->grid_ctas = std::min<uint32_t>(hl::batch_persistent_grid(p->device), uint32_t(items + work.size()));
+        p->grid_ctas = std::min<uint32_t>(hl::batch_persistent_grid(p->device), uint32_t(work.size()));
         e = cudaMalloc(&p->tiles, sizeof(uint2) * std::max<size_t>(work.size(), 1));
         if (e == cudaSuccess) e = cudaMalloc(&p->chain, sizeof(unsigned long long) * std::max<uint64_t>(items, 1));
         if (e == cudaSuccess) e = cudaMalloc(&p->state, sizeof(hl::BinChainState));

@@ -2,9 +2,9 @@
 // G-buffer over froxel lists, the headline form of hl_shade.
 //
 // One CTA of 256 threads lights a 32x16-pixel tile:
-//  1. threads decode the tile's G-buffer texels (coalesced along x) and set each pixel
+//  1. threads load the tile's G-buffer texels (coalesced along x) first and set each pixel
 //     up into a shared-memory record: camera-relative position, unit normal, NdV, F0,
-//     albedo/pi and the view's BRDF constants, with its froxel;
+//     albedo and the view's BRDF constants, with its froxel;
 //  2. pixels are counting-sorted by froxel and, inside a froxel, by a depth sub-bin of
 //     its slice, so that a group of 32 consecutive sorted pixels spans one froxel (or
 //     a few of adjacent slices) and a narrow depth range;
@@ -18,10 +18,11 @@
 //     list, in list order;
 //  4. queued (pixel, light) pairs are evaluated 32 at a time, one per lane, and added
 //     into per-pixel Kahan accumulators in queue order, which is list order for every
-//     pixel, as the reference's light loop (deferred_lighting.wgsl:1119-1146) adds them.
-//     The pairs left in the warps' queues at the end are evaluated together, 32 per
-//     warp, and each warp then adds its own in order;
-//  5. threads compose hemisphere ambient and store their pixels.
+//     pixel, as the reference's light loop (deferred_lighting.wgsl:1119-1146) adds them;
+//  5. when no group is left, a warp evaluates the pairs left in its queue and stores the
+//     pixels of the groups it walked (hemisphere ambient added): every pair of a pixel
+//     is queued, evaluated and accumulated by the warp that walked its group, so the
+//     warps finish the tile without waiting for one another.
 #include <algorithm>
 
 #include "hl_bin_item.cuh"
@@ -55,7 +56,7 @@ struct Rec {
     float4 p;   // camera-relative position (f32), 1 / |P| (V = -P / |P|)
     float4 n;   // unit normal, max(N.V, 0)
     float4 f0;  // F0 rgb, NDC depth (negative: seen at a grazing angle, every pair precise)
-    float4 d;   // albedo / pi rgb, metallic
+    float4 d;   // albedo rgb, metallic
     float4 b;   // roughness^4, (r+1)^2/8, Schlick-GGX of the view, unused
 };
 static_assert(sizeof(Rec) == 80, "pixel record");
@@ -71,18 +72,11 @@ struct Smem {
         } sort;
         uint32_t queue[kWarps][kQueue];  // walk: ring of (pixel << 23) | light index
     } u;
-    union {
-        struct {
-            uint32_t fidx[NPX];    // froxel of the pixel
-            uint16_t order[NPX];   // pixels sorted by key
-        } walk;
-        struct {
-            uint32_t left[kThreads];  // pairs left in the warps' queues
-            float4 res[kThreads];     // their contributions (w: status)
-        } tail;
+    struct {
+        uint32_t fidx[NPX];    // froxel of the pixel
+        uint16_t order[NPX];   // pixels sorted by key
     } w;
-    uint32_t warp_tot[kWarps];
-    uint32_t n_valid, next_group, n_left;
+    uint32_t n_valid, next_group;
     uint32_t fx0, fy0, ncx, ncols, kshift, by_column;
 };
 
@@ -149,7 +143,7 @@ __device__ __forceinline__ float4 eval_pair(const f16k::Smem& s, uint32_t q, uin
     p.Vz = -p.Pz * r0.w;
     p.NdV = r1.w;
     p.f0r = r2.x; p.f0g = r2.y; p.f0b = r2.z;
-    p.dr = r3.x; p.dg = r3.y; p.db = r3.z;
+    p.dr = r3.x * kInvPi; p.dg = r3.y * kInvPi; p.db = r3.z * kInvPi;
     PixelBrdf pb;
     pb.a2 = r4.x;
     pb.k = r4.y;
@@ -230,8 +224,9 @@ __device__ __forceinline__ void accumulate(f16k::Smem& s, bool lit, uint32_t q, 
     }
 }
 
-// Evaluates the 32 queued pairs at ring positions head..head+31 and accumulates them.
-__device__ __noinline__ void flush32(f16k::Smem& s, const uint32_t* queue, uint32_t head, uint32_t lane,
+// Evaluates the 32 queued pairs at ring positions head..head+31 and accumulates them
+// (inlined into the walk: a call there costs its live registers a trip through the stack).
+__device__ __forceinline__ void flush32(f16k::Smem& s, const uint32_t* queue, uint32_t head, uint32_t lane,
                                      const GpuCamera* cam, const GpuLight* lights, const GBufView& gb, uint32_t x0,
                                      uint32_t y0, const PairLog& log) {
     using namespace f16k;
@@ -272,6 +267,27 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
     const uint32_t x0 = bx * TW, y0 = by * TH;
     const hl_froxel_params& fp = grid.fp;
 
+    // the tile's G-buffer texels, loaded before the first barrier so that their latency
+    // overlaps the set-up of shared memory (outside the view: depth 1, sky)
+    uint2 ga[PPT];
+    uint32_t gn[PPT];
+    uint16_t gm[PPT];
+    float gd[PPT];
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+        const uint32_t i = t + k * kThreads;
+        const uint32_t x = x0 + i % TW, y = y0 + i / TW;
+        ga[k] = make_uint2(0u, 0u);
+        gn[k] = 0u;
+        gm[k] = 0u;
+        gd[k] = 1.0f;
+        if (x < gb.width && y < gb.height) {
+            ga[k] = *reinterpret_cast<const uint2*>(gb.plane[0] + gb.pitch[0] * y + 8ull * x);
+            gn[k] = *reinterpret_cast<const uint32_t*>(gb.plane[1] + gb.pitch[1] * y + 4ull * x);
+            gm[k] = *reinterpret_cast<const uint16_t*>(gb.plane[2] + gb.pitch[2] * y + 2ull * x);
+            gd[k] = *reinterpret_cast<const float*>(gb.plane[3] + gb.pitch[3] * y + 4ull * x);
+        }
+    }
     for (uint32_t b = t; b < uint32_t(kBins); b += kThreads) s.u.sort.hist[b] = 0;
     for (uint32_t k = t; k <= fp.grid_z; k += kThreads) s.u.sort.tab[k] = tabz[k];
     // froxel column of each pixel column and row of the tile (x * grid_x < 2^32 for
@@ -301,7 +317,6 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
         s.acc[0][t + k * kThreads] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         s.acc[1][t + k * kThreads] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
-    if (t == 0) s.n_left = 0;
     __syncthreads();
 
     const float camx = cam->position_near[0], camy = cam->position_near[1], camz = cam->position_near[2];
@@ -328,11 +343,11 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
         valid[k] = false;
         key[k] = 0;
         slot[k] = 0;
-        if (x < gb.width && y < gb.height) {
-            const uint2 a = *reinterpret_cast<const uint2*>(gb.plane[0] + gb.pitch[0] * y + 8ull * x);
-            const uint32_t on = *reinterpret_cast<const uint32_t*>(gb.plane[1] + gb.pitch[1] * y + 4ull * x);
-            const uint16_t mt = *reinterpret_cast<const uint16_t*>(gb.plane[2] + gb.pitch[2] * y + 2ull * x);
-            const float depth = *reinterpret_cast<const float*>(gb.plane[3] + gb.pitch[3] * y + 4ull * x);
+        {
+            const uint2 a = ga[k];
+            const uint32_t on = gn[k];
+            const uint16_t mt = gm[k];
+            const float depth = gd[k];
             valid[k] = depth < 1.0f;
             if (valid[k]) {
                 const float ndx = fma_(float(2u * x + 1u), iW, -1.0f);
@@ -355,7 +370,7 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
                                    fmin_(fmax_(metallic_f0(ag, metal), 0.0f), 0.999f),
                                    fmin_(fmax_(metallic_f0(ab, metal), 0.0f), 0.999f),
                                    ndv < kFastMinNdV ? -depth : depth);
-                r.d = make_float4(ar * kInvPi, ag * kInvPi, ab * kInvPi, metal);
+                r.d = make_float4(ar, ag, ab, metal);
                 const float ra = rough * rough, r1 = rough + 1.0f;
                 const float kk = (r1 * r1) * 0.125f;
                 r.b = make_float4(ra * ra, kk, divn_(ndv, fma_(ndv, 1.0f - kk, kk + 0.0001f)), 0.0f);
@@ -370,7 +385,7 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
                 const uint32_t sl = uint32_t(min(max(int(sf), 0), int(fp.grid_z) - 1));
                 const uint32_t fx = s.u.sort.col_of[x - x0];
                 const uint32_t fy = s.u.sort.row_of[y - y0];
-                s.w.walk.fidx[i] = (fy * fp.grid_x + fx) * fp.grid_z + sl;
+                s.w.fidx[i] = (fy * fp.grid_x + fx) * fp.grid_z + sl;
                 // depth sub-bin: the position inside the slice on its logarithmic scale
                 const uint32_t nsub = 1u << kshift;
                 const uint32_t sub = uint32_t(min(max(int((sf - float(sl)) * float(nsub)), 0), int(nsub) - 1));
@@ -381,36 +396,39 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
         }
     }
     __syncthreads();
-    {   // exclusive scan of the key histogram, two bins per thread
-        const uint32_t a = s.u.sort.hist[2 * t], b = s.u.sort.hist[2 * t + 1];
-        uint32_t v = a + b;
+    if (warp == 0) {
+        // exclusive scan of the key histogram by one warp: 16 consecutive bins per lane
+        uint4 h[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) h[m] = reinterpret_cast<const uint4*>(s.u.sort.hist)[lane * 4 + m];
+        uint32_t sum = 0;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) sum += h[m].x + h[m].y + h[m].z + h[m].w;
+        uint32_t inc = sum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t n = __shfl_up_sync(0xffffffffu, v, o);
-            if (lane >= uint32_t(o)) v += n;
+            const uint32_t n = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= uint32_t(o)) inc += n;
         }
-        if (lane == 31) s.warp_tot[warp] = v;
-        __syncthreads();
-        uint32_t before = 0, total = 0;
+        uint32_t run = inc - sum;
 #pragma unroll
-        for (int w = 0; w < kWarps; ++w) {
-            const uint32_t wt = s.warp_tot[w];
-            before += (uint32_t(w) < warp) ? wt : 0u;
-            total += wt;
+        for (int m = 0; m < 4; ++m) {
+            uint4 e;
+            e.x = run; run += h[m].x;
+            e.y = run; run += h[m].y;
+            e.z = run; run += h[m].z;
+            e.w = run; run += h[m].w;
+            reinterpret_cast<uint4*>(s.u.sort.hist)[lane * 4 + m] = e;
         }
-        const uint32_t excl = before + v - (a + b);
-        __syncthreads();
-        s.u.sort.hist[2 * t] = excl;
-        s.u.sort.hist[2 * t + 1] = excl + a;
-        if (t == 0) {
-            s.n_valid = total;
+        if (lane == 31) {
+            s.n_valid = inc;
             s.next_group = 0;
         }
     }
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < PPT; ++k)
-        if (valid[k]) s.w.walk.order[s.u.sort.hist[key[k]] + slot[k]] = uint16_t(t + k * kThreads);
+        if (valid[k]) s.w.order[s.u.sort.hist[key[k]] + slot[k]] = uint16_t(t + k * kThreads);
 
     if (prefetch_next != ~0u) {
         // ask L2 for the G-buffer rows of the tile the next wave will likely take:
@@ -436,6 +454,7 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
     const uint32_t n_valid = s.n_valid;
     uint32_t* queue = s.u.queue[warp];
     uint32_t head = 0, qlen = 0;  // ring position of the oldest pending pair, pending pairs
+    uint32_t mine = 0;            // the groups this warp walked
 #pragma unroll 1
     for (;;) {
         // warps take groups as they finish, last group first: the far slices sort last
@@ -446,16 +465,17 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
         if (g >= uint32_t(NG)) break;
         g = uint32_t(NG - 1) - g;
         if (g * 32u >= n_valid) continue;  // empty group
+        mine |= 1u << g;
         const uint32_t gs = g * 32 + lane;
         const bool own = gs < n_valid;
-        const uint32_t i = own ? s.w.walk.order[gs] : 0u;
+        const uint32_t i = own ? s.w.order[gs] : 0u;
         float px = 0, py = 0, pz = 0, nx = 0, ny = 0, nz = 0;
         uint32_t f = 0xffffffffu, lb = 0, le = 0;
         if (own) {
             const float4 rp = s.rec[i].p, rn = s.rec[i].n;
             px = rp.x; py = rp.y; pz = rp.z;
             nx = rn.x; ny = rn.y; nz = rn.z;
-            f = s.w.walk.fidx[i];
+            f = s.w.fidx[i];
             lb = list_ld<COHERENT>(grid.counts + f);
             le = list_ld<COHERENT>(grid.counts + f + 1);
             if (!(lb <= le && le <= grid.lists_capacity)) {
@@ -527,33 +547,22 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
         }
     }
 
-    // ---- the pairs left in the queues: evaluated together, accumulated by their warp ------
-    __syncthreads();  // every warp has walked: the walk's arrays are free
-    uint32_t base = 0;
-    if (lane == 0 && qlen > 0) base = atomicAdd(&s.n_left, qlen);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (lane < qlen) s.w.tail.left[base + lane] = queue[(head + lane) & (kQueue - 1)];
-    __syncthreads();
-    const uint32_t n_left = s.n_left;
-    for (uint32_t c0 = warp * 32; c0 < n_left; c0 += kThreads) {
-        const bool act = c0 + lane < n_left;
-        const uint32_t e = act ? s.w.tail.left[c0 + lane] : 0u;
+    // ---- the pairs left in the warp's queue, then the warp's own pixels ------------------
+    // Every pair of a pixel is queued, evaluated and accumulated by the warp that walked
+    // its group, so once the warp's queue is empty its pixels are final: no CTA barrier.
+    if (qlen > 0) {
+        const bool act = lane < qlen;
+        const uint32_t e = act ? queue[(head + lane) & (kQueue - 1)] : 0u;
         const uint32_t q = e >> 23, li = e & 0x7fffffu;
         float4 o = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(kCut));
         if (act) o = eval_pair(s, q, li, cam, lights, gb, x0, y0);
-        log_pair(log, act && __float_as_int(o.w) == kLit, lane, x0 + q % TW, y0 + q / TW, gb.width, li);
-        if (act) s.w.tail.res[c0 + lane] = o;
-    }
-    __syncthreads();
-    if (qlen > 0) {
-        const bool act = lane < qlen;
-        const uint32_t e = act ? s.w.tail.left[base + lane] : 0u;
-        const float4 o = act ? s.w.tail.res[base + lane] : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(kCut));
-        accumulate(s, act && __float_as_int(o.w) == kLit, e >> 23, o.x, o.y, o.z);
+        const bool lit = act && __float_as_int(o.w) == kLit;
+        log_pair(log, lit, lane, x0 + q % TW, y0 + q / TW, gb.width, li);
+        accumulate(s, lit, q, o.x, o.y, o.z);
+        __syncwarp();
     }
 
     // ---- 5. output -----------------------------------------------------------------------
-    __syncthreads();
     const uint32_t debug_mode = glb->debug_mode, lcount = glb->light_count;
     // without shadow maps bound, the light-space projection view (mode 11) has no matrix
     if (t == 0 && (glb->has_rc_gi != 0u || (debug_mode == 11u && lcount > 0u)))
@@ -561,15 +570,16 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
     const float amb = glb->ambient_intensity;
     const float skr = glb->ambient_color[0] * amb, skg = glb->ambient_color[1] * amb,
                 skb = glb->ambient_color[2] * amb;
-#pragma unroll
-    for (int k = 0; k < PPT; ++k) {
-        const uint32_t i = t + k * kThreads;
+#pragma unroll 1
+    while (mine) {
+        const uint32_t g = __ffs(mine) - 1;
+        mine &= mine - 1;
+        const uint32_t gs = g * 32 + lane;
+        if (gs >= n_valid) continue;
+        const uint32_t i = s.w.order[gs];
         const uint32_t x = x0 + i % TW, y = y0 + i / TW;
-        if (!valid[k]) continue;
-        // albedo read again from the G-buffer (an L2 hit: the tile was read at set-up)
-        const uint2 alb = *reinterpret_cast<const uint2*>(gb.plane[0] + gb.pitch[0] * y + 8ull * x);
-        const float ar = f16k::h2f(alb.x & 0xffffu), ag = f16k::h2f(alb.x >> 16), ab = f16k::h2f(alb.y & 0xffffu);
-        const float4 rn = s.rec[i].n;
+        const float4 rd = s.rec[i].d, rn = s.rec[i].n;
+        const float ar = rd.x, ag = rd.y, ab = rd.z;
         const float ny = rn.y;
         const float ht = fma_(ny, 0.5f, 0.5f);
         // hemisphere ambient (deferred_lighting.wgsl:1196-1199) times ao (1, white SSAO)
@@ -650,7 +660,8 @@ __global__ void __launch_bounds__(f16k::kThreads, 3) shade_f16_batched_kernel(co
 //
 // CTAs take work items by ticket from a device counter: first the froxel binning items
 // of every view (bin::bin_item, a slice group of one froxel column), then the (view,
-// 32x16 tile) shading items in the plan's order (views with the longest lists first).
+// 32x16 tile) shading items, both in the plan's view order (views with the longest
+// lists first); the work list `tiles` names each ticket's view and item or tile.
 // A shading item waits until every binning item of its view has finished: that view's
 // counter reaches its item count times the launch's epoch. The wait polls with a bound
 // (~0.5 s), after which the item reports HL_ERR_TIMEOUT and is skipped instead of
@@ -706,19 +717,14 @@ __global__ void __launch_bounds__(f16k::kThreads, 3) batch_persistent_kernel(
         __syncthreads();
         const uint32_t tk = s_ticket, epoch = s_epoch;
         if (tk >= total) break;
+        const uint2 it = __ldg(&tiles[tk]);  // (view, binning item) or (view, tile)
         if (tk < total_bin) {
-            uint32_t lo = 0, hi = n_views;  // the view whose items hold tk
-            while (hi - lo > 1) {
-                const uint32_t mid = (lo + hi) / 2;
-                if (__ldg(&bd[mid].item_start) <= tk) lo = mid; else hi = mid;
-            }
-            persistent_bin_item(smem_raw, bd[lo], lights, n_lights, tk - bd[lo].item_start, epoch, chain, status);
+            persistent_bin_item(smem_raw, bd[it.x], lights, n_lights, it.y, epoch, chain, status);
             if (t == 0) {
                 __threadfence();
-                atomicAdd(&view_done[lo], 1u);
+                atomicAdd(&view_done[it.x], 1u);
             }
         } else {
-            const uint2 it = __ldg(&tiles[tk - total_bin]);
             const ShadeViewDesc& v = sd[it.x];
             if (t == 0) {
                 const BinViewDesc& b = bd[it.x];
