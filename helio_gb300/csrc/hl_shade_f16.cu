@@ -49,20 +49,14 @@ constexpr int kQueue = 64;           // per-warp pair ring: at most 31 + 32 pend
 constexpr int kBins = 512;           // keys of the pixel sort
 static_assert(31 + 32 <= kQueue, "pair ring too small");
 
-// Pixel record: five float4 per pixel, so that a lane evaluating a pair of a random
-// pixel reads it with five 16-byte loads (an odd stride of float4: the eight lanes of a
-// shared-memory wavefront that store consecutive pixels hit distinct banks).
-struct Rec {
-    float4 p;   // camera-relative position (f32), 1 / |P| (V = -P / |P|)
-    float4 n;   // unit normal, max(N.V, 0)
-    float4 f0;  // F0 rgb, NDC depth (negative: seen at a grazing angle, every pair precise)
-    float4 d;   // albedo rgb, metallic
-    float4 b;   // roughness^4, (r+1)^2/8, Schlick-GGX of the view, unused
-};
-static_assert(sizeof(Rec) == 80, "pixel record");
-
+// Pixel record: four arrays of 16-byte fields (consecutive pixels on consecutive banks),
+// read by a lane evaluating a pair of a random pixel with four 16-byte loads; the view
+// terms 1 / |P|, roughness^4, (r+1)^2/8 and Schlick-GGX are recomputed from them.
 struct Smem {
-    Rec rec[NPX];
+    float4 P4[NPX];  // camera-relative position (f32), roughness
+    float4 N4[NPX];  // unit normal, max(N.V, 0)
+    float4 F4[NPX];  // F0 rgb, NDC depth (negative: seen at a grazing angle, every pair precise)
+    float4 D4[NPX];  // albedo rgb, metallic
     float4 acc[2][NPX];  // Kahan sum and compensation (rgb)
     union {
         struct {
@@ -82,7 +76,7 @@ struct Smem {
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
-    asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));  // not volatile: the compiler may keep it
     return m;
 }
 
@@ -132,23 +126,25 @@ __device__ __noinline__ float4 precise_f16(const GBufView& gb, uint32_t x, uint3
 __device__ __forceinline__ float4 eval_pair(const f16k::Smem& s, uint32_t q, uint32_t li, const GpuCamera* cam,
                                             const GpuLight* lights, const GBufView& gb, uint32_t x0, uint32_t y0) {
     using namespace f16k;
-    const Rec& r = s.rec[q];
-    const float4 r0 = r.p, r1 = r.n, r2 = r.f0, r3 = r.d, r4 = r.b;
+    const float4 r0 = s.P4[q], r1 = s.N4[q], r2 = s.F4[q], r3 = s.D4[q];
     Pixel p;
     p.Px = r0.x; p.Py = r0.y; p.Pz = r0.z;
     p.Plx = p.Ply = p.Plz = 0.0f;
     p.Nx = r1.x; p.Ny = r1.y; p.Nz = r1.z;
-    p.Vx = -p.Px * r0.w;
-    p.Vy = -p.Py * r0.w;
-    p.Vz = -p.Pz * r0.w;
+    // V = -P / |P| (camera at the origin) and the BRDF's view terms, as the set-up forms them
+    const float iv = rsqrt_(fma_(p.Pz, p.Pz, fma_(p.Py, p.Py, p.Px * p.Px)));
+    p.Vx = -p.Px * iv;
+    p.Vy = -p.Py * iv;
+    p.Vz = -p.Pz * iv;
     p.NdV = r1.w;
     p.f0r = r2.x; p.f0g = r2.y; p.f0b = r2.z;
     p.dr = r3.x * kInvPi; p.dg = r3.y * kInvPi; p.db = r3.z * kInvPi;
+    const float rough = r0.w, ra = rough * rough, r1k = rough + 1.0f;
     PixelBrdf pb;
-    pb.a2 = r4.x;
-    pb.k = r4.y;
+    pb.a2 = ra * ra;
+    pb.k = (r1k * r1k) * 0.125f;
     pb.omk = 1.0f - pb.k;
-    pb.gv = r4.z;
+    pb.gv = divn_(p.NdV, fma_(p.NdV, 1.0f - pb.k, pb.k + 0.0001f));
     pb.one_m_metal = 1.0f - r3.w;
     pb.nv4 = 4.0f * p.NdV;
     pb.vlx = pb.vly = pb.vlz = 0.0f;
@@ -175,10 +171,11 @@ __device__ __forceinline__ float4 eval_pair(const f16k::Smem& s, uint32_t q, uin
 // The walk's test of a candidate pair (pixel at p, normal n; light record a, peak its
 // largest colour channel times intensity): inside the widened range, in front of the
 // surface (|N.t| within sqrt(slack) of zero is left to the exact NdL cut), and not surely
-// below the radiance cut of pbr_direct_light. The radiance bound takes the falloff with
-// the widened range (no smaller than the true one) plus 2^-20 and 2^-8 to spare, so that
-// no rounding of the fast or the precise evaluation reaches 0.002 on a pair it drops:
-// those pairs would be evaluated only to be cut. Directional lights always pass.
+// below the radiance cut of pbr_direct_light. The radiance bound, peak falloff / (d^2 +
+// 1e-4) compared as peak falloff < 0.002 (d^2 + 1e-4), takes the falloff with the
+// widened range (no smaller than the true one) plus 2^-20 and 2^-8 to spare, so that no
+// rounding of the fast or the precise evaluation reaches 0.002 on a pair it drops: those
+// pairs would be evaluated only to be cut. Directional lights always pass.
 __device__ __forceinline__ bool walk_test(float px, float py, float pz, float nx, float ny, float nz, const float4& a,
                                           float peak, float slack) {
     if (a.w < 0.0f) return true;
@@ -186,9 +183,11 @@ __device__ __forceinline__ bool walk_test(float px, float py, float pz, float nx
     const float d2 = fma_(tz, tz, fma_(ty, ty, tx * tx));
     const float ndl = fma_(nz, tz, fma_(ny, ty, nx * tx));
     if (!(d2 <= a.w) || !(ndl > 0.0f || ndl * ndl <= slack)) return false;
-    const float q = d2 * rcpn_(a.w);
-    const float bound = peak * (fmax_(fma_(-q, q, 1.0f), 0.0f) + (1.0f / 1048576.0f)) * rcpn_(d2 + 0.0001f);
-    return !(bound * (1.0f + 1.0f / 256.0f) < kRadianceCut);
+    float q;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(q) : "f"(a.w));  // within 2 ulp: the 2^-20 covers it
+    q *= d2;
+    const float fall = fmax_(fma_(-q, q, 1.0f), 0.0f) + (1.0f / 1048576.0f);
+    return !(peak * fall * (1.0f + 1.0f / 256.0f) < kRadianceCut * (d2 + 0.0001f));
 }
 
 // Records lit pairs for a verifier (hl_set_pair_log); a no-op without a log.
@@ -362,18 +361,14 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
                 const float ndv = fmax_(fma_(nz, -Pz, fma_(ny, -Py, nx * -Px)) * in * iv, 0.0f);
                 const float ar = f16k::h2f(a.x & 0xffffu), ag = f16k::h2f(a.x >> 16), ab = f16k::h2f(a.y & 0xffffu);
                 const float rough = f16k::h2f(a.y >> 16), metal = f16k::h2f(mt);
-                Rec& r = s.rec[i];
-                r.p = make_float4(Px, Py, Pz, iv);
-                r.n = make_float4(nx * in, ny * in, nz * in, ndv);
+                s.P4[i] = make_float4(Px, Py, Pz, rough);
+                s.N4[i] = make_float4(nx * in, ny * in, nz * in, ndv);
                 // grazing view: every pair of the pixel goes to the precise evaluation
-                r.f0 = make_float4(fmin_(fmax_(metallic_f0(ar, metal), 0.0f), 0.999f),
-                                   fmin_(fmax_(metallic_f0(ag, metal), 0.0f), 0.999f),
-                                   fmin_(fmax_(metallic_f0(ab, metal), 0.0f), 0.999f),
-                                   ndv < kFastMinNdV ? -depth : depth);
-                r.d = make_float4(ar, ag, ab, metal);
-                const float ra = rough * rough, r1 = rough + 1.0f;
-                const float kk = (r1 * r1) * 0.125f;
-                r.b = make_float4(ra * ra, kk, divn_(ndv, fma_(ndv, 1.0f - kk, kk + 0.0001f)), 0.0f);
+                s.F4[i] = make_float4(fmin_(fmax_(metallic_f0(ar, metal), 0.0f), 0.999f),
+                                      fmin_(fmax_(metallic_f0(ag, metal), 0.0f), 0.999f),
+                                      fmin_(fmax_(metallic_f0(ab, metal), 0.0f), 0.999f),
+                                      ndv < kFastMinNdV ? -depth : depth);
+                s.D4[i] = make_float4(ar, ag, ab, metal);
                 // own froxel: column of (x, y), slice of the linear view depth (the lists
                 // are conservative by 2^-10 of the slice depth, so the slice only needs
                 // the depth to a few ulp)
@@ -472,7 +467,7 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
         float px = 0, py = 0, pz = 0, nx = 0, ny = 0, nz = 0;
         uint32_t f = 0xffffffffu, lb = 0, le = 0;
         if (own) {
-            const float4 rp = s.rec[i].p, rn = s.rec[i].n;
+            const float4 rp = s.P4[i], rn = s.N4[i];
             px = rp.x; py = rp.y; pz = rp.z;
             nx = rn.x; ny = rn.y; nz = rn.z;
             f = s.w.fidx[i];
@@ -578,7 +573,7 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
         if (gs >= n_valid) continue;
         const uint32_t i = s.w.order[gs];
         const uint32_t x = x0 + i % TW, y = y0 + i / TW;
-        const float4 rd = s.rec[i].d, rn = s.rec[i].n;
+        const float4 rd = s.D4[i], rn = s.N4[i];
         const float ar = rd.x, ag = rd.y, ab = rd.z;
         const float ny = rn.y;
         const float ht = fma_(ny, 0.5f, 0.5f);
