@@ -480,27 +480,34 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
         }
         // |N.t| within |P| 2^-20 of zero is left to the exact NdL cut
         const float slack = fma_(pz, pz, fma_(py, py, px * px)) * (1.0f / 1099511627776.0f);
+        const int ox = f2o(px), oy = f2o(py), oz = f2o(pz);  // for the box reductions
 #pragma unroll 1
         for (uint32_t c0 = 0;; c0 += 32) {
             const bool act = own && lb + c0 < le;
             uint32_t pending = __ballot_sync(0xffffffffu, act);
             if (!pending) break;
             // A: per froxel of the group, the 32 list entries from c0 on, culled against the
-            // bounding box of the group's pixels in that froxel
+            // bounding box of the group's pixels in that froxel (a chunk of at most four
+            // entries goes to the walk as it is: its box would cost more than it saves)
             uint32_t smask = 0;
             while (pending) {
                 const uint32_t leader = __ffs(pending) - 1;
                 const uint32_t fk = __shfl_sync(0xffffffffu, f, leader);
                 const bool mine = act && f == fk;
                 pending &= ~__ballot_sync(0xffffffffu, mine);
-                const float b0x = o2f(__reduce_min_sync(0xffffffffu, mine ? f2o(px) : 0x7fffffff));
-                const float b0y = o2f(__reduce_min_sync(0xffffffffu, mine ? f2o(py) : 0x7fffffff));
-                const float b0z = o2f(__reduce_min_sync(0xffffffffu, mine ? f2o(pz) : 0x7fffffff));
-                const float b1x = o2f(__reduce_max_sync(0xffffffffu, mine ? f2o(px) : int(0x80000000)));
-                const float b1y = o2f(__reduce_max_sync(0xffffffffu, mine ? f2o(py) : int(0x80000000)));
-                const float b1z = o2f(__reduce_max_sync(0xffffffffu, mine ? f2o(pz) : int(0x80000000)));
                 const uint32_t j = __shfl_sync(0xffffffffu, lb, leader) + c0 + lane;
                 const uint32_t je = __shfl_sync(0xffffffffu, le, leader);
+                if (je - (j - lane) <= 4u) {
+                    const uint32_t m = __ballot_sync(0xffffffffu, j < je);
+                    if (mine) smask = m;
+                    continue;
+                }
+                const float b0x = o2f(__reduce_min_sync(0xffffffffu, mine ? ox : 0x7fffffff));
+                const float b0y = o2f(__reduce_min_sync(0xffffffffu, mine ? oy : 0x7fffffff));
+                const float b0z = o2f(__reduce_min_sync(0xffffffffu, mine ? oz : 0x7fffffff));
+                const float b1x = o2f(__reduce_max_sync(0xffffffffu, mine ? ox : int(0x80000000)));
+                const float b1y = o2f(__reduce_max_sync(0xffffffffu, mine ? oy : int(0x80000000)));
+                const float b1z = o2f(__reduce_max_sync(0xffffffffu, mine ? oz : int(0x80000000)));
                 const uint32_t lj = j < je ? list_ld<COHERENT>(grid.lists + j) : 0xffffffffu;
                 const bool ok = lj < n_lights;
                 if (j < je && !ok) raise_status(status, HL_ERR_DEVICE_BOUNDS);
@@ -508,9 +515,9 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
                 // the per-pixel test's operations on the box-clamped differences: for a pixel
                 // in the box each |difference| rounds no smaller, so a light the box rejects
                 // fails the range test at every pixel of the box
-                const float dx = fmax_(fmax_(b0x - c.x, c.x - b1x), 0.0f);
-                const float dy = fmax_(fmax_(b0y - c.y, c.y - b1y), 0.0f);
-                const float dz = fmax_(fmax_(b0z - c.z, c.z - b1z), 0.0f);
+                const float dx = fmaxf(fmaxf(b0x - c.x, c.x - b1x), 0.0f);  // no NaN here: box and
+                const float dy = fmaxf(fmaxf(b0y - c.y, c.y - b1y), 0.0f);  // record are finite
+                const float dz = fmaxf(fmaxf(b0z - c.z, c.z - b1z), 0.0f);
                 const bool keep = ok && (c.w < 0.0f || fma_(dz, dz, fma_(dy, dy, dx * dx)) <= c.w);
                 const uint32_t m = __ballot_sync(0xffffffffu, keep);
                 if (mine) smask = m;
@@ -525,9 +532,13 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
                     const uint32_t bit = __ffs(smask) - 1;
                     smask &= smask - 1;
                     li = list_ld<COHERENT>(grid.lists + cb + bit);
-                    const float4 a = __ldg(cand + li);
-                    const float peak = __ldg(reinterpret_cast<const float*>(cand + n_lights) + li);
-                    pass = walk_test(px, py, pz, nx, ny, nz, a, peak, slack);
+                    if (li < n_lights) {  // (entries of short chunks reach here unchecked)
+                        const float4 a = __ldg(cand + li);
+                        const float peak = __ldg(reinterpret_cast<const float*>(cand + n_lights) + li);
+                        pass = walk_test(px, py, pz, nx, ny, nz, a, peak, slack);
+                    } else {
+                        raise_status(status, HL_ERR_DEVICE_BOUNDS);
+                    }
                 }
                 const uint32_t pm = __ballot_sync(0xffffffffu, pass);
                 if (pass) queue[(head + qlen + __popc(pm & lanemask_lt())) & (kQueue - 1)] = (i << 23) | li;

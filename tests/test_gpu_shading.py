@@ -183,6 +183,36 @@ def test_shade_rejects_bad_arguments(ctx):
     assert e.value.status == N.HL_ERR_INVALID_ARGUMENT
 
 
+def test_fp16_froxel_out_of_range_light_index_is_reported(ctx):
+    """FP16 G-buffer over froxel lists: an entry beyond n_lights, in a list of at most four
+    entries (walked without the box cull) and in a long one, is skipped and reported
+    (HL_ERR_DEVICE_BOUNDS), never read; the other pixels are unaffected."""
+    import torch
+
+    w = S.workload(1, scale=0.25)
+    gb, cam = w.gbuffer, w.camera
+    p = L.froxel_params(*w.froxel_grid, gb.width, gb.height, cam.far)
+    off, idx = oracle.bin_froxels(cam.record, w.lights, p, capacity=1 << 24)
+    lens = np.diff(off.astype(np.int64))
+    short = int(np.flatnonzero((lens >= 1) & (lens <= 4))[0])
+    long_ = int(np.argmax(lens))
+    assert lens[long_] > 4
+    bad = idx.copy()
+    bad[off[short]] = 10_000_000
+    bad[off[long_] + lens[long_] // 2] = 10_000_000
+    df = FR.upload(cam.record, w.globals_, w.lights, gb)
+    doff = torch.from_numpy(off.view(np.int32).copy()).cuda()
+    didx = torch.from_numpy(bad.view(np.int32).copy()).cuda()
+    grid = N.froxel_grid_struct(didx, doff, N.froxel_params_from_numpy(p), didx.numel())
+    out = torch.zeros((gb.height, gb.width, 4), dtype=torch.float32, device="cuda")
+    ctx.shade(df.camera, df.globals_, df.gbuffer, df.lights, df.n_lights, grid, N.target_struct(out))
+    with pytest.raises(N.HelioError) as e:
+        ctx.sync_status()
+    assert e.value.status == N.HL_ERR_DEVICE_BOUNDS
+    ctx.sync_status()  # cleared
+    assert np.isfinite(out.cpu().numpy()).all()
+
+
 def test_shade_out_of_range_light_index_is_reported(ctx):
     """A list entry beyond n_lights is skipped and reported, never read."""
     import torch
