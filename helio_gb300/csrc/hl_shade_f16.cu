@@ -124,7 +124,8 @@ __device__ __noinline__ float4 precise_f16(const GBufView& gb, uint32_t x, uint3
 // fast path, handed to precise_f16 when the guard flags it or the pixel is grazing.
 // Returns (r, g, b) and the status in w.
 __device__ __forceinline__ float4 eval_pair(const f16k::Smem& s, uint32_t q, uint32_t li, const GpuCamera* cam,
-                                            const GpuLight* lights, const GBufView& gb, uint32_t x0, uint32_t y0) {
+                                            const float3& camp, const GpuLight* lights, const GBufView& gb,
+                                            uint32_t x0, uint32_t y0) {
     using namespace f16k;
     const float4 r0 = s.P4[q], r1 = s.N4[q], r2 = s.F4[q], r3 = s.D4[q];
     Pixel p;
@@ -152,9 +153,9 @@ __device__ __forceinline__ float4 eval_pair(const f16k::Smem& s, uint32_t q, uin
     const float4 a = __ldg(gl + 0), b = __ldg(gl + 1), c = __ldg(gl + 2);
     const uint4 d = __ldg(reinterpret_cast<const uint4*>(gl + 3));
     ShadeLight l;
-    l.px = a.x - cam->position_near[0];  // camera-relative light position (high word of its two-sum)
-    l.py = a.y - cam->position_near[1];
-    l.pz = a.z - cam->position_near[2];
+    l.px = a.x - camp.x;  // camera-relative light position (high word of its two-sum)
+    l.py = a.y - camp.y;
+    l.pz = a.z - camp.z;
     l.range = a.w;
     l.dx = b.x; l.dy = b.y; l.dz = b.z; l.cos_outer = b.w;
     l.cr = c.x; l.cg = c.y; l.cb = c.z; l.intensity = c.w;
@@ -226,12 +227,12 @@ __device__ __forceinline__ void accumulate(f16k::Smem& s, bool lit, uint32_t q, 
 // Evaluates the 32 queued pairs at ring positions head..head+31 and accumulates them
 // (inlined into the walk: a call there costs its live registers a trip through the stack).
 __device__ __forceinline__ void flush32(f16k::Smem& s, const uint32_t* queue, uint32_t head, uint32_t lane,
-                                     const GpuCamera* cam, const GpuLight* lights, const GBufView& gb, uint32_t x0,
-                                     uint32_t y0, const PairLog& log) {
+                                     const GpuCamera* cam, const float3& camp, const GpuLight* lights,
+                                     const GBufView& gb, uint32_t x0, uint32_t y0, const PairLog& log) {
     using namespace f16k;
     const uint32_t e = queue[(head + lane) & (kQueue - 1)];
     const uint32_t q = e >> 23, li = e & 0x7fffffu;
-    const float4 o = eval_pair(s, q, li, cam, lights, gb, x0, y0);
+    const float4 o = eval_pair(s, q, li, cam, camp, lights, gb, x0, y0);
     const bool lit = __float_as_int(o.w) == kLit;
     log_pair(log, lit, lane, x0 + q % TW, y0 + q / TW, gb.width, li);
     accumulate(s, lit, q, o.x, o.y, o.z);
@@ -319,6 +320,7 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
     __syncthreads();
 
     const float camx = cam->position_near[0], camy = cam->position_near[1], camz = cam->position_near[2];
+    const float3 camp = make_float3(camx, camy, camz);  // kept in registers for the pair evaluations
     const float W = float(gb.width), H = float(gb.height);
     // slices are exponential from slice_near to tab[grid_z]: slice ~ log2(d / near) * scale
     const float slice_inv_near = rcpn_(fp.slice_near);
@@ -545,7 +547,7 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
                 qlen += __popc(pm);
                 __syncwarp();
                 if (qlen >= 32) {
-                    flush32(s, queue, head, lane, cam, lights, gb, x0, y0, log);
+                    flush32(s, queue, head, lane, cam, camp, lights, gb, x0, y0, log);
                     head += 32;
                     qlen -= 32;
                 }
@@ -561,7 +563,7 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
         const uint32_t e = act ? queue[(head + lane) & (kQueue - 1)] : 0u;
         const uint32_t q = e >> 23, li = e & 0x7fffffu;
         float4 o = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(kCut));
-        if (act) o = eval_pair(s, q, li, cam, lights, gb, x0, y0);
+        if (act) o = eval_pair(s, q, li, cam, camp, lights, gb, x0, y0);
         const bool lit = act && __float_as_int(o.w) == kLit;
         log_pair(log, lit, lane, x0 + q % TW, y0 + q / TW, gb.width, li);
         accumulate(s, lit, q, o.x, o.y, o.z);
