@@ -160,9 +160,10 @@ __device__ __forceinline__ void load_pixel(const Smem<NPX, NF>& s, int i, Pixel&
 }  // namespace sk
 
 // Evaluates nb queued pairs (ring positions head..head+nb-1), one per lane, and adds
-// them into the per-pixel Kahan accumulators in queue order.
+// them into the per-pixel Kahan accumulators in queue order. Out of line so that the
+// BRDF code exists once in the kernel.
 template <uint32_t LAYOUT, bool STATS, int TW, int NPX, bool EXT>
-__device__ __forceinline__ void flush_batch_body(sk::Smem<NPX, sk::record_fields<LAYOUT>()>& s, const uint32_t* queue, uint32_t head, uint32_t nb,
+__device__ __noinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>()>& s, const uint32_t* queue, uint32_t head, uint32_t nb,
                                          uint32_t lane, const GpuCamera* cam, const GpuLight* lights, uint32_t x0,
                                          uint32_t y0, float W, float H, const ExtView* sv, const PairLog log) {
     using namespace sk;
@@ -254,25 +255,6 @@ __device__ __forceinline__ void flush_batch_body(sk::Smem<NPX, sk::record_fields
         }
     }
     __syncwarp();
-}
-
-// Out of line for the extended variant (shadow term, RC GI), whose pair evaluation is too
-// large to inline into the walk without spilling; inline for the others.
-template <uint32_t LAYOUT, bool STATS, int TW, int NPX, bool EXT>
-__device__ __noinline__ void flush_batch_ool(sk::Smem<NPX, sk::record_fields<LAYOUT>()>& s, const uint32_t* queue, uint32_t head, uint32_t nb,
-                                         uint32_t lane, const GpuCamera* cam, const GpuLight* lights, uint32_t x0,
-                                         uint32_t y0, float W, float H, const ExtView* sv, const PairLog log) {
-    flush_batch_body<LAYOUT, STATS, TW, NPX, EXT>(s, queue, head, nb, lane, cam, lights, x0, y0, W, H, sv, log);
-}
-
-template <uint32_t LAYOUT, bool STATS, int TW, int NPX, bool EXT>
-__device__ __forceinline__ void flush_batch(sk::Smem<NPX, sk::record_fields<LAYOUT>()>& s, const uint32_t* queue, uint32_t head, uint32_t nb,
-                                         uint32_t lane, const GpuCamera* cam, const GpuLight* lights, uint32_t x0,
-                                         uint32_t y0, float W, float H, const ExtView* sv, const PairLog log) {
-    if constexpr (EXT)
-        flush_batch_ool<LAYOUT, STATS, TW, NPX, EXT>(s, queue, head, nb, lane, cam, lights, x0, y0, W, H, sv, log);
-    else
-        flush_batch_body<LAYOUT, STATS, TW, NPX, EXT>(s, queue, head, nb, lane, cam, lights, x0, y0, W, H, sv, log);
 }
 
 // Light-space projection view of shadow debug mode 11 (deferred_lighting.wgsl:1066-1080):
