@@ -80,12 +80,19 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
-// Order-preserving map of f32 to s32 (for warp min/max reductions of coordinates).
-__device__ __forceinline__ int f2o(float v) {
-    const int k = __float_as_int(v);
-    return k ^ ((k >> 31) & 0x7fffffff);
+
+// Warp minimum / maximum of f32 values (redux.sync on f32, sm_100 and later); the values
+// here are finite, and a lane outside the set passes +inf / -inf.
+__device__ __forceinline__ float warp_min(float v) {
+    float r;
+    asm volatile("redux.sync.min.f32 %0, %1, 0xffffffff;" : "=f"(r) : "f"(v));
+    return r;
 }
-__device__ __forceinline__ float o2f(int k) { return __int_as_float(k ^ ((k >> 31) & 0x7fffffff)); }
+__device__ __forceinline__ float warp_max(float v) {
+    float r;
+    asm volatile("redux.sync.max.f32 %0, %1, 0xffffffff;" : "=f"(r) : "f"(v));
+    return r;
+}
 
 __device__ __forceinline__ float h2f(uint32_t bits16) { return __half2float(__ushort_as_half(uint16_t(bits16))); }
 
@@ -482,7 +489,6 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
         }
         // |N.t| within |P| 2^-20 of zero is left to the exact NdL cut
         const float slack = fma_(pz, pz, fma_(py, py, px * px)) * (1.0f / 1099511627776.0f);
-        const int ox = f2o(px), oy = f2o(py), oz = f2o(pz);  // for the box reductions
 #pragma unroll 1
         for (uint32_t c0 = 0;; c0 += 32) {
             const bool act = own && lb + c0 < le;
@@ -504,12 +510,11 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
                     if (mine) smask = m;
                     continue;
                 }
-                const float b0x = o2f(__reduce_min_sync(0xffffffffu, mine ? ox : 0x7fffffff));
-                const float b0y = o2f(__reduce_min_sync(0xffffffffu, mine ? oy : 0x7fffffff));
-                const float b0z = o2f(__reduce_min_sync(0xffffffffu, mine ? oz : 0x7fffffff));
-                const float b1x = o2f(__reduce_max_sync(0xffffffffu, mine ? ox : int(0x80000000)));
-                const float b1y = o2f(__reduce_max_sync(0xffffffffu, mine ? oy : int(0x80000000)));
-                const float b1z = o2f(__reduce_max_sync(0xffffffffu, mine ? oz : int(0x80000000)));
+                const float inf = __int_as_float(0x7f800000);
+                const float b0x = warp_min(mine ? px : inf), b0y = warp_min(mine ? py : inf),
+                            b0z = warp_min(mine ? pz : inf);
+                const float b1x = warp_max(mine ? px : -inf), b1y = warp_max(mine ? py : -inf),
+                            b1z = warp_max(mine ? pz : -inf);
                 const uint32_t lj = j < je ? list_ld<COHERENT>(grid.lists + j) : 0xffffffffu;
                 const bool ok = lj < n_lights;
                 if (j < je && !ok) raise_status(status, HL_ERR_DEVICE_BOUNDS);
