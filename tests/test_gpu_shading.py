@@ -89,6 +89,19 @@ def test_shade_4k_clumped(ctx):
     _check(ctx, w.camera.record, w.globals_, w.lights, w.gbuffer, w.froxel_grid, "froxels", TOL[S.LAYOUT_F32])
 
 
+def test_shade_fp16_clumped_long_lists(ctx):
+    """The FP16 kernel over froxel lists of hundreds of entries (the clumped 4096-light
+    workload's lights and grid at 1920x1080 on an FP16 G-buffer): several 32-entry chunks
+    per froxel, culls and pair flushes under load; FP64 oracle with the kernel's own
+    branch decisions."""
+    w = S.workload(2, scale=0.5)
+    gb = S.make_gbuffer(w.camera, S.LAYOUT_F16, seed=2000)
+    p = L.froxel_params(*w.froxel_grid, gb.width, gb.height, w.camera.far)
+    off, _ = oracle.bin_froxels(w.camera.record, w.lights, p, capacity=1 << 26)
+    assert np.diff(off.astype(np.int64)).max() > 96
+    _check(ctx, w.camera.record, w.globals_, w.lights, gb, w.froxel_grid, "froxels", TOL[S.LAYOUT_F16])
+
+
 @pytest.mark.parametrize("layout", [S.LAYOUT_REFERENCE, S.LAYOUT_F32, S.LAYOUT_F16])
 def test_shade_mixed_lights_with_ambient(ctx, layout):
     W, H = 480, 272
