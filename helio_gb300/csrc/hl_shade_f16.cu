@@ -80,7 +80,6 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
-
 // Warp minimum / maximum of f32 values (redux.sync on f32, sm_100 and later); the values
 // here are finite, and a lane outside the set passes +inf / -inf.
 __device__ __forceinline__ float warp_min(float v) {
