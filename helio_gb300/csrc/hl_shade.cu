@@ -314,6 +314,18 @@ __device__ __forceinline__ void shade_tile(
     const float W = float(gb.width), H = float(gb.height);
     const float camx = cam->position_near[0], camy = cam->position_near[1], camz = cam->position_near[2];
 
+    // the tile's G-buffer texels, loaded before the first barrier so that their latency
+    // overlaps the set-up of shared memory; decoded in the set-up loop
+    gbuf::RawTexel raw[PPT];
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+        const uint32_t i = t + k * kThreads;
+        const uint32_t x = x0 + i % TW, y = y0 + i / TW;
+        raw[k] = gbuf::RawTexel{};
+        raw[k].depth = 1.0f;
+        if (x < gb.width && y < gb.height) raw[k] = gbuf::load_raw<LAYOUT>(gb, x, y);
+    }
+
     for (uint32_t b = t; b < uint32_t(kBins); b += kThreads) s.u.sort.hist[b] = 0;
     if (FROXELS) {
         for (uint32_t k = t; k <= grid.fp.grid_z; k += kThreads) s.u.sort.tab[k] = tabz[k];
@@ -373,7 +385,7 @@ __device__ __forceinline__ void shade_tile(
         key[k] = 0;
         slot[k] = 0;
         if (x < gb.width && y < gb.height) {
-            const Texel<LAYOUT> tx = load_texel<LAYOUT>(gb, x, y);
+            const Texel<LAYOUT> tx = gbuf::decode_texel<LAYOUT>(raw[k]);
             valid[k] = tx.depth < 1.0f;
             if (valid[k]) {
                 Pixel p;
