@@ -67,20 +67,19 @@ __device__ __forceinline__ Texel<LAYOUT> decode_texel(const RawTexel& r) {
     Texel<LAYOUT> t;
     t.depth = r.depth;
     if (LAYOUT == HL_GBUF_REFERENCE) {
-        const uchar4 a = *reinterpret_cast<const uchar4*>(&r.a.x);
-        const uchar4 o = *reinterpret_cast<const uchar4*>(&r.o.x);
-        t.ar = div_(float(a.x), 255.0f);
-        t.ag = div_(float(a.y), 255.0f);
-        t.ab = div_(float(a.z), 255.0f);
-        t.alpha = div_(float(a.w), 255.0f);
+        // RGBA8 bytes in memory order: x in the low byte
+        t.ar = div_(float(r.a.x & 0xffu), 255.0f);
+        t.ag = div_(float((r.a.x >> 8) & 0xffu), 255.0f);
+        t.ab = div_(float((r.a.x >> 16) & 0xffu), 255.0f);
+        t.alpha = div_(float(r.a.x >> 24), 255.0f);
         t.nx = h2f(uint16_t(r.n.x & 0xffffu));
         t.ny = h2f(uint16_t(r.n.x >> 16));
         t.nz = h2f(uint16_t(r.n.y & 0xffffu));
         t.f0r = h2f(uint16_t(r.n.y >> 16));
-        t.ao = div_(float(o.x), 255.0f);
-        t.rough = div_(float(o.y), 255.0f);
-        t.metal = div_(float(o.z), 255.0f);
-        t.f0g = div_(float(o.w), 255.0f);
+        t.ao = div_(float(r.o.x & 0xffu), 255.0f);
+        t.rough = div_(float((r.o.x >> 8) & 0xffu), 255.0f);
+        t.metal = div_(float((r.o.x >> 16) & 0xffu), 255.0f);
+        t.f0g = div_(float(r.o.x >> 24), 255.0f);
         t.er = h2f(uint16_t(r.e.x & 0xffffu));
         t.eg = h2f(uint16_t(r.e.x >> 16));
         t.eb = h2f(uint16_t(r.e.y & 0xffffu));
@@ -113,9 +112,67 @@ __device__ __forceinline__ Texel<LAYOUT> decode_texel(const RawTexel& r) {
     return t;
 }
 
+// Loads and decodes in one step (the same values as decode_texel(load_raw(...)); the
+// kernels that read their texel among other loads keep this form, whose code the compiler
+// schedules with theirs).
 template <uint32_t LAYOUT>
 __device__ __forceinline__ Texel<LAYOUT> load_texel(const GBufView& g, uint32_t x, uint32_t y) {
-    return decode_texel<LAYOUT>(load_raw<LAYOUT>(g, x, y));
+    Texel<LAYOUT> t;
+    if (LAYOUT == HL_GBUF_REFERENCE) {
+        const uchar4 a = *reinterpret_cast<const uchar4*>(g.plane[0] + g.pitch[0] * y + 4ull * x);
+        const uint2 nr = *reinterpret_cast<const uint2*>(g.plane[1] + g.pitch[1] * y + 8ull * x);
+        const uchar4 o = *reinterpret_cast<const uchar4*>(g.plane[2] + g.pitch[2] * y + 4ull * x);
+        const uint2 e = *reinterpret_cast<const uint2*>(g.plane[3] + g.pitch[3] * y + 8ull * x);
+        t.depth = *reinterpret_cast<const float*>(g.plane[4] + g.pitch[4] * y + 4ull * x);
+        t.ar = div_(float(a.x), 255.0f);
+        t.ag = div_(float(a.y), 255.0f);
+        t.ab = div_(float(a.z), 255.0f);
+        t.alpha = div_(float(a.w), 255.0f);
+        t.nx = h2f(uint16_t(nr.x & 0xffffu));
+        t.ny = h2f(uint16_t(nr.x >> 16));
+        t.nz = h2f(uint16_t(nr.y & 0xffffu));
+        t.f0r = h2f(uint16_t(nr.y >> 16));
+        t.ao = div_(float(o.x), 255.0f);
+        t.rough = div_(float(o.y), 255.0f);
+        t.metal = div_(float(o.z), 255.0f);
+        t.f0g = div_(float(o.w), 255.0f);
+        t.er = h2f(uint16_t(e.x & 0xffffu));
+        t.eg = h2f(uint16_t(e.x >> 16));
+        t.eb = h2f(uint16_t(e.y & 0xffffu));
+        t.f0b = h2f(uint16_t(e.y >> 16));
+    } else if (LAYOUT == HL_GBUF_F32) {
+        const float4 a = *reinterpret_cast<const float4*>(g.plane[0] + g.pitch[0] * y + 16ull * x);
+        const float4 n = *reinterpret_cast<const float4*>(g.plane[1] + g.pitch[1] * y + 16ull * x);
+        t.depth = *reinterpret_cast<const float*>(g.plane[2] + g.pitch[2] * y + 4ull * x);
+        t.ar = a.x;
+        t.ag = a.y;
+        t.ab = a.z;
+        t.rough = a.w;
+        t.nx = n.x;
+        t.ny = n.y;
+        t.nz = n.z;
+        t.metal = n.w;
+    } else {
+        const uint2 a = *reinterpret_cast<const uint2*>(g.plane[0] + g.pitch[0] * y + 8ull * x);
+        const uint32_t on = *reinterpret_cast<const uint32_t*>(g.plane[1] + g.pitch[1] * y + 4ull * x);
+        const uint16_t m = *reinterpret_cast<const uint16_t*>(g.plane[2] + g.pitch[2] * y + 2ull * x);
+        t.depth = *reinterpret_cast<const float*>(g.plane[3] + g.pitch[3] * y + 4ull * x);
+        t.ar = h2f(uint16_t(a.x & 0xffffu));
+        t.ag = h2f(uint16_t(a.x >> 16));
+        t.ab = h2f(uint16_t(a.y & 0xffffu));
+        t.rough = h2f(uint16_t(a.y >> 16));
+        oct_decode(h2f(uint16_t(on & 0xffffu)), h2f(uint16_t(on >> 16)), t.nx, t.ny, t.nz);
+        t.metal = h2f(m);
+    }
+    if (LAYOUT != HL_GBUF_REFERENCE) {
+        t.alpha = 1.0f;
+        t.ao = 1.0f;
+        t.er = t.eg = t.eb = 0.0f;
+        t.f0r = metallic_f0(t.ar, t.metal);
+        t.f0g = metallic_f0(t.ag, t.metal);
+        t.f0b = metallic_f0(t.ab, t.metal);
+    }
+    return t;
 }
 
 // Planes of each layout and their bytes per texel.
