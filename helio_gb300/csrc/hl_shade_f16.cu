@@ -3,19 +3,20 @@
 //
 // One CTA of 256 threads lights a 32x16-pixel tile:
 //  1. threads load the tile's G-buffer texels (coalesced along x) first and set each pixel
-//     up into a shared-memory record: camera-relative position, unit normal, NdV, F0,
-//     albedo and the view's BRDF constants, with its froxel;
+//     up into a shared-memory record: camera-relative position, roughness, unit normal,
+//     NdV, F0, albedo, metallic, with its froxel;
 //  2. pixels are counting-sorted by froxel and, inside a froxel, by a depth sub-bin of
 //     its slice, so that a group of 32 consecutive sorted pixels spans one froxel (or
 //     a few of adjacent slices) and a narrow depth range;
 //  3. a warp takes a group. For each froxel of the group it culls the froxel's list
 //     against the bounding box of the group's pixels in that froxel (lanes test 32
-//     lights at once), and each of those pixels keeps the survivors as a bit mask. Then
-//     every lane walks its own mask, testing its pixel against each surviving light for
-//     range and the NdL sign. The box test applies the per-pixel test's own f32
-//     operations to box-clamped differences, so every pair the per-pixel test passes
-//     survives it: the queued pairs are exactly those of a walk over the pixel's whole
-//     list, in list order;
+//     lights at once; a chunk of at most four entries is kept whole), and each of those
+//     pixels keeps the survivors as a bit mask. Then every lane walks its own mask,
+//     testing its pixel against each surviving light for range, the NdL sign and a
+//     conservative bound of the radiance against the 0.002 cut (walk_test). The box test
+//     applies the per-pixel range test's own f32 operations to box-clamped differences,
+//     so every pair the per-pixel test passes survives it: the queued pairs are exactly
+//     those of walk_test over the pixel's whole list, in list order;
 //  4. queued (pixel, light) pairs are evaluated 32 at a time, one per lane, and added
 //     into per-pixel Kahan accumulators in queue order, which is list order for every
 //     pixel, as the reference's light loop (deferred_lighting.wgsl:1119-1146) adds them;
