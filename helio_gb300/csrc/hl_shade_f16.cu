@@ -50,6 +50,9 @@ constexpr int kQueue = 64;           // per-warp pair ring: at most 31 + 32 pend
 constexpr int kBins = 512;           // keys of the pixel sort
 static_assert(31 + 32 <= kQueue, "pair ring too small");
 
+// Shared memory of a tile: 54.4 KB, so that three CTAs fit the 164 KB shared-memory
+// configuration of an SM and leave 92 KB to L1 (the lists, the candidate table and the
+// lights are read through it); 16 bytes more would need the 196 KB one.
 // Pixel record: four arrays of 16-byte fields (consecutive pixels on consecutive banks),
 // read by a lane evaluating a pair of a random pixel with four 16-byte loads; the view
 // terms 1 / |P|, roughness^4, (r+1)^2/8 and Schlick-GGX are recomputed from them.
@@ -62,7 +65,6 @@ struct Smem {
     union {
         struct {
             uint32_t hist[kBins];
-            float tab[kMaxSlices + 1];
             uint16_t col_of[TW], row_of[TH];
         } sort;
         uint32_t queue[kWarps][kQueue];  // walk: ring of (pixel << 23) | light index
@@ -74,6 +76,8 @@ struct Smem {
     uint32_t n_valid, next_group;
     uint32_t fx0, fy0, ncx, ncols, kshift, by_column;
 };
+// three CTAs (with the 1 KB each that the driver reserves, in 128-byte steps) in 164 KB
+static_assert(((sizeof(Smem) + 1024 + 127) / 128) * 128 * 3 <= 164 * 1024, "tile no longer fits 3 CTAs in 164 KB");
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
@@ -296,7 +300,6 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
         }
     }
     for (uint32_t b = t; b < uint32_t(kBins); b += kThreads) s.u.sort.hist[b] = 0;
-    for (uint32_t k = t; k <= fp.grid_z; k += kThreads) s.u.sort.tab[k] = tabz[k];
     // froxel column of each pixel column and row of the tile (x * grid_x < 2^32 for
     // viewports of at most 65536 pixels per side)
     if (t < uint32_t(TW)) {
@@ -332,7 +335,7 @@ __device__ __forceinline__ void shade_tile_f16(f16k::Smem& s, const GpuCamera* _
     // slices are exponential from slice_near to tab[grid_z]: slice ~ log2(d / near) * scale
     const float slice_inv_near = rcpn_(fp.slice_near);
     const float slice_scale =
-        float(fp.grid_z) * rcpn_(__log2f(fmaxf(s.u.sort.tab[fp.grid_z] * slice_inv_near, 2.0f)));
+        float(fp.grid_z) * rcpn_(__log2f(fmaxf(__ldg(tabz + fp.grid_z) * slice_inv_near, 2.0f)));
     const float nr = cam->position_near[3], fr = cam->forward_far[3];
     const float nrfr = nr * fr, frmnr = fr - nr;
     const uint32_t fx0 = s.fx0, fy0 = s.fy0, ncx = s.ncx, ncols = s.ncols, kshift = s.kshift;
